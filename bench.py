@@ -1,0 +1,401 @@
+"""Benchmark of the level-set transport step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload: the curvilinear solitary-wave case, 256 x 128 x 96 nodes
+(x = 8 xi + 0.05 sin(2 pi eta), y = 2 eta, z = zeta^1.3), phi0 redistanced by
+50 reinitialisation pseudo-steps, uniform flow plus the solitary-wave
+perturbation, CFL 0.4, WENO3 + TVD-RK3, 10 reinitialisation pseudo-steps per
+physical step, 6-cell narrow band: one `levelsetmethod` call per step, in
+the plain FP64 arithmetic of the reference.  Synthetic inputs with the
+workload's shapes and value distributions (the reference ships no decks).
+
+Metric: Gcell-steps/s = grid nodes x physical steps / second (whole job).
+  value : device-resident inputs, CUDA events on the library's stream.
+  e2e   : the same steps through the C-ABI with pinned HOST arrays, so every
+          step copies its inputs host->device and phi device->host.
+The reference arm (--impl reference) times the CPU FP64 restatement of the
+reference (the Fortran/MPI original cannot be built: no Fortran compiler)
+with all host threads on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "ns-lsm-single-phase_gb300"))
+
+WORKLOAD = dict(ni=256, nj=128, nk=96, reinit_iters=10, redistance=50)
+
+# algorithmic HBM words per node for one launch of each kernel (FP64 = 8 bytes)
+ALGO_WORDS = {
+    "rk_stage_kernel": 20.0 / 3.0,   # stages read phi_prev, phi^n (stages 2-3), U(3), aj; write phi
+    "reinit_step_kernel": 15.0,      # d, s, phi0, |grad phi0|, delta, metrics(9); write d
+    "sign_ini_kernel": 13.0,         # phi0, metrics(9); write s, |grad phi0|, delta
+    "contra_kernel": 16.0,           # u,v,w, metrics(9), aj; write U(3)
+    "volume_kernel": 4.0,            # phi, x, y, z
+    "bc_full_kernel": 2.0,
+    "copy_kernel": 2.0,
+}
+
+
+def _env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+def dist_setup(n_gpus):
+    rank, world = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+        if torch.cuda.is_available():
+            torch.cuda.set_device(_env_int("LOCAL_RANK", 0))
+    return rank, world
+
+
+def dist_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if torch.cuda.is_available() and dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx.append(float(r[1]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- workload
+def make_case(ni, nj, nk, reinit_iters):
+    from nslsm import configs
+    return configs.solitary_wave(ni, nj, nk, reinit_iters=reinit_iters)
+
+
+def prepare_device(case, ls, torch):
+    """Upload inputs, compute metrics on the GPU, redistance phi0, set dt."""
+    from nslsm import LsmParams  # noqa: F401
+    g = case.grid
+
+    def dev(a):
+        return torch.from_numpy(np.ascontiguousarray(np.asfortranarray(a).T)).cuda()
+
+    x, y, z = dev(case.x), dev(case.y), dev(case.z)
+    csi, eta, zet, aj = ls.mg_metrics(g, x, y, z)
+    q = dev(case.q(0.0))
+    # CFL time step in computational space (csi/eta/zet . u)
+    u = q[..., 1:4]
+    smax = max(float((m * u).sum(-1).abs().max()) for m in (csi, eta, zet))
+    p = case.params.replace(delti_lsm=case.cfl / smax)
+    phi = dev(case.phi0)
+    if case.redistance_iters:
+        pr = p.replace(RNitermax=case.redistance_iters)
+        phi = ls.reinitialization(g, pr, phi, csi, eta, zet)
+        ls.bcond_lsm(g, pr, phi)
+    return dict(g=g, p=p, q=q, csi=csi, eta=eta, zet=zet, aj=aj, phi=phi, x=x, y=y, z=z)
+
+
+def roofline_from_profile(prof, n_nodes, peaks):
+    if not prof:
+        return None
+    name, (launches, ms) = max(prof.items(), key=lambda kv: kv[1][1])
+    words = ALGO_WORDS.get(name)
+    avg_s = ms / 1e3 / max(launches, 1)
+    achieved = None if words is None else words * 8.0 * n_nodes / avg_s / 1e9
+    peak = float(peaks.get("hbm_gbs", 6800.0)) if peaks else 6800.0
+    traffic = read_traffic(name, n_nodes)
+    total = sum(v[1] for v in prof.values())
+    return {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": None if achieved is None else achieved / peak, "traffic": traffic,
+            "algorithmic_bytes_per_launch": None if words is None else words * 8.0 * n_nodes,
+            "avg_launch_us": avg_s * 1e6, "share": ms / total if total else None,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s"}
+
+
+def read_traffic(kernel, n_nodes):
+    """DRAM bytes per launch from the committed ncu summary (bytes per node,
+    measured on a smaller case and scaled by the node count)."""
+    path = os.path.join(REPO, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 3 and parts[0] == "traffic" and parts[1] == kernel:
+            try:
+                return float(parts[2]) * n_nodes
+            except ValueError:
+                return None
+    return None
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
+
+
+# ------------------------------------------------------------- CPU baseline
+def cpu_oracle_time(case, steps, threads):
+    """Seconds per physical step of the CPU FP64 oracle (OpenMP build) on `case`."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    import oracle as O
+    O.build()
+    orc = O.Oracle(omp=True)
+    g = O.make_grid(case.grid.ni, case.grid.nj, case.grid.nk)
+    csi, eta, zet, aj = orc.mg_metrics(g, case.x, case.y, case.z)
+    q = case.q(0.0)
+    u = q[1:4]
+    smax = max(float(np.abs(m[0] * u[0] + m[1] * u[1] + m[2] * u[2]).max()) for m in (csi, eta, zet))
+    cp = case.params
+    p = O.make_params(epslsm=cp.epslsm, delti_lsm=case.cfl / smax, RNitermax=cp.RNitermax,
+                      RNtimestep=cp.RNtimestep, isnarrow=cp.isnarrow, narrowcoef=cp.narrowcoef)
+    phi = case.phi0
+    t0 = time.perf_counter()
+    for it in range(1, steps + 1):
+        phi, _ = orc.levelsetmethod(g, p, q, csi, eta, zet, aj, phi, phi, case.x, case.y, case.z, it)
+    return (time.perf_counter() - t0) / steps, orc.threads
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(args):
+    import torch
+    from nslsm import LevelSet
+    from nslsm._lib import KernelTimer
+
+    rank, world = dist_setup(args.gpus)
+    dev_index = torch.cuda.current_device()
+    W = dict(WORKLOAD)
+    case = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"])
+    case.redistance_iters = W["redistance"]
+    n = case.grid.n
+    ls = LevelSet(device=dev_index)
+    ls.set_stream(torch.cuda.current_stream().cuda_stream)
+    d = prepare_device(case, ls, torch)
+    phi = d["phi"]
+    phin = phi.clone()
+
+    def step(it):
+        phin.copy_(phi)
+        ls.levelsetmethod(d["g"], d["p"], d["q"], d["csi"], d["eta"], d["zet"], d["aj"], phi, phin, d["x"],
+                          d["y"], d["z"], it)
+
+    for it in range(1, args.warmup + 1):
+        step(it)
+    torch.cuda.synchronize()
+    dist_barrier(world)
+    l0 = ls.launches
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev_index) as clocks:
+        torch.cuda.synchronize()
+        ev0.record()
+        for it in range(args.warmup + 1, args.warmup + args.steps + 1):
+            step(it)
+        ev1.record()
+        torch.cuda.synchronize()
+    launches = ls.launches - l0
+    dist_barrier(world)
+    ms = ev0.elapsed_time(ev1)
+    ms_max = dist_max(ms, world)
+    value = world * n * args.steps / (ms_max / 1e3) / 1e9
+
+    # per-kernel attribution (a separate pass with the event timer on)
+    with KernelTimer() as kt:
+        for it in range(1, min(args.steps, 5) + 1):
+            step(it)
+        torch.cuda.synchronize()
+        prof = kt.read()
+    roof = roofline_from_profile(prof, n, load_peaks())
+
+    # end-to-end through the C-ABI with pinned host arrays
+    def pinned(a):
+        a = np.asfortranarray(a)
+        t = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
+        v = t.numpy().reshape(a.shape, order="F")
+        v[...] = a
+        return v, t
+
+    keep = []
+    host = {}
+    for k in ("q", "csi", "eta", "zet", "aj", "x", "y", "z"):
+        arr = d[k].cpu().numpy().T
+        host[k], t = pinned(arr)
+        keep.append(t)
+    hphi, t1 = pinned(phi.cpu().numpy().T)
+    hphin, t2 = pinned(phi.cpu().numpy().T)
+    keep += [t1, t2]
+    e2e_steps = max(2, min(args.steps, 10))
+    ls.set_stream(None)
+    for it in range(1, 2):
+        ls.levelsetmethod(d["g"], d["p"], host["q"], host["csi"], host["eta"], host["zet"], host["aj"], hphi, hphin,
+                          host["x"], host["y"], host["z"], it)
+    torch.cuda.synchronize()
+    dist_barrier(world)
+    t0 = time.perf_counter()
+    for it in range(1, e2e_steps + 1):
+        hphin[...] = hphi
+        ls.levelsetmethod(d["g"], d["p"], host["q"], host["csi"], host["eta"], host["zet"], host["aj"], hphi, hphin,
+                          host["x"], host["y"], host["z"], it)
+    e2e_s = dist_max(time.perf_counter() - t0, world)
+    e2e_value = world * n * e2e_steps / e2e_s / 1e9
+    h2d = 8 * n * (4 + 9 + 1 + 1 + 1 + 3)
+    d2h = 8 * n + 32
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sample = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"])
+        threads = host_threads()
+        sec, used = cpu_oracle_time(sample, 1, threads)
+        cpu = {"value": n / sec / 1e9, "unit": "Gcell-steps/s", "cores": used, "kind": "port",
+               "sample": "1 physical step of the full 256x128x96 workload (FP64 oracle, OpenMP, %d threads, "
+                         "phi0 not redistanced)" % used}
+    if rank == 0:
+        line = {
+            "metric": "Gcell-steps/s (plain FP64 level-set step: WENO3-RK3 advection + reinitialisation + volume)",
+            "value": value, "unit": "Gcell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (analytic solitary-wave workload; the reference ships no decks)",
+            "config": {"workload": "solitary_wave curvilinear %dx%dx%d, CFL 0.4, WENO3+TVD-RK3, %d reinit "
+                                   "pseudo-steps/step, volume each step" % (W["ni"], W["nj"], W["nk"],
+                                                                            W["reinit_iters"]),
+                       "nodes": n, "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (working set %.2f GB > 129 MB)" % (n * 8 * 30 / 1e9)},
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "Gcell-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+            "clocks": clocks.summary(),
+            "gpu_launches": launches,
+            "kernel_times_ms": {k: {"launches": v[0], "total_ms": round(v[1], 4)} for k, v in prof.items()},
+        }
+        print(json.dumps(line))
+    ls.close()
+
+
+# ---------------------------------------------------------- reference arm
+def run_reference(args):
+    rank, world = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1)
+    if rank != 0:
+        return
+    W = dict(WORKLOAD)
+    case = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"])
+    threads = host_threads()
+    # warm-up (page-in, thread pool) then timed steps, each a full physical step
+    cpu_oracle_time(case, max(1, min(args.warmup, 1)), threads)
+    steps = max(1, min(args.steps, 3))
+    sec, used = cpu_oracle_time(case, steps, threads)
+    v = case.grid.n / sec / 1e9
+    line = {
+        "impl": "reference",
+        "metric": "Gcell-steps/s (plain FP64 level-set step: WENO3-RK3 advection + reinitialisation + volume)",
+        "value": v, "unit": "Gcell-steps/s", "n_gpus": world, "steps": steps, "warmup": 1,
+        "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": "solitary_wave curvilinear %dx%dx%d, %d reinit pseudo-steps/step"
+                                        % (W["ni"], W["nj"], W["nk"], W["reinit_iters"])},
+        "cpu_baseline": {"value": v, "unit": "Gcell-steps/s", "cores": used, "kind": "port",
+                         "sample": "%d full physical steps; CPU FP64 restatement of the reference (the Fortran/MPI "
+                                   "original cannot be built here: no Fortran compiler)" % steps},
+        "e2e": {"value": v, "unit": "Gcell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,123 @@
+"""Synthetic workloads of the level-set transport step (host, FP64, numpy).
+
+The reference ships no input decks, so each workload is generated from its
+analytic description: grid coordinates, initial level set phi0 (water is
+phi > 0, as in AnalyticalPhiSphere, src/AdvectionMethods.F90:1733) and the
+Cartesian velocity q(2:4).  Sizes are parameters so the same geometry can be
+run small (parity tests) or at full size (benchmarks).
+
+  sphere_deformation   64^3 unit box, sphere r=0.15 at (0.35,0.35,0.35), LeVeque
+                       3-D deformation field, WENO3 + TVD-RK3 at CFL 0.5, 5
+                       reinit pseudo-steps per step, eps = 1.5 h, 6-cell band.
+  solitary_wave        256x128x96 curvilinear grid x = 8 xi + 0.05 sin(2 pi eta),
+                       y = 2 eta, z = zeta^1.3, phi0 = z - (0.5 + A sech^2(k(x-2))),
+                       uniform flow + solitary-wave perturbation, CFL 0.4, 10
+                       reinit pseudo-steps per step.
+"""
+from __future__ import annotations
+
+import dataclasses as dc
+import math
+from typing import Callable, Optional
+
+import numpy as np
+
+from .api import Grid
+from .params import LsmParams
+
+
+@dc.dataclass
+class Case:
+    name: str
+    grid: Grid
+    x: np.ndarray
+    y: np.ndarray
+    z: np.ndarray
+    phi0: np.ndarray
+    params: LsmParams
+    steps: int
+    cfl: float
+    velocity: Callable[[float], np.ndarray]   # t -> q (4, ni, nj, nk), Fortran order
+    redistance_iters: int = 0
+    h: float = 0.0
+
+    def q(self, t: float = 0.0) -> np.ndarray:
+        return self.velocity(t)
+
+    def time_step(self, csi: np.ndarray, eta: np.ndarray, zet: np.ndarray, t: float = 0.0) -> float:
+        """CFL time step in computational space: cfl / max_nodes max_m |grad xi_m . u|."""
+        q = self.velocity(t)
+        u = q[1:4]
+        s = 0.0
+        for m in (csi, eta, zet):
+            U = np.abs(m[0] * u[0] + m[1] * u[1] + m[2] * u[2])
+            s = max(s, float(U.max()))
+        return self.cfl / s
+
+
+def _fortran(a: np.ndarray) -> np.ndarray:
+    return np.asfortranarray(a, dtype=np.float64)
+
+
+def _mesh(ni, nj, nk):
+    xi = np.arange(ni, dtype=np.float64) / (ni - 1)
+    eta = np.arange(nj, dtype=np.float64) / (nj - 1)
+    zeta = np.arange(nk, dtype=np.float64) / (nk - 1)
+    return np.meshgrid(xi, eta, zeta, indexing="ij")
+
+
+def sphere_deformation(n: int = 64, steps: int = 100, reinit_iters: int = 5) -> Case:
+    X, Y, Z = _mesh(n, n, n)
+    h = 1.0 / (n - 1)
+    x, y, z = _fortran(X), _fortran(Y), _fortran(Z)
+    phi0 = _fortran(0.15 - np.sqrt((X - 0.35) ** 2 + (Y - 0.35) ** 2 + (Z - 0.35) ** 2))
+    sx, sy, sz = np.sin(np.pi * X), np.sin(np.pi * Y), np.sin(np.pi * Z)
+    s2x, s2y, s2z = np.sin(2 * np.pi * X), np.sin(2 * np.pi * Y), np.sin(2 * np.pi * Z)
+    u0 = 2.0 * sx ** 2 * s2y * s2z
+    v0 = -s2x * sy ** 2 * s2z
+    w0 = -s2x * s2y * sz ** 2
+
+    def velocity(t: float) -> np.ndarray:
+        c = math.cos(math.pi * t / 3.0)
+        q = np.zeros((4, n, n, n), order="F")
+        q[1], q[2], q[3] = u0 * c, v0 * c, w0 * c
+        return q
+
+    p = LsmParams(epslsm=1.5 * h, numiter_lsm=1, delti_lsm=0.5 * h / 2.0, RNitermax=reinit_iters,
+                  RNtimestep=0.5 * h, RNfreq=1, btype_lsm=(1,) * 6, isnarrow=1, narrowcoef=4.0, orderAD=1,
+                  BigPhi=5.0, M_Sphi0=1)
+    return Case("sphere_deformation_%dx%dx%d" % (n, n, n), Grid(n, n, n), x, y, z, phi0, p, steps, 0.5,
+                velocity, 0, h)
+
+
+def solitary_wave(ni: int = 256, nj: int = 128, nk: int = 96, steps: int = 200, reinit_iters: int = 10,
+                  Lx: float = 8.0, Ly: float = 2.0, Lz: float = 1.0, x0: float = 2.0,
+                  redistance_iters: int = 50) -> Case:
+    XI, ET, ZE = _mesh(ni, nj, nk)
+    X = Lx * XI + 0.05 * np.sin(2 * np.pi * ET)
+    Y = Ly * ET
+    Z = Lz * ZE ** 1.3
+    A, depth, g = 0.1, 0.5, 9.81
+    k = math.sqrt(3.0 * A / (4.0 * depth ** 3))
+    sech2 = 1.0 / np.cosh(k * (X - x0)) ** 2
+    phi0 = _fortran(Z - (depth + A * sech2))
+    c = A * math.sqrt(g * depth)
+    u = 1.0 + c * sech2
+    w = c * sech2
+    q0 = np.zeros((4, ni, nj, nk), order="F")
+    q0[1], q0[3] = u, w
+
+    def velocity(t: float) -> np.ndarray:
+        return q0
+
+    dx, dy = Lx / (ni - 1), Ly / (nj - 1)
+    dz_min = Lz * (1.0 / (nk - 1)) ** 1.3
+    h = max(dx, dy)
+    p = LsmParams(epslsm=1.5 * h, numiter_lsm=1, delti_lsm=0.0, RNitermax=reinit_iters,
+                  RNtimestep=0.5 * min(dx, dy, dz_min), RNfreq=1, btype_lsm=(1,) * 6, isnarrow=1,
+                  narrowcoef=4.0, orderAD=1, BigPhi=5.0, M_Sphi0=1)
+    return Case("solitary_wave_%dx%dx%d" % (ni, nj, nk), Grid(ni, nj, nk), _fortran(X), _fortran(Y), _fortran(Z),
+                phi0, p, steps, 0.4, velocity, redistance_iters, h)
+
+
+CASES = {"sphere_deformation": sphere_deformation, "solitary_wave": solitary_wave}

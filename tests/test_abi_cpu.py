@@ -1,0 +1,72 @@
+"""C-ABI checks that need no GPU: the library builds and loads, exports
+every entry point declared in include/*.h, and its host-only functions
+behave (parameter defaults, status strings, the GlobalVolume.txt writer,
+the no-device error path)."""
+import ctypes as C
+import glob
+import os
+import re
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b(lsm\w+)\s*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_header_declares_the_reference_routines():
+    names = _declared()
+    for n in ("lsm_levelsetmethod", "lsm_ad_rktvd3", "lsm_calc_rh_ad_weno3", "lsm_calc_rh_ad",
+              "lsm_rhs_contra_j", "lsm_bcond_lsm", "lsm_reinitialization", "lsm_calc_sign_ini",
+              "lsm_calc_rh_rn", "lsm_calc_lambda_rn", "lsm_narrowband", "lsm_total_water_volume",
+              "lsm_get_gfm_list", "lsm_write_total_water_volume"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(lib_built):
+    lib = C.CDLL(lib_built)
+    missing = [n for n in sorted(_declared()) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_every_symbol(lib_built):
+    from nslsm import _lib
+    declared = _declared()
+    bound = set(_lib.SIGNATURES)
+    assert declared <= bound, declared - bound
+
+
+def test_host_only_functions(lib_built, tmp_path):
+    from nslsm import _lib
+    lib = _lib.load()
+    p = _lib.LsmParams()
+    lib.lsm_params_default(C.byref(p))
+    assert p.orderAD == 1 and p.RNitermax == 15 and p.BigPhi == 5.0 and p.M_Sphi0 == 1
+    assert list(p.btype_lsm) == [1] * 6
+    assert lib.lsm_status_string(_lib.LSM_ERR_NEGATIVE_VOLUME) == b"negative tetrahedron water volume"
+    path = str(tmp_path / "GlobalVolume.txt")
+    assert lib.lsm_write_total_water_volume(0.0128813727994583, path.encode()) == 0
+    assert lib.lsm_write_total_water_volume(1.5e-3, path.encode()) == 0
+    lines = open(path).read().splitlines()
+    assert len(lines) == 2
+    assert float(lines[0]) == pytest.approx(0.0128813727994583, rel=1e-15)
+    assert float(lines[1]) == 1.5e-3
+
+
+def test_no_device_is_an_error_not_a_crash(lib_built):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from nslsm import _lib
+    lib = _lib.load()
+    h = C.c_void_p()
+    st = lib.lsm_create(C.byref(h), 0, None)
+    assert st == _lib.LSM_ERR_NO_DEVICE
