@@ -80,8 +80,9 @@ def test_error_codes(ls):
     n = 8
     g, x, y, z, phi, q = cases.sphere(n)
     gg = Grid(n, n, n)
+    m3 = np.zeros((3, n, n, n), order="F")
     with pytest.raises(LsmError) as e:
-        ls.levelsetmethod(gg, LsmParams(hybrid_reinitialisation=True), q, x, x, x, x, phi, phi, x, y, z, 1)
+        ls.levelsetmethod(gg, LsmParams(hybrid_reinitialisation=True), q, m3, m3, m3, x, phi, phi, x, y, z, 1)
     assert e.value.status == _lib.LSM_ERR_UNSUPPORTED
     with pytest.raises(LsmError) as e:
         ls.bcond_lsm(Grid(3, n, n), LsmParams(), np.zeros((3, n, n), order="F"))
