@@ -203,6 +203,26 @@ int lsm_total_water_volume(lsm_handle h, const lsm_grid* g, const double* phi,
                            const double* x, const double* y, const double* z,
                            double* volumes, int* advection_nodes);
 
+/* Allocation-free variant of lsm_total_water_volume.  It has no counterpart
+   in the reference.  It is for callers that cannot call cudaMalloc -- code
+   running under another framework's memory pool or allocator hooks that
+   forbid raw device allocations, or a real-time loop where an allocation's
+   latency or failure is not allowed -- and so cannot create a handle (a
+   handle allocates its pool).  phi, x, y, z must be device arrays of the
+   current GPU; `volumes` (4 doubles, host or device) receives the same
+   numbers as lsm_total_water_volume.  The call allocates nothing: its
+   scratch is one file-scope device array of fixed size (about 6 MiB, held by
+   every GPU that loads this library until the process exits), sized for at
+   most LSM_NOALLOC_MAX_CELLS cells; larger grids return LSM_ERR_CAPACITY.
+   The first call on each device looks the array's address up, so make that
+   first call before any stream capture.  Every call shares the one array:
+   calls that overlap on the GPU (other streams or threads) race and must be
+   serialised by the caller.  The call returns after `stream` has drained. */
+#define LSM_NOALLOC_MAX_CELLS (64LL * 1024 * 1024)
+int lsm_total_water_volume_noalloc(const lsm_grid* g, const double* phi, const double* x,
+                                   const double* y, const double* z, double* volumes,
+                                   void* cuda_stream);
+
 /* Per-cell water volume (diagnostic restatement of the same loop): cellvol
    has the grid's node shape; entry (i,j,k) holds the volume of cell
    (i..i+1, j..j+1, k..k+1), 0 where the loop does not visit. */

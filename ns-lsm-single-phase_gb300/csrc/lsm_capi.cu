@@ -849,3 +849,87 @@ int lsm_mg_metrics(lsm_handle h, const lsm_grid* g, const double* x, const doubl
 }
 
 }  // extern "C"
+
+// ===================================================== allocation-free volume
+// lsm_total_water_volume_noalloc: the TotalWaterVolume reduction for callers
+// that must not allocate device memory themselves.  Its only scratch (the
+// per-block partial sums, the four result words and the error flag) lives in
+// one file-scope device array that every GPU loading this library holds
+// until the process exits.
+namespace {
+
+// layout: [0, 32) result (VK, V2, VB, total); [32, 36) error flag;
+//         [256, 256 + 24 * kNoAllocMaxBlocks) per-block partials (K, S, B)
+constexpr size_t kNoAllocMaxBlocks = (size_t)LSM_NOALLOC_MAX_CELLS / 256;
+constexpr size_t kNoAllocBytes = 256 + 24 * kNoAllocMaxBlocks;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_ptr[64] = {nullptr};  // device address of the array, per device
+
+// Once per device, with that device current: the host-side name of a
+// __device__ array is not a device address, so look the address up.
+int noalloc_scratch(int dev, unsigned char** out) {
+    if (dev < 0 || dev >= 64) return set_err(nullptr, LSM_ERR_NO_DEVICE, "device index too large");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetSymbolAddress(no-alloc scratch)");
+        g_noalloc_ptr[dev] = (unsigned char*)p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return LSM_OK;
+}
+
+bool is_device_ptr(const void* p, int dev) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) && at.device == dev;
+}
+
+}  // namespace
+
+extern "C" int lsm_total_water_volume_noalloc(const lsm_grid* g, const double* phi, const double* x,
+                                              const double* y, const double* z, double* volumes, void* stream) {
+    DevGrid dg;
+    LSM_TRY(check_grid(nullptr, g, &dg));
+    const long long ncell = (long long)((dg.ib - (dg.pf ? 1 : 0)) - dg.ia + 1) *
+                            ((dg.jb - (dg.pr ? 1 : 0)) - dg.ja + 1) * ((dg.kb - (dg.pu ? 1 : 0)) - dg.ka + 1);
+    if (ncell > (long long)LSM_NOALLOC_MAX_CELLS || (size_t)lsm::volume_partial_blocks(dg) > kNoAllocMaxBlocks)
+        return set_err(nullptr, LSM_ERR_CAPACITY,
+                       "grid has more cells than LSM_NOALLOC_MAX_CELLS; use lsm_total_water_volume");
+    if (!phi || !x || !y || !z || !volumes) return set_err(nullptr, LSM_ERR_NULL, "array is NULL");
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(nullptr, LSM_ERR_NO_DEVICE, "no CUDA device");
+    }
+    for (const double* a : {phi, x, y, z})
+        if (!is_device_ptr(a, dev))
+            return set_err(nullptr, LSM_ERR_MIXED_MEMORY, "inputs must be device arrays of the current GPU");
+    unsigned char* base = nullptr;
+    LSM_TRY(noalloc_scratch(dev, &base));
+    cudaStream_t s = (cudaStream_t)stream;
+    double* result = (double*)base;
+    unsigned* err = (unsigned*)(base + 32);
+    double* partials = (double*)(base + 256);
+    // the array keeps the previous call's contents: only the error flag must start at zero
+    LSM_CU(nullptr, cudaMemsetAsync(err, 0, sizeof(unsigned), s));
+    lsm::launch_volume(dg, phi, x, y, z, partials, result, nullptr, nullptr, err, s);
+    LSM_TRY(after_launch(nullptr));
+    double res[4];
+    unsigned flags = 0;
+    const cudaMemcpyKind k = is_device_ptr(volumes, dev) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    LSM_CU(nullptr, cudaMemcpyAsync(k == cudaMemcpyDeviceToHost ? (void*)res : (void*)volumes, result,
+                                    sizeof(res), k, s));
+    LSM_CU(nullptr, cudaMemcpyAsync(&flags, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    LSM_CU(nullptr, cudaStreamSynchronize(s));
+    if (k == cudaMemcpyDeviceToHost) std::memcpy(volumes, res, sizeof(res));
+    if (flags & lsm::kErrNegativeVolume)
+        return set_err(nullptr, LSM_ERR_NEGATIVE_VOLUME, "negative tetrahedron water volume");
+    return LSM_OK;
+}

@@ -76,6 +76,7 @@ SIGNATURES = {
     "lsm_narrowband": (_i, [_vp, _G, _P, _vp, _vp]),
     "lsm_total_water_volume": (_i, [_vp, _G] + [_vp] * 6),
     "lsm_cell_water_volumes": (_i, [_vp, _G] + [_vp] * 5),
+    "lsm_total_water_volume_noalloc": (_i, [_G] + [_vp] * 6),
     "lsm_get_gfm_list": (_i, [_vp, _G, _P, _vp, C.POINTER(_i), _vp, _i]),
     "lsm_write_total_water_volume": (_i, [_d, C.c_char_p]),
     "lsm_mg_metrics": (_i, [_vp, _G] + [_vp] * 7),
