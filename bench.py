@@ -96,11 +96,12 @@ class ClockSampler:
         self.index = index
         self.rows = []
         self.proc = None
+        self.window = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -110,7 +111,11 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.rows.append([c.strip() for c in line.split(",")])
+            self.rows.append((time.time(), [c.strip() for c in line.split(",")]))
+
+    def mark(self, t0, t1):
+        """Keep the samples taken inside [t0, t1] (the timed region)."""
+        self.window = (t0, t1)
 
     def __exit__(self, *exc):
         if self.proc:
@@ -123,7 +128,15 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in self.rows:
+        rows = self.rows
+        if self.window:
+            inside = [r for r in rows if self.window[0] - 0.1 <= r[0] <= self.window[1] + 0.1]
+            if inside:
+                rows = inside
+            elif rows:   # region shorter than the sampling period: the nearest sample
+                mid = 0.5 * (self.window[0] + self.window[1])
+                rows = [min(rows, key=lambda r: abs(r[0] - mid))]
+        for _, r in rows:
             try:
                 sm.append(float(r[0]))
                 mx.append(float(r[1]))
@@ -246,7 +259,7 @@ def run_ours(args):
 
     rank, world = dist_setup(args.gpus)
     dev_index = torch.cuda.current_device()
-    W = dict(WORKLOAD)
+    W = workload(args)
     case = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"])
     case.redistance_iters = W["redistance"]
     n = case.grid.n
@@ -268,12 +281,16 @@ def run_ours(args):
     l0 = ls.launches
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev_index) as clocks:
+        time.sleep(0.5)          # let the sampler start before the timed region
         torch.cuda.synchronize()
+        t_start = time.time()
         ev0.record()
         for it in range(args.warmup + 1, args.warmup + args.steps + 1):
             step(it)
         ev1.record()
         torch.cuda.synchronize()
+        clocks.mark(t_start, time.time())
+        time.sleep(0.2)
     launches = ls.launches - l0
     dist_barrier(world)
     ms = ev0.elapsed_time(ev1)
@@ -358,7 +375,7 @@ def run_reference(args):
     rank, world = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1)
     if rank != 0:
         return
-    W = dict(WORKLOAD)
+    W = workload(args)
     case = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"])
     threads = host_threads()
     # warm-up (page-in, thread pool) then timed steps, each a full physical step
@@ -381,13 +398,21 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def workload(args):
+    W = dict(WORKLOAD)
+    if args.grid:
+        W["ni"], W["nj"], W["nk"] = (int(v) for v in args.grid.lower().split("x"))
+    return W
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grid", default=None, help="NIxNJxNK instead of the 256x128x96 workload (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
