@@ -51,6 +51,10 @@ void fold() {
 }  // namespace
 
 ProfScope::ProfScope(const char* name, cudaStream_t s) : name_(name), s_(s) {
+    // launches recorded into a CUDA graph are counted when the graph is replayed
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s_, &cs) != cudaSuccess) cudaGetLastError();
+    if (cs != cudaStreamCaptureStatusNone) return;
     ++g_launches;
     if (!g_on) return;
     std::lock_guard<std::mutex> lk(g_mu);

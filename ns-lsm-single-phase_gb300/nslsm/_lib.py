@@ -45,6 +45,18 @@ class LsmParams(C.Structure):
                 ("write_global_volume", C.c_int)]
 
 
+class LsmBatchInstance(C.Structure):
+    """struct lsm_batch_instance"""
+    _fields_ = [("ni", C.c_int), ("nj", C.c_int), ("nk", C.c_int), ("dt", C.c_double), ("dtau", C.c_double),
+                ("eps", C.c_double)]
+
+
+class LsmBatchConfig(C.Structure):
+    """struct lsm_batch_config"""
+    _fields_ = [("RNitermax", C.c_int), ("btype_lsm", C.c_int * 6), ("BigPhi", C.c_double),
+                ("use_graph", C.c_int), ("autotune", C.c_int), ("shape", C.c_int)]
+
+
 EXCHANGE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.POINTER(LsmGrid))
 
 _vp = C.c_void_p
@@ -76,10 +88,22 @@ SIGNATURES = {
     "lsm_narrowband": (_i, [_vp, _G, _P, _vp, _vp]),
     "lsm_total_water_volume": (_i, [_vp, _G] + [_vp] * 6),
     "lsm_cell_water_volumes": (_i, [_vp, _G] + [_vp] * 5),
-    "lsm_total_water_volume_noalloc": (_i, [_G] + [_vp] * 6),
     "lsm_get_gfm_list": (_i, [_vp, _G, _P, _vp, C.POINTER(_i), _vp, _i]),
     "lsm_write_total_water_volume": (_i, [_d, C.c_char_p]),
     "lsm_mg_metrics": (_i, [_vp, _G] + [_vp] * 7),
+    "lsm_total_water_volume_noalloc": (_i, [_G] + [_vp] * 6),
+    "lsm_batch_create": (_i, [C.POINTER(_vp), _i, _vp, _i, C.POINTER(LsmBatchInstance),
+                              C.POINTER(LsmBatchConfig)]),
+    "lsm_batch_destroy": (_i, [_vp]),
+    "lsm_batch_set_geometry": (_i, [_vp, _i] + [_vp] * 6),
+    "lsm_batch_set_velocity": (_i, [_vp, _i, _vp]),
+    "lsm_batch_set_phi": (_i, [_vp, _i, _vp]),
+    "lsm_batch_get_phi": (_i, [_vp, _i, _vp]),
+    "lsm_batch_step": (_i, [_vp, _i, _vp]),
+    "lsm_batch_shape": (_i, [_vp] + [C.POINTER(_i)] * 4),
+    "lsm_batch_nodes": (C.c_longlong, [_vp]),
+    "lsm_batch_launches_per_step": (_i, [_vp]),
+    "lsm_batch_last_error": (C.c_char_p, [_vp]),
     "lsm_profile_enable": (_i, [_i]),
     "lsm_profile_reset": (_i, []),
     "lsm_profile_count": (_i, []),

@@ -120,4 +120,66 @@ def solitary_wave(ni: int = 256, nj: int = 128, nk: int = 96, steps: int = 200, 
                 phi0, p, steps, 0.4, velocity, redistance_iters, h)
 
 
+@dc.dataclass
+class Instance:
+    """One instance of a batched workload (single zone, all faces physical)."""
+    grid: Grid
+    x: np.ndarray
+    y: np.ndarray
+    z: np.ndarray
+    phi0: np.ndarray
+    q: np.ndarray
+    eps: float
+    dtau: float
+    cfl: float
+
+    def time_step(self, csi, eta, zet) -> float:
+        u = self.q[1:4]
+        s = max(float(np.abs(m[0] * u[0] + m[1] * u[1] + m[2] * u[2]).max()) for m in (csi, eta, zet))
+        return self.cfl / s
+
+
+def batched_instances(n_inst: int = 64, lo: int = 32, hi: int = 96, seed: int = 0, cfl: float = 0.5) -> list:
+    """64 independent instances with per-axis sizes drawn from {lo..hi}: unit box
+    mapped by identity + random shear (off-diagonal coefficients U(-0.1, 0.1)),
+    phi0 = z - 0.5 - (4 Fourier modes, amplitudes U(0, 0.05), wavenumbers 1-4),
+    velocity = curl of a vector potential with 8 Fourier modes (Gaussian
+    amplitudes, sigma = 0.2), divergence-free."""
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(lo, hi + 1, size=(n_inst, 3))
+    out = []
+    for b in range(n_inst):
+        ni, nj, nk = (int(v) for v in sizes[b])
+        XI, ET, ZE = _mesh(ni, nj, nk)
+        S = np.eye(3)
+        for r in range(3):
+            for c in range(3):
+                if r != c:
+                    S[r, c] = rng.uniform(-0.1, 0.1)
+        X = S[0, 0] * XI + S[0, 1] * ET + S[0, 2] * ZE
+        Y = S[1, 0] * XI + S[1, 1] * ET + S[1, 2] * ZE
+        Z = S[2, 0] * XI + S[2, 1] * ET + S[2, 2] * ZE
+        phi = Z - 0.5
+        for _ in range(4):
+            a = rng.uniform(0.0, 0.05)
+            kx, ky = rng.integers(1, 5, size=2)
+            th = rng.uniform(0, 2 * np.pi)
+            phi = phi - a * np.cos(2 * np.pi * (kx * X + ky * Y) + th)
+        U = np.zeros((3,) + X.shape)
+        for _ in range(8):
+            amp = rng.normal(0.0, 0.2, size=3)
+            kv = rng.integers(1, 5, size=3)
+            th = rng.uniform(0, 2 * np.pi)
+            c = 2 * np.pi * np.cos(2 * np.pi * (kv[0] * X + kv[1] * Y + kv[2] * Z) + th)
+            cr = np.cross(kv, amp)          # curl(a sin(2 pi k.x + th)) = 2 pi cos(...) (k x a)
+            for d in range(3):
+                U[d] += c * cr[d]
+        q = np.zeros((4, ni, nj, nk), order="F")
+        q[1], q[2], q[3] = U[0], U[1], U[2]
+        h = [1.0 / (ni - 1), 1.0 / (nj - 1), 1.0 / (nk - 1)]
+        out.append(Instance(Grid(ni, nj, nk), _fortran(X), _fortran(Y), _fortran(Z), _fortran(phi), q,
+                            1.5 * max(h), 0.5 * min(h), cfl))
+    return out
+
+
 CASES = {"sphere_deformation": sphere_deformation, "solitary_wave": solitary_wave}
