@@ -1,22 +1,27 @@
 """Benchmark of the level-set transport step on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload batched|fp64]
 
-Workload: the curvilinear solitary-wave case, 256 x 128 x 96 nodes
-(x = 8 xi + 0.05 sin(2 pi eta), y = 2 eta, z = zeta^1.3), phi0 redistanced by
-50 reinitialisation pseudo-steps, uniform flow plus the solitary-wave
-perturbation, CFL 0.4, WENO3 + TVD-RK3, 10 reinitialisation pseudo-steps per
-physical step, 6-cell narrow band: one `levelsetmethod` call per step, in
-the plain FP64 arithmetic of the reference.  Synthetic inputs with the
-workload's shapes and value distributions (the reference ships no decks).
+Default workload ("batched"): 64 independent instances with per-axis sizes
+drawn from {32..96} (numpy seed 0), identity-plus-random-shear grids,
+phi0 = z - 0.5 - 4 random Fourier modes, divergence-free curl velocity,
+CFL 0.5, 5 reinitialisation pseudo-steps per step -- the whole batch
+advanced by the FP32 batched kernels (one launch per pass, CUDA graph per
+step, autotuned tile shape) with the FP64 water volume every step.
+
+"fp64" workload: the curvilinear solitary-wave case, 256 x 128 x 96 nodes,
+10 reinitialisation pseudo-steps per step, through `lsm_levelsetmethod` in
+the reference's FP64 arithmetic.
 
 Metric: Gcell-steps/s = grid nodes x physical steps / second (whole job).
-  value : device-resident inputs, CUDA events on the library's stream.
-  e2e   : the same steps through the C-ABI with pinned HOST arrays, so every
-          step copies its inputs host->device and phi device->host.
-The reference arm (--impl reference) times the CPU FP64 restatement of the
-reference (the Fortran/MPI original cannot be built: no Fortran compiler)
-with all host threads on the same workload.
+  value : device-resident inputs, CUDA events on the launching stream.
+  e2e   : the same steps with the per-step inputs (velocity) copied in from
+          pinned host memory and phi read back every step.
+Synthetic inputs with the workloads' shapes and value distributions (the
+reference ships no input decks).  The reference arm (--impl reference)
+times the CPU FP64 restatement of the reference (the Fortran/MPI original
+cannot be built: no Fortran compiler) with all host threads.
 """
 from __future__ import annotations
 
@@ -251,8 +256,230 @@ def host_threads():
         return os.cpu_count() or 1
 
 
-# ---------------------------------------------------------------- our arm
+# ---------------------------------------------------------- batched FP32 arm
+BATCH = dict(n_inst=64, lo=32, hi=96, seed=0, reinit_iters=5, cfl=0.5)
+
+# algorithmic HBM bytes per node for one launch of the batched FP32 kernels
+BATCH_ALGO_BYTES = {
+    "k_stage": 17.0 / 3.0 * 4,   # phi_prev, phi^n (stages 2-3), W(3); phi
+    "k_reinit": 12.0 * 4,        # d, s, metrics(9); d
+    "k_sign": 11.0 * 4,          # phi0, metrics(9); s
+    "k_contra": 15.0 * 4,        # u(3), metrics(9); W(3)
+    "k_volume": 4.0 + 8.0,       # phi (FP32) + FP64 cell volume (+ coordinates of interface cells only)
+    "k_bc_full": 8.0,
+}
+
+
+def batch_setup(torch, ls, stream, reinit_iters, use_graph=True, autotune=True, shape=0, n_inst=None):
+    """Build the 64-instance workload on the GPU: FP64 metrics per instance
+    (lsm_mg_metrics), CFL time step per instance, packed FP32 batch."""
+    from nslsm import configs
+    from nslsm.batch import LevelSetBatch
+    kw = dict(BATCH)
+    if n_inst:
+        kw["n_inst"] = n_inst
+    insts = configs.batched_instances(kw["n_inst"], kw["lo"], kw["hi"], kw["seed"], kw["cfl"])
+
+    def dev(a):
+        return torch.from_numpy(np.ascontiguousarray(np.asfortranarray(a).T)).cuda()
+
+    meta = []
+    for it in insts:
+        csi, eta, zet, aj = ls.mg_metrics(it.grid, dev(it.x), dev(it.y), dev(it.z))
+        u = dev(it.q)[..., 1:4]
+        smax = max(float((m * u).sum(-1).abs().max()) for m in (csi, eta, zet))
+        meta.append(dict(inst=it, csi=csi, eta=eta, zet=zet, aj=aj, dt=it.cfl / smax))
+    b = LevelSetBatch([(*m["inst"].grid.shape, m["dt"], m["inst"].dtau, m["inst"].eps) for m in meta],
+                      RNitermax=reinit_iters, btype=(1,) * 6, BigPhi=5.0, stream=stream, use_graph=use_graph,
+                      autotune=autotune, shape=shape)
+    for k, m in enumerate(meta):
+        it = m["inst"]
+        b.set_geometry(k, dev(it.x), dev(it.y), dev(it.z), m["csi"], m["eta"], m["zet"])
+        b.set_velocity(k, dev(it.q))
+        b.set_phi(k, dev(it.phi0))
+    return b, meta
+
+
+def run_batched(args):
+    import torch
+    from nslsm import LevelSet, LsmParams
+    from nslsm._lib import KernelTimer
+
+    rank, world = dist_setup(args.gpus)
+    dev_index = torch.cuda.current_device()
+    R = BATCH["reinit_iters"]
+    ls = LevelSet(device=dev_index)
+    stream = torch.cuda.Stream()
+    b, meta = batch_setup(torch, ls, stream.cuda_stream, R, n_inst=args.n_inst)
+    n = b.nodes
+    b.step(args.warmup, volumes=False)          # includes the tile autotune and graph capture
+    torch.cuda.synchronize()
+    dist_barrier(world)
+    from nslsm import _lib
+    lib = _lib.load()
+    l0 = lib.lsm_kernel_launch_count(None)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev_index) as clocks:
+        time.sleep(0.5)
+        torch.cuda.synchronize()
+        t_start = time.time()
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            b.step(args.steps, volumes=False)
+            ev1.record(stream)
+        torch.cuda.synchronize()
+        clocks.mark(t_start, time.time())
+        time.sleep(0.2)
+    launches = lib.lsm_kernel_launch_count(None) - l0
+    dist_barrier(world)
+    ms = ev0.elapsed_time(ev1)
+    ms_max = dist_max(ms, world)
+    value = world * n * args.steps / (ms_max / 1e3) / 1e9
+    shape = b.shape
+
+    # per-kernel attribution: the same batch without the graph (the event
+    # timer brackets each launch on the batch's stream)
+    b2, _ = batch_setup(torch, ls, stream.cuda_stream, R, use_graph=False, autotune=False, shape=shape[0],
+                        n_inst=args.n_inst)
+    b2.step(2, volumes=False)
+    torch.cuda.synchronize()
+    with KernelTimer() as kt:
+        b2.step(5, volumes=False)
+        torch.cuda.synchronize()
+        prof = kt.read()
+    b2.close()
+    roof = None
+    if prof:
+        name, (cnt, tms) = max(prof.items(), key=lambda kv: kv[1][1])
+        byt = BATCH_ALGO_BYTES.get(name)
+        avg = tms / 1e3 / max(cnt, 1)
+        peaks = load_peaks()
+        peak = float(peaks.get("hbm_gbs", 6800.0)) if peaks else 6800.0
+        ach = None if byt is None else byt * n / avg / 1e9
+        total = sum(v[1] for v in prof.values())
+        roof = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak, "unit": "GB/s",
+                "frac": None if ach is None else ach / peak, "traffic": read_traffic(name, n),
+                "algorithmic_bytes_per_launch": None if byt is None else byt * n, "avg_launch_us": avg * 1e6,
+                "share": tms / total if total else None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s",
+                "per_kernel_frac": {k: (BATCH_ALGO_BYTES[k] * n / (v[1] / 1e3 / v[0]) / 1e9 / peak)
+                                    for k, v in prof.items() if k in BATCH_ALGO_BYTES}}
+
+    # the plain FP64 GPU path on the same instances (one levelsetmethod call per instance)
+    fp64 = None
+    if not args.no_fp64_compare:
+        steps64 = 2
+        tot64 = 0.0
+        nodes64 = 0
+        for m in meta[:16]:
+            it = m["inst"]
+            g = it.grid
+            p = LsmParams(epslsm=it.eps, delti_lsm=m["dt"], RNitermax=R, RNtimestep=it.dtau, isnarrow=1,
+                          narrowcoef=4.0, BigPhi=5.0)
+
+            def dev(a):
+                return torch.from_numpy(np.ascontiguousarray(np.asfortranarray(a).T)).cuda()
+            q, x, y, z = dev(it.q), dev(it.x), dev(it.y), dev(it.z)
+            phi = dev(it.phi0)
+            phin = phi.clone()
+            ls.set_stream(torch.cuda.current_stream().cuda_stream)
+            ls.levelsetmethod(g, p, q, m["csi"], m["eta"], m["zet"], m["aj"], phi, phin, x, y, z, 1)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for s in range(steps64):
+                phin.copy_(phi)
+                ls.levelsetmethod(g, p, q, m["csi"], m["eta"], m["zet"], m["aj"], phi, phin, x, y, z, s + 2)
+            torch.cuda.synchronize()
+            tot64 += time.perf_counter() - t0
+            nodes64 += g.n * steps64
+        v64 = nodes64 / tot64 / 1e9
+        fp64 = {"value": v64, "unit": "Gcell-steps/s", "sample": "first 16 instances, %d steps each, "
+                "lsm_levelsetmethod (reference FP64 arithmetic)" % steps64, "speedup_fp32_batched": value / v64}
+
+    # end-to-end: every step copies each instance's velocity in from pinned
+    # host memory and reads every instance's phi back
+    pinned = []
+    for m in meta:
+        a = np.asfortranarray(m["inst"].q)
+        t = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
+        v = t.numpy().reshape(a.shape, order="F")
+        v[...] = a
+        o = torch.empty(m["inst"].grid.n, dtype=torch.float64, pin_memory=True)
+        pinned.append((v, t, o.numpy().reshape(m["inst"].grid.shape, order="F"), o))
+    e2e_steps = max(2, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in range(e2e_steps):
+        for k, (v, _t, _o, _ot) in enumerate(pinned):
+            b.set_velocity(k, v)
+        b.step(1, volumes=True)
+        for k, (_v, _t, o, _ot) in enumerate(pinned):
+            b._chk(b.lib.lsm_batch_get_phi(b.h, k, o.ctypes.data), "get_phi")
+    torch.cuda.synchronize()
+    e2e_s = dist_max(time.perf_counter() - t0, world)
+    e2e_value = world * n * e2e_steps / e2e_s / 1e9
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = batch_cpu_baseline(meta[:6], R)
+    if rank == 0:
+        line = {
+            "metric": "Gcell-steps/s (batched FP32 level-set step, forward: WENO3-RK3 + %d reinit pseudo-steps + "
+                      "FP64 volume, 64 uneven instances)" % R,
+            "value": value, "unit": "Gcell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (64 instances, sizes U{32..96} seed 0, shear metrics, Fourier phi0, "
+                                    "curl velocity; the reference ships no decks)",
+            "config": {"workload": "batched_instances 64 x U{32..96}^3 (%d nodes), CFL 0.5, %d reinit "
+                                   "pseudo-steps/step, volume each step, one launch per pass, CUDA graph" % (n, R),
+                       "nodes": n, "tile_shape": shape[1], "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (working set %.2f GB > 129 MB)" % (n * 4 * 30 / 1e9)},
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "fp64_gpu_path": fp64,
+            "e2e": {"value": e2e_value, "unit": "Gcell-steps/s", "h2d_bytes_per_step": 32 * n,
+                    "d2h_bytes_per_step": 8 * n + 32 * len(meta), "steps": e2e_steps},
+            "clocks": clocks.summary(),
+            "gpu_launches": launches,
+            "kernel_times_ms": {k: {"launches": v[0], "total_ms": round(v[1], 4)} for k, v in prof.items()},
+        }
+        print(json.dumps(line))
+    b.close()
+    ls.close()
+
+
+def batch_cpu_baseline(meta, R):
+    """CPU FP64 oracle (OpenMP, all host threads) on a bounded sample of the
+    batched workload: one physical step of each of the first instances."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    threads = host_threads()
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    import oracle as O
+    O.build()
+    orc = O.Oracle(omp=True)
+    nodes, sec = 0, 0.0
+    for m in meta:
+        it = m["inst"]
+        g = O.make_grid(*it.grid.shape)
+        csi, eta, zet, aj = orc.mg_metrics(g, it.x, it.y, it.z)
+        p = O.make_params(epslsm=it.eps, delti_lsm=m["dt"], RNitermax=R, RNtimestep=it.dtau, BigPhi=5.0)
+        t0 = time.perf_counter()
+        orc.levelsetmethod(g, p, it.q, csi, eta, zet, aj, it.phi0, it.phi0, it.x, it.y, it.z, 1)
+        sec += time.perf_counter() - t0
+        nodes += it.grid.n
+    return {"value": nodes / sec / 1e9, "unit": "Gcell-steps/s", "cores": orc.threads, "kind": "port",
+            "sample": "1 physical step of each of the first %d instances (%d nodes), CPU FP64 oracle, OpenMP"
+                      % (len(meta), nodes)}
+
+
+# ---------------------------------------------------------------- FP64 arm
 def run_ours(args):
+    if args.workload == "batched":
+        return run_batched(args)
+    return run_fp64(args)
+
+
+def run_fp64(args):
     import torch
     from nslsm import LevelSet
     from nslsm._lib import KernelTimer
@@ -375,6 +602,8 @@ def run_reference(args):
     rank, world = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1)
     if rank != 0:
         return
+    if args.workload == "batched":
+        return run_reference_batched(args, world)
     W = workload(args)
     case = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"])
     threads = host_threads()
@@ -398,6 +627,59 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_reference_batched(args, world):
+    """The CPU FP64 restatement of the reference (all host threads) on the
+    batched workload: each timed step advances a rotating group of 8 of the
+    64 instances by one physical step (bounded sample)."""
+    from nslsm import configs
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    threads = host_threads()
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    import oracle as O
+    O.build()
+    orc = O.Oracle(omp=True)
+    R = BATCH["reinit_iters"]
+    insts = configs.batched_instances(BATCH["n_inst"], BATCH["lo"], BATCH["hi"], BATCH["seed"], BATCH["cfl"])
+    prepared = []
+    for it in insts:
+        g = O.make_grid(*it.grid.shape)
+        csi, eta, zet, aj = orc.mg_metrics(g, it.x, it.y, it.z)
+        p = O.make_params(epslsm=it.eps, delti_lsm=it.time_step(csi, eta, zet), RNitermax=R, RNtimestep=it.dtau,
+                          BigPhi=5.0)
+        prepared.append((it, g, p, csi, eta, zet, aj))
+
+    def one(group, s):
+        nodes = 0
+        for it, g, p, csi, eta, zet, aj in group:
+            orc.levelsetmethod(g, p, it.q, csi, eta, zet, aj, it.phi0, it.phi0, it.x, it.y, it.z, s)
+            nodes += it.grid.n
+        return nodes
+
+    one(prepared[:2], 1)
+    steps = max(1, min(args.steps, 3))
+    nodes, t0 = 0, time.perf_counter()
+    for s in range(steps):
+        grp = [prepared[(8 * s + q) % len(prepared)] for q in range(8)]
+        nodes += one(grp, s + 1)
+    sec = time.perf_counter() - t0
+    v = nodes / sec / 1e9
+    line = {
+        "impl": "reference",
+        "metric": "Gcell-steps/s (batched FP32 level-set step, forward: WENO3-RK3 + %d reinit pseudo-steps + "
+                  "FP64 volume, 64 uneven instances)" % R,
+        "value": v, "unit": "Gcell-steps/s", "n_gpus": world, "steps": steps, "warmup": 1,
+        "ms_per_step": sec / steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "batched_instances 64 x U{32..96}^3, %d reinit pseudo-steps/step" % R},
+        "cpu_baseline": {"value": v, "unit": "Gcell-steps/s", "cores": orc.threads, "kind": "port",
+                         "sample": "%d steps, each one physical step of 8 of the 64 instances (%d nodes in total); "
+                                   "CPU FP64 restatement of the reference (the Fortran/MPI original cannot be built "
+                                   "here: no Fortran compiler)" % (steps, nodes)},
+        "e2e": {"value": v, "unit": "Gcell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
 def workload(args):
     W = dict(WORKLOAD)
     if args.grid:
@@ -413,6 +695,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", default=None, help="NIxNJxNK instead of the 256x128x96 workload (profiling runs)")
+    ap.add_argument("--workload", choices=["batched", "fp64"], default="batched")
+    ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--n-inst", type=int, default=None, help="instances of the batched workload (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

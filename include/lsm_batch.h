@@ -12,10 +12,22 @@
  * bcond_lsm after every stage, RNitermax pseudo-steps of `reinitialization`
  * and a final bcond_lsm.
  *
- * Precision: the stencils run in FP32; the water volume is FP64 (FP32 phi,
- * FP64 coordinates, the reference's marching tetrahedra) with fixed-order
- * sums per instance.  No counterpart exists in the reference, which
- * advances one subdomain per MPI rank.
+ * Precision: the stencils run in FP32 (precision 0, throughput) or FP64
+ * (precision 1, gradient checks); the water volume is FP64 per cell (the
+ * reference's marching tetrahedra on FP64 coordinates), rounded to a
+ * multiple of 2^-48 and summed as 64-bit integers, so each instance's sum is
+ * exact and independent of the summation order (valid below 2^15 units^3).
+ *
+ * Adjoint: lsm_batch_forward_record runs `nsteps` steps keeping the state
+ * every `checkpoint_every` steps; after seeding dL/dphi^{nsteps} per
+ * instance, lsm_batch_backward recomputes each segment from its checkpoint
+ * and runs the hand-written reverse kernels (WENO3 nonlinear weights
+ * differentiated, upwind side frozen; Godunov selections and the sign field
+ * frozen), giving dL/dphi^0 and dL/dq(2:4) (the velocity is held fixed over
+ * the recorded steps).
+ *
+ * No counterpart exists in the reference, which advances one subdomain per
+ * MPI rank and has no adjoint.
  */
 #ifndef LSM_BATCH_H
 #define LSM_BATCH_H
@@ -40,6 +52,7 @@ typedef struct lsm_batch_config {
     int use_graph;      /* 1: capture the per-step launches in a CUDA graph */
     int autotune;       /* 1: time every tile shape on this batch and keep the fastest */
     int shape;          /* tile shape index when autotune == 0 (0..4) */
+    int precision;      /* 0: FP32 stencils, 1: FP64 stencils (tile shape 0, no autotune) */
 } lsm_batch_config;
 
 typedef struct lsm_batch* lsm_batch_handle;
@@ -63,6 +76,20 @@ int lsm_batch_get_phi(lsm_batch_handle h, int inst, double* phi);
    host, 4*ninst doubles) receives each instance's pre-advection volumes of
    the last step (K-tetrahedra, second tetrahedra, bulk, total). */
 int lsm_batch_step(lsm_batch_handle h, int nsteps, double* volumes);
+
+/* Adjoint.  Run `nsteps` steps from the current phi (which becomes phi^0),
+   keeping checkpoints; device memory ~ N (nsteps/checkpoint_every +
+   checkpoint_every + RNitermax + 22) elements. */
+int lsm_batch_forward_record(lsm_batch_handle h, int nsteps, int checkpoint_every);
+/* Seed dL/dphi at the end of the recorded steps for one instance (FP64, host
+   or device; instances not seeded get zero). */
+int lsm_batch_set_grad_phi(lsm_batch_handle h, int inst, const double* grad);
+/* Reverse the recorded steps. */
+int lsm_batch_backward(lsm_batch_handle h);
+/* dL/dphi^0 of one instance (FP64, host or device, ni*nj*nk). */
+int lsm_batch_get_grad_phi0(lsm_batch_handle h, int inst, double* grad);
+/* dL/dq of one instance in the layout of q (4, ni, nj, nk); q(1) gets zero. */
+int lsm_batch_get_grad_velocity(lsm_batch_handle h, int inst, double* grad_q);
 
 /* Tile shape in use (index, and its TX, TY, TZ). */
 int lsm_batch_shape(lsm_batch_handle h, int* index, int* tx, int* ty, int* tz);

@@ -1,23 +1,33 @@
-// lsm_batch.cu -- batched FP32 kernels of the level-set transport step.
+// lsm_batch.cu -- batched kernels of the level-set transport step, forward
+// and adjoint, templated on the scalar type (FP32 for throughput, FP64 for
+// gradient checks).
 //
-// One launch per pass covers every instance of the batch: the CTAs are
-// persistent (grid = SMs x resident CTAs) and walk a brick table in which
-// each brick of TX x TY x TZ nodes belongs to one instance.  Every kernel is
-// HBM-bound by design; the per-node algorithmic traffic (4-byte words) is
+// Forward: one launch per pass covers every instance of the batch: the CTAs
+// are persistent (grid = SMs x resident CTAs) and walk a brick table in
+// which each brick of TX x TY x TZ nodes belongs to one instance.  The
+// kernels are HBM-bound by design; per-node algorithmic traffic (FP32 words)
 //   contra 15 (u 3, metrics 9; W 3), RK stage 5/6/6 (phi_prev, phi^n, W 3;
 //   phi), sign 11 (phi0, metrics 9; s), reinit pseudo-step 12 (d, s,
-//   metrics 9; d), volume 7 (phi + FP64 x, y, z).
+//   metrics 9; d), volume 3 (phi + 64-bit fixed-point cell volume).
 //
-// Arithmetic: FP32 stencils with the reference's formulas rearranged for
-// FP32 (one division per WENO3 reconstruction); the volume is FP64 (the
-// reference's marching-tetrahedra functions), with per-instance fixed-order
-// sums.  The reinitialisation uses the closed form of the reference's
-// method-0 lambda correction: with lambda = -(d1 - phi0) / (dtau delta |grad
-// phi0|) the correction dtau lambda delta |grad phi0| returns d to phi0
-// wherever delta(phi0) |grad phi0| != 0, i.e. |phi0| < eps; those nodes are
-// folded into the sign field as s = 0 (no update) and the pseudo-step reads
-// only d, s and the metrics.
+// Arithmetic: the reference's formulas rearranged for the GPU (one division
+// per WENO3 reconstruction); the water volume is FP64 per cell with exact
+// 64-bit fixed-point sums.  The reinitialisation uses the closed form of the
+// reference's method-0 lambda correction: with lambda = -(d1 - phi0) /
+// (dtau delta |grad phi0|) the correction dtau lambda delta |grad phi0|
+// returns d to phi0 wherever delta(phi0) |grad phi0| != 0, i.e.
+// |phi0| < eps; those nodes are folded into the sign field as s = 0 (no
+// update) and a pseudo-step reads only d, s and the metrics.
+//
+// Adjoint: hand-written reverse kernels, one thread per node, gathering
+// (no atomics): bcond_lsm faces in reverse order; the WENO3 stage with the
+// upwind side of every face frozen from the forward pass and the nonlinear
+// weights differentiated; the Godunov reinitialisation step with its max /
+// clip selections frozen (two passes: per-node coefficients, then gather);
+// the contravariant-velocity chain rule.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "lsm_batch.cuh"
 #include "lsm_common.cuh"
@@ -28,17 +38,33 @@ namespace lsm {
 namespace batch {
 namespace {
 
-// ------------------------------------------------------------ brick walk
-template <int TX, int TY, int TZ>
-struct Brick {
-    int inst, i, j, k;     // thread's node (may lie outside the instance)
+// ------------------------------------------------------------ scalar helpers
+template <typename T> __device__ __forceinline__ T vmax(T a, T b) { return a > b ? a : b; }
+template <typename T> __device__ __forceinline__ T vmin(T a, T b) { return a < b ? a : b; }
+template <typename T> __device__ __forceinline__ T vdiv(T a, T b) { return a / b; }
+template <> __device__ __forceinline__ float vdiv<float>(float a, float b) { return __fdividef(a, b); }
+template <typename T> __device__ __forceinline__ T vfma(T a, T b, T c) { return fma(a, b, c); }
+template <> __device__ __forceinline__ float vfma<float>(float a, float b, float c) { return fmaf(a, b, c); }
+template <typename T> __device__ __forceinline__ T vsqrt(T a) { return sqrt(a); }
+template <> __device__ __forceinline__ float vsqrt<float>(float a) { return sqrtf(a); }
+template <typename T> __device__ __forceinline__ T vsin(T a) { return sin(a); }
+template <> __device__ __forceinline__ float vsin<float>(float a) { return sinf(a); }
+template <typename T> __device__ __forceinline__ bool vfinite(T a) { return isfinite(a); }
+// per-instance parameter in the kernel's precision
+template <typename T> __device__ __forceinline__ T ipar(float f, double d);
+template <> __device__ __forceinline__ float ipar<float>(float f, double) { return f; }
+template <> __device__ __forceinline__ double ipar<double>(float, double d) { return d; }
+
+// ------------------------------------------------------------ node walks
+struct Node {
+    int inst, i, j, k;
     bool valid;
 };
 
 template <int TX, int TY, int TZ>
-__device__ __forceinline__ Brick<TX, TY, TZ> brick_node(const Inst* __restrict__ inst,
-                                                         const int* __restrict__ brick_inst, int blk) {
-    Brick<TX, TY, TZ> b;
+__device__ __forceinline__ Node brick_node(const Inst* __restrict__ inst, const int* __restrict__ brick_inst,
+                                           int blk) {
+    Node b;
     b.inst = __ldg(brick_inst + blk);
     const Inst& I = inst[b.inst];
     const int local = blk - I.brick0;
@@ -51,439 +77,988 @@ __device__ __forceinline__ Brick<TX, TY, TZ> brick_node(const Inst* __restrict__
     return b;
 }
 
-// ------------------------------------------------------------ WENO3 (FP32)
+// flat walk: node t of the packed arrays -> instance and (i, j, k)
+__device__ __forceinline__ bool flat_node(const Flat& fl, long long t, Node* nd) {
+    if (t >= fl.n) return false;
+    int lo = 0, hi = fl.ninst - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (fl.offs[mid] <= t) lo = mid; else hi = mid - 1;
+    }
+    const Inst& I = fl.inst[lo];
+    const long long r = t - I.off;
+    nd->inst = lo;
+    nd->i = (int)(r % I.ni);
+    nd->j = (int)((r / I.ni) % I.nj);
+    nd->k = (int)(r / ((long long)I.ni * I.nj));
+    nd->valid = true;
+    return true;
+}
+
+// ------------------------------------------------------------ WENO3
 // GetWENO3Reconstruction (src/AdvectionMethods.F90:195-245) on an oriented
 // stencil (fL, fC, fR): weights 2/3, 1/3 over (beta + 1e-6)^2, rearranged to
 // one division: w0 = 2 t1^2 / (2 t1^2 + t0^2), Phi = u1 + w0 (u0 - u1).
-__device__ __forceinline__ float rec3(float fL, float fC, float fR) {
-    const float b0 = (fC - fR) * (fC - fR), b1 = (fL - fC) * (fL - fC);
-    const float t0 = b0 + 1.0e-6f, t1 = b1 + 1.0e-6f;
-    const float a0 = 2.0f * t1 * t1, a1 = t0 * t0;
-    const float w0 = __fdividef(a0, a0 + a1);
-    const float u1 = 1.5f * fC - 0.5f * fL;
-    return fmaf(w0, 0.5f * (fL + fR) - fC, u1);
+template <typename T>
+__device__ __forceinline__ T rec3(T fL, T fC, T fR) {
+    const T b0 = (fC - fR) * (fC - fR), b1 = (fL - fC) * (fL - fC);
+    const T t0 = b0 + T(1.0e-6), t1 = b1 + T(1.0e-6);
+    const T a0 = T(2) * t1 * t1, a1 = t0 * t0;
+    const T w0 = vdiv(a0, a0 + a1);
+    const T u1 = T(1.5) * fC - T(0.5) * fL;
+    return vfma(w0, T(0.5) * (fL + fR) - fC, u1);
+}
+
+// gradient of rec3 with respect to (fL, fC, fR)
+template <typename T>
+__device__ __forceinline__ void rec3_grad(T fL, T fC, T fR, T* dL, T* dC, T* dR) {
+    const T eL = fL - fC, eR = fC - fR;
+    const T t0 = eR * eR + T(1.0e-6), t1 = eL * eL + T(1.0e-6);
+    const T a0 = T(2) * t1 * t1, a1 = t0 * t0;
+    const T den = a0 + a1;
+    const T w0 = a0 / den;
+    const T inv2 = T(1) / (den * den);
+    const T dw_da0 = a1 * inv2, dw_da1 = -a0 * inv2;
+    const T da0 = T(4) * t1, da1 = T(2) * t0;     // d a0 / d t1, d a1 / d t0
+    const T g = T(0.5) * (fL + fR) - fC;
+    const T wL = dw_da0 * da0 * (T(2) * eL);                                   // d w0 / d fL
+    const T wC = dw_da0 * da0 * (T(-2) * eL) + dw_da1 * da1 * (T(2) * eR);    // d w0 / d fC
+    const T wR = dw_da1 * da1 * (T(-2) * eR);                                  // d w0 / d fR
+    *dL = T(-0.5) + g * wL + T(0.5) * w0;
+    *dC = T(1.5) + g * wC - w0;
+    *dR = g * wR + T(0.5) * w0;
 }
 
 // Phi_{+1/2} - Phi_{-1/2} along one axis for the node with stencil
 // (m2, m1, c, p1, p2); lo/hi force the reference's one-sided stencils on
 // the first / last interior node (calc_RH_AD_WENO3.F90:201-245).
-__device__ __forceinline__ float weno_diff(float m2, float m1, float c, float p1, float p2, float w, bool lo,
-                                           bool hi) {
-    const bool up = w > 0.0f;
-    const float fp = (up || hi) ? rec3(m1, c, p1) : rec3(p2, p1, c);
-    const float fm = (up && !lo) ? rec3(m2, m1, c) : rec3(p1, c, m1);
+template <typename T>
+__device__ __forceinline__ T weno_diff(T m2, T m1, T c, T p1, T p2, T w, bool lo, bool hi) {
+    const bool up = w > T(0);
+    const T fp = (up || hi) ? rec3(m1, c, p1) : rec3(p2, p1, c);
+    const T fm = (up && !lo) ? rec3(m2, m1, c) : rec3(p1, c, m1);
     return fp - fm;
 }
 
+// gradient of weno_diff w.r.t. (m2, m1, c, p1, p2), same frozen orientation
+template <typename T>
+__device__ __forceinline__ void weno_diff_grad(const T (&s)[5], T w, bool lo, bool hi, T (&g)[5]) {
+    g[0] = g[1] = g[2] = g[3] = g[4] = T(0);
+    const bool up = w > T(0);
+    T a, b, c;
+    if (up || hi) { rec3_grad(s[1], s[2], s[3], &a, &b, &c); g[1] += a; g[2] += b; g[3] += c; }
+    else { rec3_grad(s[4], s[3], s[2], &a, &b, &c); g[4] += a; g[3] += b; g[2] += c; }
+    if (up && !lo) { rec3_grad(s[0], s[1], s[2], &a, &b, &c); g[0] -= a; g[1] -= b; g[2] -= c; }
+    else { rec3_grad(s[3], s[2], s[1], &a, &b, &c); g[3] -= a; g[2] -= b; g[1] -= c; }
+}
+
 // ------------------------------------------------------------ contra
-template <int TX, int TY, int TZ>
+template <typename T, int TX, int TY, int TZ>
 __global__ void __launch_bounds__(TX * TY * TZ) k_contra(const Inst* __restrict__ inst,
-        const int* __restrict__ brick_inst, int nbricks, Fields f, float dc, float de, float dz) {
+        const int* __restrict__ brick_inst, int nbricks, FieldsT<T> f) {
     for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const auto b = brick_node<TX, TY, TZ>(inst, brick_inst, blk);
+        const Node b = brick_node<TX, TY, TZ>(inst, brick_inst, blk);
         if (!b.valid) continue;
         const Inst& I = inst[b.inst];
         const long long l = I.off + b.i + (long long)I.ni * (b.j + (long long)I.nj * b.k);
-        const float u = f.u[0][l], v = f.u[1][l], w = f.u[2][l];
-        const float dd[3] = {dc, de, dz};
+        const T u = f.u[0][l], v = f.u[1][l], w = f.u[2][l];
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
-            const float c = f.m[3 * m][l] * u + f.m[3 * m + 1][l] * v + f.m[3 * m + 2][l] * w;
-            f.W[m][l] = I.dt * dd[m] * c;
+            const T c = f.m[3 * m][l] * u + f.m[3 * m + 1][l] * v + f.m[3 * m + 2][l] * w;
+            f.W[m][l] = ipar<T>(I.dt, I.dt64) * c;
         }
     }
 }
 
 // ------------------------------------------------------------ RK stage
-template <int TX, int TY, int TZ>
+__device__ __forceinline__ bool interior(const Inst& I, int i, int j, int k) {
+    return i > 0 && i < I.ni - 1 && j > 0 && j < I.nj - 1 && k > 0 && k < I.nk - 1;
+}
+
+// sum_m W_m (Phi+ - Phi-)_m at an interior node (calc_RH_AD_WENO3 x aj dt)
+template <typename T>
+__device__ __forceinline__ T stage_rhs(const FieldsT<T>& f, const T* __restrict__ phi1, const Inst& I, long long l,
+                                       int i, int j, int k) {
+    const long long sj = I.ni, sk = (long long)I.ni * I.nj;
+    const T p = __ldg(phi1 + l);
+    T R;
+    {
+        const T w = __ldg(f.W[0] + l);
+        const T m2 = i > 1 ? __ldg(phi1 + l - 2) : T(0);
+        const T p2 = i < I.ni - 2 ? __ldg(phi1 + l + 2) : T(0);
+        R = w * weno_diff(m2, __ldg(phi1 + l - 1), p, __ldg(phi1 + l + 1), p2, w, i == 1, i == I.ni - 2);
+    }
+    {
+        const T w = __ldg(f.W[1] + l);
+        const T m2 = j > 1 ? __ldg(phi1 + l - 2 * sj) : T(0);
+        const T p2 = j < I.nj - 2 ? __ldg(phi1 + l + 2 * sj) : T(0);
+        R = vfma(w, weno_diff(m2, __ldg(phi1 + l - sj), p, __ldg(phi1 + l + sj), p2, w, j == 1, j == I.nj - 2), R);
+    }
+    {
+        const T w = __ldg(f.W[2] + l);
+        const T m2 = k > 1 ? __ldg(phi1 + l - 2 * sk) : T(0);
+        const T p2 = k < I.nk - 2 ? __ldg(phi1 + l + 2 * sk) : T(0);
+        R = vfma(w, weno_diff(m2, __ldg(phi1 + l - sk), p, __ldg(phi1 + l + sk), p2, w, k == 1, k == I.nk - 2), R);
+    }
+    return R;
+}
+
+template <typename T, int TX, int TY, int TZ>
 __global__ void __launch_bounds__(TX * TY * TZ) k_stage(const Inst* __restrict__ inst,
-        const int* __restrict__ brick_inst, int nbricks, Fields f, const float* __restrict__ phin,
-        const float* __restrict__ phi1, float* __restrict__ out, float c1, float c2, float c3) {
+        const int* __restrict__ brick_inst, int nbricks, FieldsT<T> f, const T* __restrict__ phin,
+        const T* __restrict__ phi1, T* __restrict__ out, T c1, T c2, T c3) {
     for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const auto b = brick_node<TX, TY, TZ>(inst, brick_inst, blk);
+        const Node b = brick_node<TX, TY, TZ>(inst, brick_inst, blk);
         if (!b.valid) continue;
         const Inst& I = inst[b.inst];
-        const long long sj = I.ni, sk = (long long)I.ni * I.nj;
-        const long long l = I.off + b.i + sj * b.j + sk * b.k;
-        const float p = __ldg(phi1 + l);
-        float R = 0.0f;
-        const bool interior = b.i > 0 && b.i < I.ni - 1 && b.j > 0 && b.j < I.nj - 1 && b.k > 0 && b.k < I.nk - 1;
-        if (interior) {
-            {
-                const float w = __ldg(f.W[0] + l);
-                const float m2 = b.i > 1 ? __ldg(phi1 + l - 2) : 0.0f;
-                const float p2 = b.i < I.ni - 2 ? __ldg(phi1 + l + 2) : 0.0f;
-                R = w * weno_diff(m2, __ldg(phi1 + l - 1), p, __ldg(phi1 + l + 1), p2, w, b.i == 1,
-                                  b.i == I.ni - 2);
-            }
-            {
-                const float w = __ldg(f.W[1] + l);
-                const float m2 = b.j > 1 ? __ldg(phi1 + l - 2 * sj) : 0.0f;
-                const float p2 = b.j < I.nj - 2 ? __ldg(phi1 + l + 2 * sj) : 0.0f;
-                R = fmaf(w, weno_diff(m2, __ldg(phi1 + l - sj), p, __ldg(phi1 + l + sj), p2, w, b.j == 1,
-                                      b.j == I.nj - 2), R);
-            }
-            {
-                const float w = __ldg(f.W[2] + l);
-                const float m2 = b.k > 1 ? __ldg(phi1 + l - 2 * sk) : 0.0f;
-                const float p2 = b.k < I.nk - 2 ? __ldg(phi1 + l + 2 * sk) : 0.0f;
-                R = fmaf(w, weno_diff(m2, __ldg(phi1 + l - sk), p, __ldg(phi1 + l + sk), p2, w, b.k == 1,
-                                      b.k == I.nk - 2), R);
-            }
-        }
-        out[l] = c1 * __ldg(phin + l) + c2 * p - c3 * R;
+        const long long l = I.off + b.i + (long long)I.ni * (b.j + (long long)I.nj * b.k);
+        const T R = interior(I, b.i, b.j, b.k) ? stage_rhs(f, phi1, I, l, b.i, b.j, b.k) : T(0);
+        out[l] = c1 * __ldg(phin + l) + c2 * __ldg(phi1 + l) - c3 * R;
     }
 }
 
 // ------------------------------------------------------------ bcond_lsm
-__device__ __forceinline__ float bc_rule(int type, float n1, float n2, float BigPhi) {
+template <typename T>
+__device__ __forceinline__ T bc_rule(int type, T n1, T n2, float BigPhi) {
     if (type == 0) return n1;
-    if (type == 1) return fabsf(n2) >= BigPhi ? n1 : (4.0f / 3.0f) * n1 - (1.0f / 3.0f) * n2;
-    return 2.0f * n1 - n2;  // type 2 on the im face
+    if (type == 1) return fabs(n2) >= T(BigPhi) ? n1 : T(4.0 / 3.0) * n1 - T(1.0 / 3.0) * n2;
+    return T(2) * n1 - n2;  // type 2 on the im face
 }
 __device__ __forceinline__ bool face_on(const BC& bc, int face) {
     const int t = bc.type[face];
     return t == 0 || t == 1 || (t == 2 && face == 1);
 }
 
-template <class P0>
-__device__ float bval_i(const BC& bc, const P0& p0, int ni, int i, int j, int k) {
-    if (i == 0 && face_on(bc, 0)) return bc_rule(bc.type[0], p0(1, j, k), p0(2, j, k), bc.BigPhi);
-    if (i == ni - 1 && face_on(bc, 1)) return bc_rule(bc.type[1], p0(i - 1, j, k), p0(i - 2, j, k), bc.BigPhi);
+template <typename T, class P0>
+__device__ T bval_i(const BC& bc, const P0& p0, int ni, int i, int j, int k) {
+    if (i == 0 && face_on(bc, 0)) return bc_rule<T>(bc.type[0], p0(1, j, k), p0(2, j, k), bc.BigPhi);
+    if (i == ni - 1 && face_on(bc, 1)) return bc_rule<T>(bc.type[1], p0(i - 1, j, k), p0(i - 2, j, k), bc.BigPhi);
     return p0(i, j, k);
 }
-template <class P0>
-__device__ float bval_j(const BC& bc, const P0& p0, int ni, int nj, int i, int j, int k) {
+template <typename T, class P0>
+__device__ T bval_j(const BC& bc, const P0& p0, int ni, int nj, int i, int j, int k) {
     if (j == 0 && face_on(bc, 2))
-        return bc_rule(bc.type[2], bval_i(bc, p0, ni, i, 1, k), bval_i(bc, p0, ni, i, 2, k), bc.BigPhi);
+        return bc_rule<T>(bc.type[2], bval_i<T>(bc, p0, ni, i, 1, k), bval_i<T>(bc, p0, ni, i, 2, k), bc.BigPhi);
     if (j == nj - 1 && face_on(bc, 3))
-        return bc_rule(bc.type[3], bval_i(bc, p0, ni, i, j - 1, k), bval_i(bc, p0, ni, i, j - 2, k), bc.BigPhi);
-    return bval_i(bc, p0, ni, i, j, k);
+        return bc_rule<T>(bc.type[3], bval_i<T>(bc, p0, ni, i, j - 1, k), bval_i<T>(bc, p0, ni, i, j - 2, k),
+                          bc.BigPhi);
+    return bval_i<T>(bc, p0, ni, i, j, k);
 }
-template <class P0>
-__device__ float bval_k(const BC& bc, const P0& p0, int ni, int nj, int nk, int i, int j, int k) {
+template <typename T, class P0>
+__device__ T bval_k(const BC& bc, const P0& p0, int ni, int nj, int nk, int i, int j, int k) {
     if (k == 0 && face_on(bc, 4))
-        return bc_rule(bc.type[4], bval_j(bc, p0, ni, nj, i, j, 1), bval_j(bc, p0, ni, nj, i, j, 2), bc.BigPhi);
+        return bc_rule<T>(bc.type[4], bval_j<T>(bc, p0, ni, nj, i, j, 1), bval_j<T>(bc, p0, ni, nj, i, j, 2),
+                          bc.BigPhi);
     if (k == nk - 1 && face_on(bc, 5))
-        return bc_rule(bc.type[5], bval_j(bc, p0, ni, nj, i, j, k - 1), bval_j(bc, p0, ni, nj, i, j, k - 2),
-                       bc.BigPhi);
-    return bval_j(bc, p0, ni, nj, i, j, k);
+        return bc_rule<T>(bc.type[5], bval_j<T>(bc, p0, ni, nj, i, j, k - 1), bval_j<T>(bc, p0, ni, nj, i, j, k - 2),
+                          bc.BigPhi);
+    return bval_j<T>(bc, p0, ni, nj, i, j, k);
 }
 
+template <typename T>
 struct P0Stage {
-    const float *phin, *phi1, *out;
+    const T *phin, *phi1, *out;
     long long off, sj, sk;
     int ni, nj, nk;
-    float c1, c2;
-    __device__ float operator()(int i, int j, int k) const {
+    T c1, c2;
+    __device__ T operator()(int i, int j, int k) const {
         const long long l = off + i + sj * j + sk * k;
         const bool bnd = i == 0 || i == ni - 1 || j == 0 || j == nj - 1 || k == 0 || k == nk - 1;
         return bnd ? c1 * phin[l] + c2 * phi1[l] : out[l];
     }
 };
+template <typename T>
 struct P0Src {
-    const float* src;
+    const T* src;
     long long off, sj, sk;
-    __device__ float operator()(int i, int j, int k) const { return src[off + i + sj * j + sk * k]; }
+    __device__ T operator()(int i, int j, int k) const { return src[off + i + sj * j + sk * k]; }
 };
 
-__global__ void k_bc_stage(const Inst* __restrict__ inst, int ninst, long long nface, BC bc,
-                           const float* __restrict__ phin, const float* __restrict__ phi1, float* out, float c1,
-                           float c2) {
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (t >= nface) return;
+__device__ __forceinline__ int face_instance(const Inst* __restrict__ inst, int ninst, long long t) {
     int lo = 0, hi = ninst - 1;
-    while (lo < hi) {  // last instance whose face0 <= t
+    while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
         if (inst[mid].face0 <= t) lo = mid; else hi = mid - 1;
     }
-    const Inst& I = inst[lo];
-    const long long r0 = t - I.face0;
-    const long long nI = (long long)I.nj * I.nk, nJ = (long long)I.ni * I.nk, nK = (long long)I.ni * I.nj;
-    int i, j, k;
-    long long r = r0;
-    if (r < 2 * nI) { i = r < nI ? 0 : I.ni - 1; r %= nI; j = (int)(r % I.nj); k = (int)(r / I.nj); }
-    else if ((r -= 2 * nI) < 2 * nJ) { j = r < nJ ? 0 : I.nj - 1; r %= nJ; i = (int)(r % I.ni); k = (int)(r / I.ni); }
-    else { r -= 2 * nJ; if (r >= 2 * nK) return; k = r < nK ? 0 : I.nk - 1; r %= nK; i = (int)(r % I.ni); j = (int)(r / I.ni); }
-    P0Stage p0{phin, phi1, out, I.off, I.ni, (long long)I.ni * I.nj, I.ni, I.nj, I.nk, c1, c2};
-    out[I.off + i + p0.sj * j + p0.sk * k] = bval_k(bc, p0, I.ni, I.nj, I.nk, i, j, k);
+    return lo;
 }
 
-template <int TX, int TY, int TZ>
+__device__ __forceinline__ bool face_coords(const Inst& I, long long r, int* pi, int* pj, int* pk) {
+    const long long nI = (long long)I.nj * I.nk, nJ = (long long)I.ni * I.nk, nK = (long long)I.ni * I.nj;
+    if (r < 2 * nI) { *pi = r < nI ? 0 : I.ni - 1; r %= nI; *pj = (int)(r % I.nj); *pk = (int)(r / I.nj); return true; }
+    r -= 2 * nI;
+    if (r < 2 * nJ) { *pj = r < nJ ? 0 : I.nj - 1; r %= nJ; *pi = (int)(r % I.ni); *pk = (int)(r / I.ni); return true; }
+    r -= 2 * nJ;
+    if (r >= 2 * nK) return false;
+    *pk = r < nK ? 0 : I.nk - 1; r %= nK; *pi = (int)(r % I.ni); *pj = (int)(r / I.ni);
+    return true;
+}
+
+template <typename T>
+__global__ void k_bc_stage(const Inst* __restrict__ inst, int ninst, long long nface, BC bc,
+                           const T* __restrict__ phin, const T* __restrict__ phi1, T* out, T c1, T c2) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= nface) return;
+    const Inst& I = inst[face_instance(inst, ninst, t)];
+    int i, j, k;
+    if (!face_coords(I, t - I.face0, &i, &j, &k)) return;
+    P0Stage<T> p0{phin, phi1, out, I.off, I.ni, (long long)I.ni * I.nj, I.ni, I.nj, I.nk, c1, c2};
+    out[I.off + i + p0.sj * j + p0.sk * k] = bval_k<T>(bc, p0, I.ni, I.nj, I.nk, i, j, k);
+}
+
+template <typename T, int TX, int TY, int TZ>
 __global__ void __launch_bounds__(TX * TY * TZ) k_bc_full(const Inst* __restrict__ inst,
-        const int* __restrict__ brick_inst, int nbricks, BC bc, const float* __restrict__ src,
-        float* __restrict__ dst, unsigned* err) {
+        const int* __restrict__ brick_inst, int nbricks, BC bc, const T* __restrict__ src, T* __restrict__ dst,
+        unsigned* err) {
     for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const auto b = brick_node<TX, TY, TZ>(inst, brick_inst, blk);
+        const Node b = brick_node<TX, TY, TZ>(inst, brick_inst, blk);
         if (!b.valid) continue;
         const Inst& I = inst[b.inst];
         const long long sj = I.ni, sk = (long long)I.ni * I.nj;
         const long long l = I.off + b.i + sj * b.j + sk * b.k;
         const bool bnd = b.i == 0 || b.i == I.ni - 1 || b.j == 0 || b.j == I.nj - 1 || b.k == 0 || b.k == I.nk - 1;
-        float v;
+        T v;
         if (bnd) {
-            P0Src p0{src, I.off, sj, sk};
-            v = bval_k(bc, p0, I.ni, I.nj, I.nk, b.i, b.j, b.k);
+            P0Src<T> p0{src, I.off, sj, sk};
+            v = bval_k<T>(bc, p0, I.ni, I.nj, I.nk, b.i, b.j, b.k);
         } else {
             v = src[l];
         }
         dst[l] = v;
-        if (err && !isfinite(v)) atomicOr(err, (unsigned)kErrNonFinite);
+        if (err && !vfinite(v)) atomicOr(err, (unsigned)kErrNonFinite);
     }
 }
 
 // ------------------------------------------------------------ Godunov |grad|
-// One-sided differences (calc_RH_RN.F90:36-170) contracted with the metrics
-// and the Godunov norm chosen by the sign (calc_RH_RN.F90:190-236), FP32.
-__device__ __forceinline__ float godunov(const Fields& f, const float* __restrict__ d, long long l, long long sj,
-                                         long long sk, int i, int j, int k, int ni, int nj, int nk, float s) {
-    const float c = __ldg(d + l);
-    float mas[3], men[3];
-    {
-        const float a = i < ni - 1 ? __ldg(d + l + 1) - c : 0.0f, bk = i > 0 ? c - __ldg(d + l - 1) : 0.0f;
-        mas[0] = i < ni - 1 ? a : bk; men[0] = i > 0 ? bk : a;
-    }
-    {
-        const float a = j < nj - 1 ? __ldg(d + l + sj) - c : 0.0f, bk = j > 0 ? c - __ldg(d + l - sj) : 0.0f;
-        mas[1] = j < nj - 1 ? a : bk; men[1] = j > 0 ? bk : a;
-    }
-    {
-        const float a = k < nk - 1 ? __ldg(d + l + sk) - c : 0.0f, bk = k > 0 ? c - __ldg(d + l - sk) : 0.0f;
-        mas[2] = k < nk - 1 ? a : bk; men[2] = k > 0 ? bk : a;
-    }
-    float acc = 0.0f;
+// One-sided differences (calc_RH_RN.F90:36-170) along one axis: mas
+// (forward) and men (backward); on a physical face both take the one
+// available difference.
+template <typename T>
+__device__ __forceinline__ void one_sided(const T* __restrict__ d, long long l, long long s, int c, int n, T* mas,
+                                          T* men) {
+    const T x = __ldg(d + l);
+    const T a = c < n - 1 ? __ldg(d + l + s) - x : T(0);
+    const T b = c > 0 ? x - __ldg(d + l - s) : T(0);
+    *mas = c < n - 1 ? a : b;
+    *men = c > 0 ? b : a;
+}
+
+template <typename T>
+__device__ __forceinline__ void godunov_diffs(const T* __restrict__ d, const Inst& I, long long l, int i, int j, int k,
+                                              T (&mas)[3], T (&men)[3]) {
+    one_sided(d, l, 1, i, I.ni, &mas[0], &men[0]);
+    one_sided(d, l, (long long)I.ni, j, I.nj, &mas[1], &men[1]);
+    one_sided(d, l, (long long)I.ni * I.nj, k, I.nk, &mas[2], &men[2]);
+}
+
+// Godunov norm (calc_RH_RN.F90:190-236) chosen by the sign s
+template <typename T>
+__device__ __forceinline__ T godunov(const FieldsT<T>& f, const T* __restrict__ d, const Inst& I, long long l, int i,
+                                     int j, int k, T s) {
+    T mas[3], men[3];
+    godunov_diffs(d, I, l, i, j, k, mas, men);
+    T acc = T(0);
 #pragma unroll
     for (int x = 0; x < 3; ++x) {
-        const float m0 = __ldg(f.m[x] + l), m1 = __ldg(f.m[3 + x] + l), m2 = __ldg(f.m[6 + x] + l);
-        const float bb = m0 * men[0] + m1 * men[1] + m2 * men[2];
-        const float ff = m0 * mas[0] + m1 * mas[1] + m2 * mas[2];
-        const float e = s > 0.0f ? fmaxf(fmaxf(bb, 0.0f) * fmaxf(bb, 0.0f), fminf(ff, 0.0f) * fminf(ff, 0.0f))
-                                 : fmaxf(fminf(bb, 0.0f) * fminf(bb, 0.0f), fmaxf(ff, 0.0f) * fmaxf(ff, 0.0f));
-        acc += e;
+        const T m0 = __ldg(f.m[x] + l), m1 = __ldg(f.m[3 + x] + l), m2 = __ldg(f.m[6 + x] + l);
+        const T bb = m0 * men[0] + m1 * men[1] + m2 * men[2];
+        const T ff = m0 * mas[0] + m1 * mas[1] + m2 * mas[2];
+        const T P = s > T(0) ? vmax(bb, T(0)) : vmin(bb, T(0));
+        const T Q = s > T(0) ? vmin(ff, T(0)) : vmax(ff, T(0));
+        acc += vmax(P * P, Q * Q);
     }
-    return sqrtf(acc);
+    return vsqrt(acc);
 }
 
 // calc_sign_ini (Kang sign) with the frozen band folded in: s = 0 where
 // |phi0| < eps and |grad phi0| > 0 (the lambda correction pins d to phi0).
-template <int TX, int TY, int TZ>
+template <typename T, int TX, int TY, int TZ>
 __global__ void __launch_bounds__(TX * TY * TZ) k_sign(const Inst* __restrict__ inst,
-        const int* __restrict__ brick_inst, int nbricks, Fields f, const float* __restrict__ phi0) {
+        const int* __restrict__ brick_inst, int nbricks, FieldsT<T> f, const T* __restrict__ phi0) {
     for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const auto b = brick_node<TX, TY, TZ>(inst, brick_inst, blk);
+        const Node b = brick_node<TX, TY, TZ>(inst, brick_inst, blk);
         if (!b.valid) continue;
         const Inst& I = inst[b.inst];
-        const long long sj = I.ni, sk = (long long)I.ni * I.nj;
-        const long long l = I.off + b.i + sj * b.j + sk * b.k;
-        const float p = __ldg(phi0 + l);
-        const float g = godunov(f, phi0, l, sj, sk, b.i, b.j, b.k, I.ni, I.nj, I.nk, p > 0.0f ? 1.0f : -1.0f);
-        float s;
-        if (p >= I.eps) s = 1.0f;
-        else if (p <= -I.eps) s = -1.0f;
-        else if (p != 0.0f && g > 0.0f) s = 0.0f;
-        else s = p / I.eps - (float)(1.0 / kPi) * sinf((float)kPi * p / I.eps);
+        const long long l = I.off + b.i + (long long)I.ni * (b.j + (long long)I.nj * b.k);
+        const T p = __ldg(phi0 + l);
+        const T eps = ipar<T>(I.eps, I.eps64);
+        const T g = godunov(f, phi0, I, l, b.i, b.j, b.k, p > T(0) ? T(1) : T(-1));
+        T s;
+        if (p >= eps) s = T(1);
+        else if (p <= -eps) s = T(-1);
+        else if (p != T(0) && g > T(0)) s = T(0);
+        else s = p / eps - T(1.0 / kPi) * vsin(T(kPi) * p / eps);
         f.sgn[l] = s;
     }
 }
 
-// one reinitialisation pseudo-step: d_out = d - dtau s (|grad d|_G - 1)
-template <int TX, int TY, int TZ>
+// one reinitialisation pseudo-step at a node: d - dtau s (|grad d|_G - 1)
+template <typename T>
+__device__ __forceinline__ T reinit_node(const FieldsT<T>& f, const T* __restrict__ din, const Inst& I, long long l,
+                                         int i, int j, int k) {
+    const T s = __ldg(f.sgn + l);
+    const T d = __ldg(din + l);
+    if (s == T(0)) return d;
+    const T g = godunov(f, din, I, l, i, j, k, s);
+    return d - ipar<T>(I.dtau, I.dtau64) * s * (g - T(1));
+}
+
+template <typename T, int TX, int TY, int TZ>
 __global__ void __launch_bounds__(TX * TY * TZ) k_reinit(const Inst* __restrict__ inst,
-        const int* __restrict__ brick_inst, int nbricks, Fields f, const float* __restrict__ din,
-        float* __restrict__ dout) {
+        const int* __restrict__ brick_inst, int nbricks, FieldsT<T> f, const T* __restrict__ din,
+        T* __restrict__ dout, unsigned* err) {
     for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const auto b = brick_node<TX, TY, TZ>(inst, brick_inst, blk);
+        const Node b = brick_node<TX, TY, TZ>(inst, brick_inst, blk);
         if (!b.valid) continue;
         const Inst& I = inst[b.inst];
-        const long long sj = I.ni, sk = (long long)I.ni * I.nj;
-        const long long l = I.off + b.i + sj * b.j + sk * b.k;
-        const float s = __ldg(f.sgn + l);
-        const float d = __ldg(din + l);
-        float r = d;
-        if (s != 0.0f) {
-            const float g = godunov(f, din, l, sj, sk, b.i, b.j, b.k, I.ni, I.nj, I.nk, s);
-            r = d - I.dtau * s * (g - 1.0f);
-        }
+        const long long l = I.off + b.i + (long long)I.ni * (b.j + (long long)I.nj * b.k);
+        const T r = reinit_node(f, din, I, l, b.i, b.j, b.k);
         dout[l] = r;
+        if (err && !vfinite(r)) atomicOr(err, (unsigned)kErrNonFinite);
     }
 }
 
+// P0 after the last pseudo-step: interior from its output, boundary nodes
+// recomputed from its input (their output slots are being overwritten).
+template <typename T>
+struct P0Reinit {
+    FieldsT<T> f;
+    const T *din, *dout;
+    const Inst* I;
+    __device__ T operator()(int i, int j, int k) const {
+        const long long l = I->off + i + (long long)I->ni * (j + (long long)I->nj * k);
+        const bool bnd = i == 0 || i == I->ni - 1 || j == 0 || j == I->nj - 1 || k == 0 || k == I->nk - 1;
+        return bnd ? reinit_node(f, din, *I, l, i, j, k) : dout[l];
+    }
+};
+
+template <typename T>
+__global__ void k_bc_reinit(const Inst* __restrict__ inst, int ninst, long long nface, BC bc, FieldsT<T> f,
+                            const T* __restrict__ din, T* dout) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= nface) return;
+    const Inst& I = inst[face_instance(inst, ninst, t)];
+    int i, j, k;
+    if (!face_coords(I, t - I.face0, &i, &j, &k)) return;
+    P0Reinit<T> p0{f, din, dout, &I};
+    dout[I.off + i + (long long)I.ni * (j + (long long)I.nj * k)] = bval_k<T>(bc, p0, I.ni, I.nj, I.nk, i, j, k);
+}
+
 // ------------------------------------------------------------ volume (FP64)
-template <int TX, int TY, int TZ>
+// Water volume of one tetrahedron of an interface cell: the same regions as
+// MarchingTetrahedron + GetWaterVolume (src/TetrahedronMethods.F90:26-954),
+// each sub-tetrahedron's share of the tetrahedron evaluated in barycentric
+// closed form: one FP64 determinant per tetrahedron instead of up to four
+// (equal in exact arithmetic, rounding differs).
+__device__ __forceinline__ double tet_water(const double (&V)[4][3], const double (&ph)[4]) {
+    const double TV = tetvol_fast(V[0], V[1], V[2], V[3]);
+    int s[4], nz = 0, fi = 0;
+    bool allp = true, alln = true, allge = true, allle = true;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        s[v] = ph[v] > kTinyD ? 1 : (ph[v] < -kTinyD ? -1 : 0);
+        allp &= s[v] == 1; alln &= s[v] == -1; nz += s[v] == 0;
+        allge &= s[v] >= 0; allle &= s[v] <= 0;
+        if (s[v] == -1) fi |= 1 << v;
+    }
+    if (allp) return TV;
+    if (alln) return 0.0;
+    if (nz > 0 && (allge || allle)) {
+        // the reference's zero-vertex cases: full or empty tetrahedron
+        int water = -1;
+        if (nz == 1) {
+            if (s[0] == 0) water = s[1] == 1; else if (s[1] == 0) water = s[0] == 1;
+            else if (s[2] == 0) water = s[0] == 1; else water = s[0] == 1;
+        } else if (nz == 2) {
+            if (s[0] == 0 && s[1] == 0) water = s[2] == 1;
+            else if (s[1] == 0 && s[2] == 0) water = s[0] == 1;
+            else if (s[2] == 0 && s[0] == 0) water = s[1] == 1;
+            else if (s[0] == 0 && s[3] == 0) water = s[1] == 1;
+            else if (s[1] == 0 && s[3] == 0) water = s[0] == 1;
+            else water = s[0] == 1;
+        } else if (nz == 3) {
+            for (int v = 0; v < 4; ++v) if (s[v] != 0) { water = s[v] == 1; break; }
+        }
+        return water == 0 ? 0.0 : TV;   // four zero vertices: full (FlagIndex 0)
+    }
+    // one vertex isolated from the other three (cases 2/15, 3/14, 5/12, 9/8)
+    int iso = -1;
+    if (fi == 1 || fi == 14) iso = 0; else if (fi == 2 || fi == 13) iso = 1;
+    else if (fi == 4 || fi == 11) iso = 2; else if (fi == 8 || fi == 7) iso = 3;
+    if (iso >= 0) {
+        double fr = 1.0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k != iso) fr *= ph[iso] / (ph[iso] - ph[k]);
+        const double AV = TV * fr;
+        return (s[iso] == -1) ? TV - AV : AV;   // isolated vertex negative: the rest is water
+    }
+    // two against two (cases 4/13, 6/11, 7/10): pair (A, B) as listed by the
+    // reference's sub-tetrahedra, C, D the other pair
+    int A, B, C, D;
+    if (fi == 3 || fi == 12) { A = 0; B = 1; C = 2; D = 3; }
+    else if (fi == 5 || fi == 10) { A = 0; B = 2; C = 1; D = 3; }
+    else { A = 1; B = 2; C = 0; D = 3; }
+    const double aC = ph[A] / (ph[A] - ph[C]), aD = ph[A] / (ph[A] - ph[D]);
+    const double bC = ph[B] / (ph[B] - ph[C]), bD = ph[B] / (ph[B] - ph[D]);
+    const double AV = TV * (aC * aD * (1.0 - bD) + aC * bD * (1.0 - bC) + bC * bD);
+    return (s[A] == -1) ? TV - AV : AV;
+}
+
+// CellAnalysis's split of an interface cell (src/TetrahedronMethods.F90:
+// 1823-2121): phase-change tetrahedra -> K, all-water tetrahedra -> S
+__device__ void cell_water_fast(const double (&P)[8], const double (&C)[8][3], double* K, double* S) {
+    double k = 0.0, s2 = 0.0;
+    bool pcc = false;
+#pragma unroll
+    for (int v = 0; v < 8; ++v) pcc |= fabs(P[v]) < kEpsSims;
+    if (!pcc) {
+        const double sg = copysign(1.0, P[0]);
+        for (int v = 1; v < 8; ++v)
+            if (sg * P[v] < 0.0) { pcc = true; break; }
+    }
+    if (pcc) {
+        for (int t = 0; t < 6; ++t) {
+            bool pct = false, second = true;
+            const double pa = P[c_tets[t][0]];
+            if (pa <= kEpsSims) second = false;
+            if (fabs(pa) < kEpsSims) pct = true;
+            const double sg = copysign(1.0, pa);
+            for (int v = 1; v < 4; ++v) {
+                const double pb = P[c_tets[t][v]];
+                if (sg * pb < 0.0 || fabs(pb) < kEpsSims) {
+                    if (pb <= kEpsSims) second = false;
+                    pct = true;
+                }
+            }
+            if (!pct && !second) continue;
+            double V[4][3], ph[4];
+            for (int v = 0; v < 4; ++v) {
+                const int cv = c_tets[t][v];
+                V[v][0] = C[cv][0]; V[v][1] = C[cv][1]; V[v][2] = C[cv][2];
+                ph[v] = P[cv];
+            }
+            if (pct) k += tet_water(V, ph);
+            else s2 += tetvol_fast(V[0], V[1], V[2], V[3]);
+        }
+    }
+    *K = k; *S = s2;
+}
+
+// Cells are classified against eps_sims = 2^-52 (exact in FP32, so the
+// comparisons equal the reference's FP64 ones on the same values).  Bulk
+// water cells add their precomputed fixed-point hexahedron volume; the block
+// then packs its interface cells into the first lanes (ballot + prefix, in
+// cell order) so the FP64 geometry runs on dense warps.  Sums are 64-bit
+// integers (exact, order-independent).
+__device__ __forceinline__ long long warp_sum_ll(long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <typename T, int TX, int TY, int TZ>
 __global__ void __launch_bounds__(TX * TY * TZ) k_volume(const Inst* __restrict__ inst,
-        const int* __restrict__ brick_inst, int nbricks, Fields f, const float* __restrict__ phi,
-        double* __restrict__ partials) {
-    constexpr int NT = TX * TY * TZ;
-    __shared__ double sh[3][NT / 32];
+        const int* __restrict__ brick_inst, int nbricks, FieldsT<T> f, const T* __restrict__ phi,
+        long long* __restrict__ partials) {
+    constexpr int NT = TX * TY * TZ, NW = NT / 32;
+    const T eps = T(2.220446049250313e-16);
+    __shared__ long long sh[3][NW];
+    __shared__ long long mixed[NT];
+    __shared__ int wcount[NW];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const auto b = brick_node<TX, TY, TZ>(inst, brick_inst, blk);
+        const Node b = brick_node<TX, TY, TZ>(inst, brick_inst, blk);
         const Inst& I = inst[b.inst];
-        double K = 0.0, S = 0.0, B = 0.0;
+        const long long sj = I.ni, sk = (long long)I.ni * I.nj;
+        long long Kq = 0, Sq = 0, Bq = 0;
+        bool mix = false;
+        long long l = 0;
         if (b.i < I.ni - 1 && b.j < I.nj - 1 && b.k < I.nk - 1) {
-            const long long sj = I.ni, sk = (long long)I.ni * I.nj;
-            const long long l = I.off + b.i + sj * b.j + sk * b.k;
+            l = I.off + b.i + sj * b.j + sk * b.k;
             const long long o[8] = {l, l + 1, l + 1 + sj, l + sj, l + sk, l + 1 + sk, l + 1 + sj + sk, l + sj + sk};
-            double P[8];
             bool allw = true, alla = true;
 #pragma unroll
             for (int v = 0; v < 8; ++v) {
+                const T p = __ldg(phi + o[v]);
+                allw &= p > eps; alla &= p < -eps;
+            }
+            if (allw) Bq = __ldg(f.cellfix + l);
+            mix = !allw && !alla;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, mix);
+        if (lane == 0) wcount[w] = __popc(m);
+        __syncthreads();
+        int base = 0, total = 0;
+        for (int q = 0; q < NW; ++q) { base += q < w ? wcount[q] : 0; total += wcount[q]; }
+        if (mix) mixed[base + __popc(m & ((1u << lane) - 1u))] = l;
+        __syncthreads();
+        if (threadIdx.x < total) {
+            const long long c = mixed[threadIdx.x];
+            const long long o[8] = {c, c + 1, c + 1 + sj, c + sj, c + sk, c + 1 + sk, c + 1 + sj + sk, c + sj + sk};
+            double P[8], C[8][3];
+#pragma unroll
+            for (int v = 0; v < 8; ++v) {
                 P[v] = (double)__ldg(phi + o[v]);
-                allw &= P[v] > kEpsSims; alla &= P[v] < -kEpsSims;
+                C[v][0] = __ldg(f.xyz[0] + o[v]); C[v][1] = __ldg(f.xyz[1] + o[v]); C[v][2] = __ldg(f.xyz[2] + o[v]);
             }
-            if (!alla) {
-                double C[8][3];
-#pragma unroll
-                for (int v = 0; v < 8; ++v) {
-                    C[v][0] = __ldg(f.xyz[0] + o[v]); C[v][1] = __ldg(f.xyz[1] + o[v]); C[v][2] = __ldg(f.xyz[2] + o[v]);
-                }
-                if (allw) B = hex_volume(C);
-                else cell_analysis(P, C, &K, &S, nullptr);
-            }
+            double K = 0.0, S = 0.0;
+            cell_water_fast(P, C, &K, &S);
+            Kq = __double2ll_rn(K * kVolScale);
+            Sq = __double2ll_rn(S * kVolScale);
         }
-        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            K += __shfl_down_sync(0xffffffffu, K, o);
-            S += __shfl_down_sync(0xffffffffu, S, o);
-            B += __shfl_down_sync(0xffffffffu, B, o);
-        }
-        if (lane == 0) { sh[0][w] = K; sh[1][w] = S; sh[2][w] = B; }
+        Kq = warp_sum_ll(Kq); Sq = warp_sum_ll(Sq); Bq = warp_sum_ll(Bq);
+        if (lane == 0) { sh[0][w] = Kq; sh[1][w] = Sq; sh[2][w] = Bq; }
         __syncthreads();
         if (threadIdx.x < 3) {
-            double acc = 0.0;
-            for (int q = 0; q < NT / 32; ++q) acc += sh[threadIdx.x][q];
+            long long acc = 0;
+            for (int q = 0; q < NW; ++q) acc += sh[threadIdx.x][q];
             partials[3 * (long long)blk + threadIdx.x] = acc;
         }
         __syncthreads();
     }
 }
 
-// one block per instance folds its bricks' partials in brick order
+// one block per instance sums its bricks' partials (exact integer sums)
 __global__ void __launch_bounds__(256) k_volume_final(const Inst* __restrict__ inst, int ninst, int nbricks,
-                                                      const double* __restrict__ partials, double* __restrict__ vols) {
+                                                      const long long* __restrict__ partials, double* __restrict__ vols) {
     const int b = blockIdx.x;
     if (b >= ninst) return;
     const int first = inst[b].brick0;
     const int last = b + 1 < ninst ? inst[b + 1].brick0 : nbricks;
-    __shared__ double sh[3][8];
-    double acc[3] = {0.0, 0.0, 0.0};
+    __shared__ long long sh[3][8];
+    long long acc[3] = {0, 0, 0};
     for (int q = first + threadIdx.x; q < last; q += 256)
         for (int c = 0; c < 3; ++c) acc[c] += partials[3 * (long long)q + c];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int c = 0; c < 3; ++c) {
-        double v = acc[c];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        const long long v = warp_sum_ll(acc[c]);
         if (lane == 0) sh[c][w] = v;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double v[3];
+        long long v[3];
         for (int c = 0; c < 3; ++c) {
-            double a = 0.0;
+            long long a = 0;
             for (int q = 0; q < 8; ++q) a += sh[c][q];
             v[c] = a;
         }
-        vols[4 * b] = v[0]; vols[4 * b + 1] = v[1]; vols[4 * b + 2] = v[2];
-        vols[4 * b + 3] = v[0] + v[1] + v[2];
+        vols[4 * b] = (double)v[0] * kVolUnit;
+        vols[4 * b + 1] = (double)v[1] * kVolUnit;
+        vols[4 * b + 2] = (double)v[2] * kVolUnit;
+        vols[4 * b + 3] = (double)(v[0] + v[1] + v[2]) * kVolUnit;
     }
 }
 
-template <template <int, int, int> class Fn, class... A>
+// fixed-point Davies-Salmond volume of every cell of one instance
+__global__ void k_cell_hex(long long off, int ni, int nj, int nk, const double* __restrict__ x,
+                           const double* __restrict__ y, const double* __restrict__ z, long long* __restrict__ cellfix) {
+    const long long ncell = (long long)(ni - 1) * (nj - 1) * (nk - 1);
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncell;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(c % (ni - 1)), j = (int)((c / (ni - 1)) % (nj - 1));
+        const int k = (int)(c / ((long long)(ni - 1) * (nj - 1)));
+        const long long sj = ni, sk = (long long)ni * nj;
+        const long long l = off + i + sj * j + sk * k;
+        const long long o[8] = {l, l + 1, l + 1 + sj, l + sj, l + sk, l + 1 + sk, l + 1 + sj + sk, l + sj + sk};
+        double C[8][3];
+#pragma unroll
+        for (int v = 0; v < 8; ++v) { C[v][0] = x[o[v]]; C[v][1] = y[o[v]]; C[v][2] = z[o[v]]; }
+        cellfix[l] = __double2ll_rn(hex_volume(C) * kVolScale);
+    }
+}
+
+// ================================================================ adjoint
+// Reverse of face `face` of bcond_lsm: for every node b of that face plane,
+// lam(n1) += a lam(b), lam(n2) += c lam(b), lam(b) = 0, with (a, c) the
+// face rule's weights (the BigPhi switch evaluated on the forward value of
+// n2 at that point of the face sequence).  Distinct nodes of one plane have
+// distinct targets, so the kernel needs no atomics.
+template <typename T, class P0>
+__device__ __forceinline__ T prev_value(const BC& bc, const P0& p0, int face, int ni, int nj, int i, int j, int k) {
+    if (face < 2) return p0(i, j, k);
+    if (face < 4) return bval_i<T>(bc, p0, ni, i, j, k);
+    return bval_j<T>(bc, p0, ni, nj, i, j, k);
+}
+
+template <typename T>
+__global__ void k_adj_face(Flat fl, int face, long long nplane, BC bc, int kind, const T* __restrict__ phin,
+                           const T* __restrict__ in, const T* __restrict__ out, T c1, T c2, T* lam) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= nplane || !face_on(bc, face)) return;
+    const int ax = face >> 1;
+    int lo = 0, hi = fl.ninst - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (fl.inst[mid].fpre[ax] <= t) lo = mid; else hi = mid - 1;
+    }
+    const Inst& I = fl.inst[lo];
+    const long long r = t - I.fpre[ax];
+    int i, j, k;
+    if (ax == 0) { i = (face == 0) ? 0 : I.ni - 1; j = (int)(r % I.nj); k = (int)(r / I.nj); }
+    else if (ax == 1) { j = (face == 2) ? 0 : I.nj - 1; i = (int)(r % I.ni); k = (int)(r / I.ni); }
+    else { k = (face == 4) ? 0 : I.nk - 1; i = (int)(r % I.ni); j = (int)(r / I.ni); }
+    const int dir = (face & 1) ? -1 : 1;     // inward direction
+    const long long sj = I.ni, sk = (long long)I.ni * I.nj;
+    const long long st = ax == 0 ? 1 : (ax == 1 ? sj : sk);
+    const long long l = I.off + i + sj * j + sk * k;
+    const T g = lam[l];
+    T a, c;
+    const int type = bc.type[face];
+    if (type == 0) { a = T(1); c = T(0); }
+    else if (type == 2) { a = T(2); c = T(-1); }
+    else {
+        const int i2 = ax == 0 ? i + 2 * dir : i, j2 = ax == 1 ? j + 2 * dir : j, k2 = ax == 2 ? k + 2 * dir : k;
+        T v2;
+        if (kind == 0) {
+            P0Stage<T> p0{phin, in, out, I.off, sj, sk, I.ni, I.nj, I.nk, c1, c2};
+            v2 = prev_value<T>(bc, p0, face, I.ni, I.nj, i2, j2, k2);
+        } else {
+            P0Src<T> p0{out, I.off, sj, sk};
+            v2 = prev_value<T>(bc, p0, face, I.ni, I.nj, i2, j2, k2);
+        }
+        if (fabs(v2) >= T(bc.BigPhi)) { a = T(1); c = T(0); }
+        else { a = T(4.0 / 3.0); c = T(-1.0 / 3.0); }
+    }
+    lam[l + dir * st] += a * g;
+    lam[l + 2 * dir * st] += c * g;
+    lam[l] = T(0);
+}
+
+// Reverse of one RK stage: node j gathers from the interior nodes i whose
+// WENO stencils contain it (i = j + o e_m, |o| <= 2).
+template <typename T>
+__global__ void k_adj_stage(Flat fl, FieldsT<T> f, const T* __restrict__ in, const T* __restrict__ lamP0,
+                            T* __restrict__ lam_in, T* __restrict__ lamPhin, T* __restrict__ lamW0,
+                            T* __restrict__ lamW1, T* __restrict__ lamW2, T c1, T c2, T c3, int last) {
+    const long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    Node nd;
+    if (!flat_node(fl, l, &nd)) return;
+    const Inst& I = fl.inst[nd.inst];
+    const int n3[3] = {I.ni, I.nj, I.nk};
+    const int c3d[3] = {nd.i, nd.j, nd.k};
+    const long long st[3] = {1, (long long)I.ni, (long long)I.ni * I.nj};
+    T* lamW[3] = {lamW0, lamW1, lamW2};
+    const T lp = lamP0[l];
+    T acc = T(0);
+    const bool jint = interior(I, nd.i, nd.j, nd.k);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        const int cm = c3d[m], nm = n3[m];
+        const long long s = st[m];
+        // the other two coordinates must be interior for any node on this line to be interior
+        bool line_ok = true;
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+            if (q != m && (c3d[q] < 1 || c3d[q] > n3[q] - 2)) line_ok = false;
+        // values of `in` along the line at offsets -4..4 (zero outside)
+        T v[9];
+#pragma unroll
+        for (int q = -4; q <= 4; ++q) {
+            const int cq = cm + q;
+            v[q + 4] = (line_ok && cq >= 0 && cq < nm) ? __ldg(in + l + q * s) : T(0);
+        }
+        if (line_ok) {
+#pragma unroll
+            for (int o = -2; o <= 2; ++o) {
+                const int ci = cm + o;
+                if (ci < 1 || ci > nm - 2) continue;
+                const long long li = l + o * s;
+                const T w = __ldg(f.W[m] + li);
+                const T lpi = __ldg(lamP0 + li);
+                // stencil of node i (positions ci-2..ci+2); the forward zeroes
+                // the unused outer value on the forced faces
+                T sv[5] = {v[o + 2], v[o + 3], v[o + 4], v[o + 5], v[o + 6]};
+                if (ci <= 1) sv[0] = T(0);
+                if (ci >= nm - 2) sv[4] = T(0);
+                T g[5];
+                weno_diff_grad(sv, w, ci == 1, ci == nm - 2, g);
+                acc = vfma(lpi * w, g[2 - o], acc);    // j sits at offset -o in node i's stencil
+            }
+        }
+        if (jint) {
+            T sv[5] = {v[2], v[3], v[4], v[5], v[6]};
+            if (cm <= 1) sv[0] = T(0);
+            if (cm >= nm - 2) sv[4] = T(0);
+            const T w = __ldg(f.W[m] + l);
+            const T D = weno_diff(sv[0], sv[1], sv[2], sv[3], sv[4], w, cm == 1, cm == nm - 2);
+            lamW[m][l] -= c3 * lp * D;
+        }
+    }
+    T r = c2 * lp - c3 * acc;
+    if (last) {
+        r += lamPhin[l] + c1 * lp;
+        lamPhin[l] = T(0);
+    } else {
+        lamPhin[l] += c1 * lp;
+    }
+    lam_in[l] = r;
+}
+
+// Reinitialisation adjoint, pass 1: per node i with s != 0, w = dtau s lam(i)
+// and the Godunov selections of the forward pass; A_m = w dG/dmen_m,
+// B_m = w dG/dmas_m (a physical face's single difference goes to B on the
+// low face, to A on the high face).
+template <typename T>
+__global__ void k_adj_reinit_coef(Flat fl, FieldsT<T> f, const T* __restrict__ d, const T* __restrict__ lam,
+                                  T* __restrict__ coef) {
+    const long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    Node nd;
+    if (!flat_node(fl, l, &nd)) return;
+    const Inst& I = fl.inst[nd.inst];
+    const T s = __ldg(f.sgn + l);
+    T A[3] = {T(0), T(0), T(0)}, B[3] = {T(0), T(0), T(0)};
+    if (s != T(0)) {
+        T mas[3], men[3];
+        godunov_diffs(d, I, l, nd.i, nd.j, nd.k, mas, men);
+        T db[3], df[3], acc = T(0);
+        T M[3][3];
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+            M[0][x] = __ldg(f.m[x] + l); M[1][x] = __ldg(f.m[3 + x] + l); M[2][x] = __ldg(f.m[6 + x] + l);
+            const T bb = M[0][x] * men[0] + M[1][x] * men[1] + M[2][x] * men[2];
+            const T ff = M[0][x] * mas[0] + M[1][x] * mas[1] + M[2][x] * mas[2];
+            const T P = s > T(0) ? vmax(bb, T(0)) : vmin(bb, T(0));
+            const T Q = s > T(0) ? vmin(ff, T(0)) : vmax(ff, T(0));
+            const bool takeP = P * P >= Q * Q;
+            acc += takeP ? P * P : Q * Q;
+            db[x] = takeP ? T(2) * P : T(0);     // d e_x / d b_x (the clip is inside P)
+            df[x] = takeP ? T(0) : T(2) * Q;
+        }
+        const T G = vsqrt(acc);
+        if (G > T(0)) {
+            const T wgt = ipar<T>(I.dtau, I.dtau64) * s * __ldg(lam + l) / (T(2) * G);
+            const int c3d[3] = {nd.i, nd.j, nd.k};
+            const int n3[3] = {I.ni, I.nj, I.nk};
+#pragma unroll
+            for (int m = 0; m < 3; ++m) {
+                const T gmen = M[m][0] * db[0] + M[m][1] * db[1] + M[m][2] * db[2];
+                const T gmas = M[m][0] * df[0] + M[m][1] * df[1] + M[m][2] * df[2];
+                if (c3d[m] == 0) { A[m] = T(0); B[m] = wgt * (gmen + gmas); }
+                else if (c3d[m] == n3[m] - 1) { A[m] = wgt * (gmen + gmas); B[m] = T(0); }
+                else { A[m] = wgt * gmen; B[m] = wgt * gmas; }
+            }
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        coef[(2 * m) * fl.n + l] = A[m];
+        coef[(2 * m + 1) * fl.n + l] = B[m];
+    }
+}
+
+// pass 2: lam_out(j) = lam(j) - sum_m [A_m(j) - B_m(j) - A_m(j+e_m) + B_m(j-e_m)]
+template <typename T>
+__global__ void k_adj_reinit_apply(Flat fl, const T* __restrict__ lam, const T* __restrict__ coef,
+                                   T* __restrict__ lam_out) {
+    const long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    Node nd;
+    if (!flat_node(fl, l, &nd)) return;
+    const Inst& I = fl.inst[nd.inst];
+    const int c3d[3] = {nd.i, nd.j, nd.k};
+    const int n3[3] = {I.ni, I.nj, I.nk};
+    const long long st[3] = {1, (long long)I.ni, (long long)I.ni * I.nj};
+    T r = __ldg(lam + l);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        const T* A = coef + (2 * m) * fl.n;
+        const T* B = coef + (2 * m + 1) * fl.n;
+        T t = __ldg(A + l) - __ldg(B + l);
+        if (c3d[m] < n3[m] - 1) t -= __ldg(A + l + st[m]);
+        if (c3d[m] > 0) t += __ldg(B + l - st[m]);
+        r -= t;
+    }
+    lam_out[l] = r;
+}
+
+template <typename T>
+__global__ void k_adj_contra(Flat fl, FieldsT<T> f, const T* __restrict__ w0, const T* __restrict__ w1,
+                             const T* __restrict__ w2, T* __restrict__ u0, T* __restrict__ u1, T* __restrict__ u2) {
+    const long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    Node nd;
+    if (!flat_node(fl, l, &nd)) return;
+    const T dt = ipar<T>(fl.inst[nd.inst].dt, fl.inst[nd.inst].dt64);
+    const T lw[3] = {w0[l], w1[l], w2[l]};
+    T* out[3] = {u0, u1, u2};
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+        out[c][l] += dt * (f.m[c][l] * lw[0] + f.m[3 + c][l] * lw[1] + f.m[6 + c][l] * lw[2]);
+}
+
+// ------------------------------------------------------------ dispatch
+template <template <typename, int, int, int> class Fn, typename T, class... A>
 void dispatch(int shape, A... a) {
-    switch (shape) {
-    case 0: Fn<32, 4, 2>::run(a...); break;
-    case 1: Fn<32, 8, 1>::run(a...); break;
-    case 2: Fn<64, 4, 1>::run(a...); break;
-    case 3: Fn<32, 2, 4>::run(a...); break;
-    default: Fn<128, 2, 1>::run(a...); break;
+    if constexpr (sizeof(T) == 8) {
+        (void)shape;
+        Fn<T, 32, 4, 2>::run(a...);   // FP64 (gradient checks): one tile shape
+    } else {
+        switch (shape) {
+        case 0: Fn<T, 32, 4, 2>::run(a...); break;
+        case 1: Fn<T, 32, 8, 1>::run(a...); break;
+        case 2: Fn<T, 64, 4, 1>::run(a...); break;
+        case 3: Fn<T, 32, 2, 4>::run(a...); break;
+        default: Fn<T, 128, 2, 1>::run(a...); break;
+        }
     }
 }
 
-#define LSM_BATCH_RUNNER(NAME, KERNEL, PARAMS, ARGS)                                     \
-    template <int TX, int TY, int TZ>                                                    \
-    struct NAME {                                                                         \
-        static void run PARAMS {                                                          \
-            ProfScope ps_(#KERNEL, s);                                                    \
-            KERNEL<TX, TY, TZ><<<grid, TX * TY * TZ, 0, s>>> ARGS;                        \
-        }                                                                                 \
+#define LSM_BATCH_RUNNER(NAME, KERNEL, PARAMS, ARGS)                                   \
+    template <typename T, int TX, int TY, int TZ>                                      \
+    struct NAME {                                                                       \
+        static void run PARAMS {                                                        \
+            ProfScope ps_(#KERNEL, s);                                                  \
+            KERNEL<T, TX, TY, TZ><<<grid, TX * TY * TZ, 0, s>>> ARGS;                   \
+        }                                                                               \
     };
 
 LSM_BATCH_RUNNER(RunContra, k_contra,
-                 (int grid, const Inst* inst, const int* bi, int nb, Fields f, float a, float b, float c, cudaStream_t s),
-                 (inst, bi, nb, f, a, b, c))
+                 (int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, cudaStream_t s),
+                 (inst, bi, nb, f))
 LSM_BATCH_RUNNER(RunStage, k_stage,
-                 (int grid, const Inst* inst, const int* bi, int nb, Fields f, const float* pn, const float* p1,
-                  float* out, float c1, float c2, float c3, cudaStream_t s),
-                 (inst, bi, nb, f, pn, p1, out, c1, c2, c3))
+                 (int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, const T* pn, const T* p1, T* out,
+                  double c1, double c2, double c3, cudaStream_t s),
+                 (inst, bi, nb, f, pn, p1, out, T(c1), T(c2), T(c3)))
 LSM_BATCH_RUNNER(RunBcFull, k_bc_full,
-                 (int grid, const Inst* inst, const int* bi, int nb, BC bc, const float* src, float* dst, unsigned* err,
+                 (int grid, const Inst* inst, const int* bi, int nb, BC bc, const T* src, T* dst, unsigned* err,
                   cudaStream_t s),
                  (inst, bi, nb, bc, src, dst, err))
 LSM_BATCH_RUNNER(RunSign, k_sign,
-                 (int grid, const Inst* inst, const int* bi, int nb, Fields f, const float* p0, cudaStream_t s),
+                 (int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, const T* p0, cudaStream_t s),
                  (inst, bi, nb, f, p0))
 LSM_BATCH_RUNNER(RunReinit, k_reinit,
-                 (int grid, const Inst* inst, const int* bi, int nb, Fields f, const float* din, float* dout,
-                  cudaStream_t s),
-                 (inst, bi, nb, f, din, dout))
+                 (int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, const T* din, T* dout,
+                  unsigned* err, cudaStream_t s),
+                 (inst, bi, nb, f, din, dout, err))
 LSM_BATCH_RUNNER(RunVolume, k_volume,
-                 (int grid, const Inst* inst, const int* bi, int nb, Fields f, const float* phi, double* part,
+                 (int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, const T* phi, long long* part,
                   cudaStream_t s),
                  (inst, bi, nb, f, phi, part))
 
-template <int TX, int TY, int TZ>
+template <typename T, int TX, int TY, int TZ>
 struct Occupancy {
     static void run(int kernel, int* out) {
         const int nt = TX * TY * TZ;
         switch (kernel) {
-        case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_stage<TX, TY, TZ>, nt, 0); break;
-        case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_reinit<TX, TY, TZ>, nt, 0); break;
-        default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_volume<TX, TY, TZ>, nt, 0); break;
+        case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_stage<T, TX, TY, TZ>, nt, 0); break;
+        case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_reinit<T, TX, TY, TZ>, nt, 0); break;
+        default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_volume<T, TX, TY, TZ>, nt, 0); break;
         }
     }
 };
 
+inline unsigned flat_blocks(long long n) { return (unsigned)((n + 255) / 256); }
+
 }  // namespace
 
-void contra(int shape, int grid, const Inst* inst, const int* bi, int nb, Fields f, float dcm[3], cudaStream_t s) {
-    dispatch<RunContra>(shape, grid, inst, bi, nb, f, dcm[0], dcm[1], dcm[2], s);
+// ------------------------------------------------------------ launchers
+template <typename T>
+void contra(int shape, int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, cudaStream_t s) {
+    dispatch<RunContra, T>(shape, grid, inst, bi, nb, f, s);
 }
-void stage(int shape, int grid, const Inst* inst, const int* bi, int nb, Fields f, const float* phin,
-           const float* phi1, float* out, float c1, float c2, float c3, cudaStream_t s) {
-    dispatch<RunStage>(shape, grid, inst, bi, nb, f, phin, phi1, out, c1, c2, c3, s);
+template <typename T>
+void stage(int shape, int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, const T* phin, const T* phi1,
+           T* out, double c1, double c2, double c3, cudaStream_t s) {
+    dispatch<RunStage, T>(shape, grid, inst, bi, nb, f, phin, phi1, out, c1, c2, c3, s);
 }
-void bc_stage(const Inst* inst, int ninst, long long nface, Fields f, BC bc, const float* phin, const float* phi1,
-              float* out, float c1, float c2, cudaStream_t s) {
-    (void)f;
+template <typename T>
+void bc_stage(const Inst* inst, int ninst, long long nface, BC bc, const T* phin, const T* phi1, T* out, double c1,
+              double c2, cudaStream_t s) {
     ProfScope ps_("k_bc_stage", s);
-    k_bc_stage<<<(unsigned)((nface + 255) / 256), 256, 0, s>>>(inst, ninst, nface, bc, phin, phi1, out, c1, c2);
+    k_bc_stage<T><<<flat_blocks(nface), 256, 0, s>>>(inst, ninst, nface, bc, phin, phi1, out, T(c1), T(c2));
 }
-void bc_full(int shape, int grid, const Inst* inst, const int* bi, int nb, BC bc, const float* src, float* dst,
-             unsigned* err, cudaStream_t s) {
-    dispatch<RunBcFull>(shape, grid, inst, bi, nb, bc, src, dst, err, s);
+template <typename T>
+void bc_full(int shape, int grid, const Inst* inst, const int* bi, int nb, BC bc, const T* src, T* dst, unsigned* err,
+             cudaStream_t s) {
+    dispatch<RunBcFull, T>(shape, grid, inst, bi, nb, bc, src, dst, err, s);
 }
-void sign(int shape, int grid, const Inst* inst, const int* bi, int nb, Fields f, const float* phi0, cudaStream_t s) {
-    dispatch<RunSign>(shape, grid, inst, bi, nb, f, phi0, s);
+template <typename T>
+void sign(int shape, int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, const T* phi0, cudaStream_t s) {
+    dispatch<RunSign, T>(shape, grid, inst, bi, nb, f, phi0, s);
 }
-void reinit(int shape, int grid, const Inst* inst, const int* bi, int nb, Fields f, const float* din, float* dout,
-            cudaStream_t s) {
-    dispatch<RunReinit>(shape, grid, inst, bi, nb, f, din, dout, s);
+template <typename T>
+void reinit(int shape, int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, const T* din, T* dout,
+            unsigned* err, cudaStream_t s) {
+    dispatch<RunReinit, T>(shape, grid, inst, bi, nb, f, din, dout, err, s);
 }
-void volume(int shape, int grid, const Inst* inst, const int* bi, int nb, Fields f, const float* phi,
-            double* partials, cudaStream_t s) {
-    dispatch<RunVolume>(shape, grid, inst, bi, nb, f, phi, partials, s);
+template <typename T>
+void bc_reinit(const Inst* inst, int ninst, long long nface, FieldsT<T> f, BC bc, const T* din, T* dout,
+               cudaStream_t s) {
+    ProfScope ps_("k_bc_reinit", s);
+    k_bc_reinit<T><<<flat_blocks(nface), 256, 0, s>>>(inst, ninst, nface, bc, f, din, dout);
 }
-void volume_final(const Inst* inst, int ninst, const int* bi, int nb, const double* partials, double* vols,
+template <typename T>
+void volume(int shape, int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, const T* phi,
+            long long* partials, cudaStream_t s) {
+    dispatch<RunVolume, T>(shape, grid, inst, bi, nb, f, phi, partials, s);
+}
+void volume_final(const Inst* inst, int ninst, const int* bi, int nb, const long long* partials, double* vols,
                   cudaStream_t s) {
     (void)bi;
     ProfScope ps_("k_volume_final", s);
     k_volume_final<<<ninst, 256, 0, s>>>(inst, ninst, nb, partials, vols);
 }
+void cell_hex(long long off, int ni, int nj, int nk, const double* x, const double* y, const double* z,
+              long long* cellfix, cudaStream_t s) {
+    const long long ncell = (long long)(ni - 1) * (nj - 1) * (nk - 1);
+    ProfScope ps_("k_cell_hex", s);
+    k_cell_hex<<<(unsigned)std::min<long long>((ncell + 255) / 256, 152 * 16), 256, 0, s>>>(off, ni, nj, nk, x, y, z,
+                                                                                             cellfix);
+}
 int max_blocks_per_sm(int shape, int kernel) {
     int n = 0;
-    dispatch<Occupancy>(shape, kernel, &n);
+    dispatch<Occupancy, float>(shape, kernel, &n);
     return n;
 }
+
+template <typename T>
+void adj_face(const Flat& fl, int face, long long nplane, BC bc, int kind, const T* phin, const T* in, const T* out,
+              double c1, double c2, T* lam, cudaStream_t s) {
+    ProfScope ps_("k_adj_face", s);
+    k_adj_face<T><<<flat_blocks(nplane), 256, 0, s>>>(fl, face, nplane, bc, kind, phin, in, out, T(c1), T(c2), lam);
+}
+template <typename T>
+void adj_stage(const Flat& fl, FieldsT<T> f, const T* in, const T* lamP0, T* lam_in, T* lamPhin, T* lamW0, T* lamW1,
+               T* lamW2, double c1, double c2, double c3, bool last, cudaStream_t s) {
+    ProfScope ps_("k_adj_stage", s);
+    k_adj_stage<T><<<flat_blocks(fl.n), 256, 0, s>>>(fl, f, in, lamP0, lam_in, lamPhin, lamW0, lamW1, lamW2, T(c1), T(c2), T(c3),
+                                                     last ? 1 : 0);
+}
+template <typename T>
+void adj_reinit(const Flat& fl, FieldsT<T> f, const T* d, const T* lam, T* coef, T* lam_out, cudaStream_t s) {
+    {
+        ProfScope ps_("k_adj_reinit_coef", s);
+        k_adj_reinit_coef<T><<<flat_blocks(fl.n), 256, 0, s>>>(fl, f, d, lam, coef);
+    }
+    ProfScope ps_("k_adj_reinit_apply", s);
+    k_adj_reinit_apply<T><<<flat_blocks(fl.n), 256, 0, s>>>(fl, lam, coef, lam_out);
+}
+template <typename T>
+void adj_contra(const Flat& fl, FieldsT<T> f, const T* w0, const T* w1, const T* w2, T* u0, T* u1, T* u2,
+                cudaStream_t s) {
+    ProfScope ps_("k_adj_contra", s);
+    k_adj_contra<T><<<flat_blocks(fl.n), 256, 0, s>>>(fl, f, w0, w1, w2, u0, u1, u2);
+}
+
+#define LSM_BATCH_INSTANTIATE(T)                                                                                      \
+    template void contra<T>(int, int, const Inst*, const int*, int, FieldsT<T>, cudaStream_t);                       \
+    template void stage<T>(int, int, const Inst*, const int*, int, FieldsT<T>, const T*, const T*, T*, double,       \
+                           double, double, cudaStream_t);                                                                     \
+    template void bc_stage<T>(const Inst*, int, long long, BC, const T*, const T*, T*, double, double, cudaStream_t);   \
+    template void bc_full<T>(int, int, const Inst*, const int*, int, BC, const T*, T*, unsigned*, cudaStream_t);      \
+    template void sign<T>(int, int, const Inst*, const int*, int, FieldsT<T>, const T*, cudaStream_t);               \
+    template void reinit<T>(int, int, const Inst*, const int*, int, FieldsT<T>, const T*, T*, unsigned*,             \
+                            cudaStream_t);                                                                            \
+    template void bc_reinit<T>(const Inst*, int, long long, FieldsT<T>, BC, const T*, T*, cudaStream_t);              \
+    template void volume<T>(int, int, const Inst*, const int*, int, FieldsT<T>, const T*, long long*, cudaStream_t);  \
+    template void adj_face<T>(const Flat&, int, long long, BC, int, const T*, const T*, const T*, double, double, T*, \
+                              cudaStream_t);                                                                          \
+    template void adj_stage<T>(const Flat&, FieldsT<T>, const T*, const T*, T*, T*, T*, T*, T*, double, double, double, \
+                               bool, cudaStream_t);                                                                   \
+    template void adj_reinit<T>(const Flat&, FieldsT<T>, const T*, const T*, T*, T*, cudaStream_t);                   \
+    template void adj_contra<T>(const Flat&, FieldsT<T>, const T*, const T*, const T*, T*, T*, T*, cudaStream_t);
+
+LSM_BATCH_INSTANTIATE(float)
+LSM_BATCH_INSTANTIATE(double)
 
 }  // namespace batch
 }  // namespace lsm

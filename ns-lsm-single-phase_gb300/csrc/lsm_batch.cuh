@@ -1,5 +1,6 @@
-// lsm_batch.cuh -- device descriptors and host launchers of the batched FP32
-// level-set path (many independent instances of uneven sizes per launch).
+// lsm_batch.cuh -- device descriptors and host launchers of the batched
+// level-set path (many independent instances of uneven sizes per launch),
+// forward and adjoint, in FP32 (throughput) or FP64 (gradient checks).
 //
 // Layout in HBM: every field of every instance is packed into one array per
 // field (instance after instance, each in the reference's i-fastest order);
@@ -19,25 +20,36 @@ struct Inst {
     int ni, nj, nk;
     int brick0;        // first brick of the instance in the current brick map
     int nbx, nby;      // bricks per row / per plane of the instance
-    float dt;          // advection time step (already multiplied into W)
+    float dt;          // advection time step (multiplied into W)
     float dtau;        // reinitialisation pseudo time step
     float eps;         // smoothing half-width epslsm
     float pad;
-    long long face0;   // first boundary-face node of the instance (bc kernels)
-    long long cell0;   // unused slot kept for alignment
+    long long face0;   // first boundary-face node of the instance (forward bc kernels)
+    long long fpre[3]; // first node of the instance's i-, j-, k-face planes (adjoint face kernels)
+    double dt64, dtau64, eps64;  // the same three parameters for the FP64 kernels
 };
 
-// Packed fields of one batch (device pointers).
-struct Fields {
-    float* phi;        // level set (state; start and end of every step)
-    float* stage[2];   // RK stage ping-pong
-    float* d[2];       // reinitialisation ping-pong
-    float* W[3];       // dt * d_m * (grad xi_m . u): contravariant velocity x dt
-    float* m[9];       // metrics: csi_x, csi_y, csi_z, eta_x, ..., zet_z
-    float* u[3];       // Cartesian velocity
-    float* sgn;        // sign field of the reinitialisation (0 where the lambda correction freezes d)
+// Packed fields of one batch (device pointers), scalar type T.
+template <typename T>
+struct FieldsT {
+    T* phi;            // level set (state; start and end of every step)
+    T* stage[2];       // RK stage ping-pong
+    T* d[2];           // reinitialisation ping-pong
+    T* W[3];           // dt * d_m * (grad xi_m . u): contravariant velocity x dt
+    T* m[9];           // metrics: csi_x, csi_y, csi_z, eta_x, ..., zet_z
+    T* u[3];           // Cartesian velocity
+    T* sgn;            // sign field of the reinitialisation (0 where the lambda correction freezes d)
     const double* xyz[3];  // FP64 coordinates (volume)
+    long long* cellfix;    // hexahedron volume of cell (i..i+1, j..j+1, k..k+1) in fixed point, by base node
 };
+using Fields = FieldsT<float>;
+
+// Batched water volumes are accumulated as 64-bit fixed point: each cell's
+// FP64 volume is rounded to a multiple of 2^-48 (coordinate units^3) and the
+// integers are summed, which is exact and independent of the summation
+// order.  Valid while an instance's volume stays below 2^15 units^3.
+constexpr double kVolScale = 281474976710656.0;       // 2^48
+constexpr double kVolUnit = 1.0 / 281474976710656.0;  // 2^-48
 
 struct BC {
     int type[6];
@@ -49,24 +61,76 @@ constexpr int kNumShapes = 5;
 struct Shape { int tx, ty, tz; };
 constexpr Shape kShapes[kNumShapes] = {{32, 4, 2}, {32, 8, 1}, {64, 4, 1}, {32, 2, 4}, {128, 2, 1}};
 
-// launchers (shape = index into kShapes); grid = persistent CTA count
-void contra(int shape, int grid, const Inst* inst, const int* brick_inst, int nbricks, Fields f, float dcm[3],
+// ------------------------------------------------------------ forward
+// (shape = index into kShapes; FP64 instantiations exist for shape 0 only)
+template <typename T>
+void contra(int shape, int grid, const Inst* inst, const int* brick_inst, int nbricks, FieldsT<T> f,
             cudaStream_t s);
-void stage(int shape, int grid, const Inst* inst, const int* brick_inst, int nbricks, Fields f, const float* phin,
-           const float* phi1, float* out, float c1, float c2, float c3, cudaStream_t s);
-void bc_stage(const Inst* inst, int ninst, long long nface, Fields f, BC bc, const float* phin, const float* phi1,
-              float* out, float c1, float c2, cudaStream_t s);
-void bc_full(int shape, int grid, const Inst* inst, const int* brick_inst, int nbricks, BC bc, const float* src,
-             float* dst, unsigned* err, cudaStream_t s);
-void sign(int shape, int grid, const Inst* inst, const int* brick_inst, int nbricks, Fields f, const float* phi0,
+template <typename T>
+void stage(int shape, int grid, const Inst* inst, const int* brick_inst, int nbricks, FieldsT<T> f, const T* phin,
+           const T* phi1, T* out, double c1, double c2, double c3, cudaStream_t s);
+template <typename T>
+void bc_stage(const Inst* inst, int ninst, long long nface, BC bc, const T* phin, const T* phi1, T* out, double c1,
+              double c2, cudaStream_t s);
+template <typename T>
+void bc_full(int shape, int grid, const Inst* inst, const int* brick_inst, int nbricks, BC bc, const T* src, T* dst,
+             unsigned* err, cudaStream_t s);
+template <typename T>
+void sign(int shape, int grid, const Inst* inst, const int* brick_inst, int nbricks, FieldsT<T> f, const T* phi0,
           cudaStream_t s);
-void reinit(int shape, int grid, const Inst* inst, const int* brick_inst, int nbricks, Fields f, const float* din,
-            float* dout, cudaStream_t s);
-void volume(int shape, int grid, const Inst* inst, const int* brick_inst, int nbricks, Fields f, const float* phi,
-            double* partials, cudaStream_t s);
-void volume_final(const Inst* inst, int ninst, const int* brick_inst, int nbricks, const double* partials,
+template <typename T>
+void reinit(int shape, int grid, const Inst* inst, const int* brick_inst, int nbricks, FieldsT<T> f, const T* din,
+            T* dout, unsigned* err, cudaStream_t s);
+// bcond_lsm on the output of the last reinitialisation pseudo-step (dout):
+// boundary values are recomputed pointwise from that step's input din.
+template <typename T>
+void bc_reinit(const Inst* inst, int ninst, long long nface, FieldsT<T> f, BC bc, const T* din, T* dout,
+               cudaStream_t s);
+template <typename T>
+void volume(int shape, int grid, const Inst* inst, const int* brick_inst, int nbricks, FieldsT<T> f, const T* phi,
+            long long* partials, cudaStream_t s);
+void volume_final(const Inst* inst, int ninst, const int* brick_inst, int nbricks, const long long* partials,
                   double* vols, cudaStream_t s);
+// fixed-point hexahedron volume of every cell of one instance (static
+// geometry); x, y, z and cellfix are the packed base arrays, `off` the
+// instance's first node
+void cell_hex(long long off, int ni, int nj, int nk, const double* x, const double* y, const double* z,
+              long long* cellfix, cudaStream_t s);
 int max_blocks_per_sm(int shape, int kernel);
+
+// ------------------------------------------------------------ adjoint
+// All adjoint kernels walk the packed nodes with one thread per node
+// (instance found by binary search over the node offsets `offs`).
+struct Flat {
+    const Inst* inst;
+    const long long* offs;  // ninst + 1 node offsets
+    int ninst;
+    long long n;            // total nodes
+};
+// Reverse of one bcond_lsm face (face = 0..5: i1, im, j1, jm, k1, km) on the
+// adjoint field lam, in place.  The forward values that decide the BigPhi
+// switch are evaluated from the pre-BC field P0, given as
+//   kind 0 (stage):  interior = out, boundary = c1*phin + c2*in
+//   kind 1 (field):  P0 = src (passed as `out`) everywhere
+template <typename T>
+void adj_face(const Flat& fl, int face, long long nface_nodes, BC bc, int kind, const T* phin, const T* in,
+              const T* out, double c1, double c2, T* lam, cudaStream_t s);
+// Reverse of one RK stage (stencil part gathered per node).  lamP0: adjoint
+// of the stage's pre-BC field; writes lam_in = c2 lamP0 - c3 (dR/din)^T lamP0
+// (+ lamPhin + c1 lamP0 when last, which also clears lamPhin), otherwise
+// accumulates lamPhin += c1 lamP0; and lamW_m -= c3 lamP0 D_m.
+template <typename T>
+void adj_stage(const Flat& fl, FieldsT<T> f, const T* in, const T* lamP0, T* lam_in, T* lamPhin, T* lamW0,
+               T* lamW1, T* lamW2, double c1, double c2, double c3, bool last, cudaStream_t s);
+// Reverse of one reinitialisation pseudo-step d' = d - dtau s (G(d) - 1):
+// coefficients (A_m, B_m) per node, then the gather lam_out = lam - sum(...).
+template <typename T>
+void adj_reinit(const Flat& fl, FieldsT<T> f, const T* d, const T* lam, T* coef /*6*n*/, T* lam_out,
+                cudaStream_t s);
+// lam_u_c += sum_m M[m][c] dt lamW_m  (the W = dt M u chain rule)
+template <typename T>
+void adj_contra(const Flat& fl, FieldsT<T> f, const T* lamW0, const T* lamW1, const T* lamW2, T* lu0, T* lu1,
+                T* lu2, cudaStream_t s);
 
 }  // namespace batch
 }  // namespace lsm

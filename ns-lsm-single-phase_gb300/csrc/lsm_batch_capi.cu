@@ -1,12 +1,15 @@
 // lsm_batch_capi.cu -- host side of include/lsm_batch.h: packed device
 // buffers of a batch of instances, the brick tables of the persistent
-// kernels, the tile-shape autotuner and the CUDA graph of one physical step.
+// kernels, the tile-shape autotuner, the CUDA graph of one physical step and
+// the checkpointed adjoint (forward_record / backward).
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <initializer_list>
+#include <type_traits>
 #include <vector>
 
 #include "lsm_batch.cuh"
@@ -14,27 +17,34 @@
 #include "lsm_c.h"
 #include "lsm_kernels.h"
 
-using lsm::batch::Fields;
+using lsm::batch::Flat;
 using lsm::batch::Inst;
+template <typename T>
+using FieldsT = lsm::batch::FieldsT<T>;
 
 struct lsm_batch {
     int device = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    int prec = 0;                // 0 FP32, 1 FP64
+    size_t esz = 4;              // bytes per element of the scalar fields
     int ninst = 0;
     std::vector<lsm_batch_instance> inst;
     lsm_batch_config cfg{};
-    std::vector<long long> off;
-    long long N = 0, nface = 0, max_inst_nodes = 0;
-    Fields f{};
-    float* bufs[6] = {};         // phi, stage0, stage1, d0, d1, sgn
-    float* comps[15] = {};       // W[3], m[9], u[3]
+    std::vector<long long> off;  // ninst + 1 node offsets
+    long long N = 0, nface = 0, max_inst_nodes = 0, nplane[3] = {0, 0, 0};
+    FieldsT<float> f32{};
+    FieldsT<double> f64{};
+    void* bufs[6] = {};          // phi, stage0, stage1, d0, d1, sgn
+    void* comps[15] = {};        // W[3], m[9], u[3]
     double* xyz = nullptr;       // 3*N FP64 coordinates
-    double* staging = nullptr;   // FP64 scratch for input conversion (4 * max instance nodes)
+    long long* cellfix = nullptr;  // N fixed-point cell hexahedron volumes
+    double* staging = nullptr;   // FP64 scratch for conversions (4 * max instance nodes)
     Inst* d_inst = nullptr;
+    long long* d_offs = nullptr;
     int* d_brick = nullptr;
     int nbricks = 0;
-    double* d_part = nullptr;
+    long long* d_part = nullptr;
     size_t part_cap = 0;
     double* d_vols = nullptr;
     double* h_vols = nullptr;    // pinned
@@ -42,6 +52,10 @@ struct lsm_batch {
     int shape = 0, grid = 0;
     bool tuned = false;
     cudaGraphExec_t exec = nullptr;
+    // adjoint state: one allocation, carved by adj_view
+    int rec_steps = 0, rec_ck = 0;
+    void* adj = nullptr;
+    size_t adj_bytes = 0;
     std::string err;
 };
 
@@ -56,71 +70,126 @@ int fail(lsm_batch* b, int st, const std::string& m) {
         cudaError_t e_ = (call);                                                                  \
         if (e_ != cudaSuccess) return fail((b), LSM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
+#define BTRY(x)              \
+    do {                     \
+        int st_ = (x);       \
+        if (st_) return st_; \
+    } while (0)
 
 struct Dev {
     int prev = -1;
-    explicit Dev(int d) { cudaGetDevice(&prev); if (prev != d) cudaSetDevice(d); }
-    ~Dev() { int c = -1; cudaGetDevice(&c); if (prev >= 0 && c != prev) cudaSetDevice(prev); }
+    explicit Dev(int d) {
+        cudaGetDevice(&prev);
+        if (prev != d) cudaSetDevice(d);
+    }
+    ~Dev() {
+        int c = -1;
+        cudaGetDevice(&c);
+        if (prev >= 0 && c != prev) cudaSetDevice(prev);
+    }
 };
 
-__global__ void k_cvt_f32(const double* __restrict__ src, int stride, int comp, long long n, float* __restrict__ dst) {
+template <typename T>
+__global__ void k_cvt_in(const double* __restrict__ src, int stride, int comp, long long n, T* __restrict__ dst) {
     for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < n; l += (long long)gridDim.x * blockDim.x)
-        dst[l] = (float)src[l * stride + comp];
+        dst[l] = (T)src[l * stride + comp];
 }
-__global__ void k_cvt_f64(const float* __restrict__ src, long long n, double* __restrict__ dst) {
+template <typename T>
+__global__ void k_cvt_out(const T* __restrict__ src, int stride, int comp, long long n, double* __restrict__ dst) {
     for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < n; l += (long long)gridDim.x * blockDim.x)
-        dst[l] = (double)src[l];
+        dst[l * stride + comp] = (double)src[l];
 }
+template <typename T>
+__global__ void k_zero(long long n, T* __restrict__ a) {
+    for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < n; l += (long long)gridDim.x * blockDim.x)
+        a[l] = T(0);
+}
+
+inline unsigned cblocks(long long n) { return (unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 8)); }
 
 bool on_device(const void* p) {
     cudaPointerAttributes a;
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-// copy an FP64 array (host or device) of `n` doubles into the staging buffer
+// copy `n` doubles (host or device) into the staging buffer
 int stage_in(lsm_batch* b, const double* src, long long n) {
     BCU(b, cudaMemcpyAsync(b->staging, src, sizeof(double) * n,
                            on_device(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, b->stream));
     return LSM_OK;
 }
-
-void cvt(lsm_batch* b, int stride, int comp, long long n, float* dst) {
-    lsm::ProfScope ps("k_cvt_f32", b->stream);
-    k_cvt_f32<<<(unsigned)std::min<long long>((n + 255) / 256, 152 * 8), 256, 0, b->stream>>>(b->staging, stride,
-                                                                                              comp, n, dst);
+void cvt_in(lsm_batch* b, int stride, int comp, long long n, void* dst) {
+    lsm::ProfScope ps("k_cvt_in", b->stream);
+    if (b->prec) k_cvt_in<double><<<cblocks(n), 256, 0, b->stream>>>(b->staging, stride, comp, n, (double*)dst);
+    else k_cvt_in<float><<<cblocks(n), 256, 0, b->stream>>>(b->staging, stride, comp, n, (float*)dst);
+}
+void cvt_out(lsm_batch* b, const void* src, int stride, int comp, long long n) {
+    lsm::ProfScope ps("k_cvt_out", b->stream);
+    if (b->prec) k_cvt_out<double><<<cblocks(n), 256, 0, b->stream>>>((const double*)src, stride, comp, n, b->staging);
+    else k_cvt_out<float><<<cblocks(n), 256, 0, b->stream>>>((const float*)src, stride, comp, n, b->staging);
+}
+int copy_out(lsm_batch* b, double* dst, long long n) {
+    BCU(b, cudaMemcpyAsync(dst, b->staging, sizeof(double) * n,
+                           on_device(dst) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, b->stream));
+    BCU(b, cudaStreamSynchronize(b->stream));
+    return LSM_OK;
 }
 
 int build_bricks(lsm_batch* b, int shape) {
+    if (b->prec) shape = 0;     // FP64 kernels exist for tile shape 0 only
     const auto sh = lsm::batch::kShapes[shape];
     std::vector<Inst> hi(b->ninst);
     std::vector<int> brick;
-    long long face = 0;
+    long long face = 0, pre[3] = {0, 0, 0};
     for (int q = 0; q < b->ninst; ++q) {
         const auto& I = b->inst[q];
         Inst& d = hi[q];
         d.off = b->off[q];
-        d.ni = I.ni; d.nj = I.nj; d.nk = I.nk;
+        d.ni = I.ni;
+        d.nj = I.nj;
+        d.nk = I.nk;
         d.nbx = (I.ni + sh.tx - 1) / sh.tx;
         d.nby = (I.nj + sh.ty - 1) / sh.ty;
         const int nbz = (I.nk + sh.tz - 1) / sh.tz;
         d.brick0 = (int)brick.size();
-        d.dt = (float)I.dt; d.dtau = (float)I.dtau; d.eps = (float)I.eps; d.pad = 0.f;
+        d.dt = (float)I.dt;
+        d.dtau = (float)I.dtau;
+        d.eps = (float)I.eps;
+        d.pad = 0.f;
+        d.dt64 = I.dt;
+        d.dtau64 = I.dtau;
+        d.eps64 = I.eps;
         d.face0 = face;
-        d.cell0 = 0;
         face += 2LL * ((long long)I.nj * I.nk + (long long)I.ni * I.nk + (long long)I.ni * I.nj);
+        for (int a = 0; a < 3; ++a) d.fpre[a] = pre[a];
+        pre[0] += (long long)I.nj * I.nk;
+        pre[1] += (long long)I.ni * I.nk;
+        pre[2] += (long long)I.ni * I.nj;
         brick.insert(brick.end(), (size_t)d.nbx * d.nby * nbz, q);
     }
     b->nface = face;
+    for (int a = 0; a < 3; ++a) b->nplane[a] = pre[a];
     b->nbricks = (int)brick.size();
-    if (b->d_brick) cudaFree(b->d_brick);
+    if (b->d_brick) {
+        cudaStreamSynchronize(b->stream);
+        cudaFree(b->d_brick);
+        b->d_brick = nullptr;
+    }
     BCU(b, cudaMalloc(&b->d_brick, sizeof(int) * brick.size()));
     BCU(b, cudaMemcpyAsync(b->d_brick, brick.data(), sizeof(int) * brick.size(), cudaMemcpyHostToDevice, b->stream));
     BCU(b, cudaMemcpyAsync(b->d_inst, hi.data(), sizeof(Inst) * hi.size(), cudaMemcpyHostToDevice, b->stream));
     const size_t need = 3 * (size_t)b->nbricks;
     if (need > b->part_cap) {
-        if (b->d_part) cudaFree(b->d_part);
-        BCU(b, cudaMalloc(&b->d_part, sizeof(double) * need));
+        if (b->d_part) {
+            cudaStreamSynchronize(b->stream);
+            cudaFree(b->d_part);
+            b->d_part = nullptr;
+        }
+        BCU(b, cudaMalloc(&b->d_part, sizeof(long long) * need));
         b->part_cap = need;
     }
     int sms = 0;
@@ -132,37 +201,78 @@ int build_bricks(lsm_batch* b, int shape) {
     return LSM_OK;
 }
 
-// TVD-RK3 coefficients, src/ad_RKTVD3.F90:36-48
-const float kC[3][3] = {{1.0f, 0.0f, 1.0f}, {0.75f, 0.25f, 0.25f}, {1.0f / 3.0f, 2.0f / 3.0f, 2.0f / 3.0f}};
+// TVD-RK3 stage coefficients (c1, c2, c3): out = c1 phi^n + c2 in - c3 dt aj RH,
+// src/ad_RKTVD3.F90:36-48
+// (double here; each kernel takes them in its own precision)
+const double kC[3][3] = {{1.0, 0.0, 1.0}, {0.75, 0.25, 0.25}, {1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0}};
 
-// enqueue one physical step on b->stream
-void enqueue_step(lsm_batch* b) {
-    namespace B = lsm::batch;
-    const int sh = b->shape, gr = b->grid, nb = b->nbricks;
-    B::BC bc;
+lsm::batch::BC make_bc(const lsm_batch* b) {
+    lsm::batch::BC bc;
     for (int q = 0; q < 6; ++q) bc.type[q] = b->cfg.btype_lsm[q];
     bc.BigPhi = (float)b->cfg.BigPhi;
-    Fields& f = b->f;
-    B::volume(sh, gr, b->d_inst, b->d_brick, nb, f, f.phi, b->d_part, b->stream);
-    B::volume_final(b->d_inst, b->ninst, b->d_brick, nb, b->d_part, b->d_vols, b->stream);
-    float one[3] = {1.0f, 1.0f, 1.0f};
-    B::contra(sh, gr, b->d_inst, b->d_brick, nb, f, one, b->stream);
-    const float* in[3] = {f.phi, f.stage[0], f.stage[1]};
-    float* out[3] = {f.stage[0], f.stage[1], f.stage[0]};
-    for (int s = 0; s < 3; ++s) {
-        B::stage(sh, gr, b->d_inst, b->d_brick, nb, f, f.phi, in[s], out[s], kC[s][0], kC[s][1], kC[s][2], b->stream);
-        B::bc_stage(b->d_inst, b->ninst, b->nface, f, bc, f.phi, in[s], out[s], kC[s][0], kC[s][1], b->stream);
+    return bc;
+}
+
+template <typename T>
+FieldsT<T>& fields(lsm_batch* b);
+template <>
+FieldsT<float>& fields<float>(lsm_batch* b) { return b->f32; }
+template <>
+FieldsT<double>& fields<double>(lsm_batch* b) { return b->f64; }
+
+// Recorded internals of one step (adjoint): the three stage outputs and the
+// RNitermax raw reinitialisation outputs (D + k N).
+template <typename T>
+struct Rec {
+    T* A[3];
+    T* D;
+};
+
+// One physical step phin -> phi_out (phi_out may alias phin).  With `rec`
+// the stage outputs and the pseudo-step outputs are kept and the final
+// bcond_lsm is skipped (phi_out unused); `vol` adds the pre-advection water
+// volume.
+template <typename T>
+void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec, bool vol) {
+    namespace B = lsm::batch;
+    const int sh = b->shape, gr = b->grid, nb = b->nbricks;
+    const B::BC bc = make_bc(b);
+    FieldsT<T>& f = fields<T>(b);
+    const long long N = b->N;
+    if (vol) {
+        B::volume<T>(sh, gr, b->d_inst, b->d_brick, nb, f, phin, b->d_part, b->stream);
+        B::volume_final(b->d_inst, b->ninst, b->d_brick, nb, b->d_part, b->d_vols, b->stream);
     }
-    const float* cur = f.stage[0];
-    if (b->cfg.RNitermax > 0) {
-        B::sign(sh, gr, b->d_inst, b->d_brick, nb, f, f.stage[0], b->stream);
-        for (int it = 0; it < b->cfg.RNitermax; ++it) {
-            float* o = f.d[it & 1];
-            B::reinit(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, b->stream);
+    B::contra<T>(sh, gr, b->d_inst, b->d_brick, nb, f, b->stream);
+    T* S[3] = {rec ? rec->A[0] : f.stage[0], rec ? rec->A[1] : f.stage[1], rec ? rec->A[2] : f.stage[0]};
+    const T* in[3] = {phin, S[0], S[1]};
+    for (int s = 0; s < 3; ++s) {
+        B::stage<T>(sh, gr, b->d_inst, b->d_brick, nb, f, phin, in[s], S[s], kC[s][0], kC[s][1], kC[s][2], b->stream);
+        B::bc_stage<T>(b->d_inst, b->ninst, b->nface, bc, phin, in[s], S[s], kC[s][0], kC[s][1], b->stream);
+    }
+    const int R = b->cfg.RNitermax;
+    if (R > 0) {
+        // reinitialization (src/reinitialization.F90:55-104); the last
+        // pseudo-step writes phi and gets the final bcond_lsm
+        // (src/levelsetmethod.F90:318-321)
+        B::sign<T>(sh, gr, b->d_inst, b->d_brick, nb, f, S[2], b->stream);
+        const T* cur = S[2];
+        for (int it = 0; it < R; ++it) {
+            const bool last = it == R - 1;
+            T* o = rec ? rec->D + (long long)it * N : (last ? phi_out : f.d[it & 1]);
+            B::reinit<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, (last && !rec) ? b->d_err : nullptr,
+                         b->stream);
+            if (last && !rec) B::bc_reinit<T>(b->d_inst, b->ninst, b->nface, f, bc, cur, phi_out, b->stream);
             cur = o;
         }
+    } else if (!rec) {
+        B::bc_full<T>(sh, gr, b->d_inst, b->d_brick, nb, bc, S[2], phi_out, b->d_err, b->stream);
     }
-    B::bc_full(sh, gr, b->d_inst, b->d_brick, nb, bc, cur, f.phi, b->d_err, b->stream);
+}
+
+void enqueue_step(lsm_batch* b) {
+    if (b->prec) enqueue_step_io<double>(b, b->f64.phi, b->f64.phi, nullptr, true);
+    else enqueue_step_io<float>(b, b->f32.phi, b->f32.phi, nullptr, true);
 }
 
 int autotune(lsm_batch* b) {
@@ -172,14 +282,14 @@ int autotune(lsm_batch* b) {
     cudaEventCreate(&e1);
     float best = 1e30f;
     int best_shape = 0;
+    FieldsT<float>& f = b->f32;
     for (int s = 0; s < B::kNumShapes; ++s) {
-        int st = build_bricks(b, s);
-        if (st) return st;
-        B::sign(s, b->grid, b->d_inst, b->d_brick, b->nbricks, b->f, b->f.phi, b->stream);
+        BTRY(build_bricks(b, s));
+        B::sign<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, f.phi, b->stream);
         auto pass = [&]() {
-            B::stage(s, b->grid, b->d_inst, b->d_brick, b->nbricks, b->f, b->f.phi, b->f.phi, b->f.stage[0], 1.f, 0.f,
-                     1.f, b->stream);
-            B::reinit(s, b->grid, b->d_inst, b->d_brick, b->nbricks, b->f, b->f.phi, b->f.d[0], b->stream);
+            B::stage<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, f.phi, f.phi, f.stage[0], 1.0, 0.0, 1.0,
+                            b->stream);
+            B::reinit<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, f.phi, f.d[0], nullptr, b->stream);
         };
         pass();
         cudaEventRecord(e0, b->stream);
@@ -187,12 +297,16 @@ int autotune(lsm_batch* b) {
         cudaEventRecord(e1, b->stream);
         cudaError_t e = cudaEventSynchronize(e1);
         if (e != cudaSuccess) {
-            cudaEventDestroy(e0); cudaEventDestroy(e1);
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
             return fail(b, LSM_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(e));
         }
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best) { best = ms; best_shape = s; }
+        if (ms < best) {
+            best = ms;
+            best_shape = s;
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -201,8 +315,8 @@ int autotune(lsm_batch* b) {
 
 int prepare(lsm_batch* b) {
     if (!b->tuned) {
-        int st = b->cfg.autotune ? autotune(b) : build_bricks(b, std::min(std::max(b->cfg.shape, 0), 4));
-        if (st) return st;
+        const bool tune = b->cfg.autotune && !b->prec;
+        BTRY(tune ? autotune(b) : build_bricks(b, std::min(std::max(b->cfg.shape, 0), 4)));
         b->tuned = true;
     }
     if (b->cfg.use_graph && !b->exec) {
@@ -218,6 +332,181 @@ int prepare(lsm_batch* b) {
     return LSM_OK;
 }
 
+int run_steps(lsm_batch* b, int nsteps) {
+    for (int s = 0; s < nsteps; ++s) {
+        if (b->exec) {
+            lsm::g_launches += (unsigned long long)lsm_batch_launches_per_step(b);
+            BCU(b, cudaGraphLaunch(b->exec, b->stream));
+        } else {
+            enqueue_step(b);
+        }
+    }
+    return LSM_OK;
+}
+
+int check_inst(lsm_batch* b, int q) {
+    if (q < 0 || q >= b->ninst) return fail(b, LSM_ERR_BAD_PARAM, "instance index out of range");
+    return LSM_OK;
+}
+
+// ------------------------------------------------------------ adjoint state
+// Checkpoints (nck N), segment states (ck N), stage outputs (3 N),
+// pseudo-step outputs (R N), adjoint fields lam, lam2, lamPhin (3 N), lamW
+// (3 N), reinitialisation coefficients (6 N), lam_u (3 N).
+template <typename T>
+struct AdjView {
+    T *ckpt, *seg, *A[3], *D, *lam, *lam2, *lamPhin, *lamW[3], *coef, *lamU[3];
+};
+
+int n_ckpt(int nsteps, int ck) { return (nsteps + ck - 1) / ck; }
+
+size_t adj_elems(const lsm_batch* b, int nsteps, int ck) {
+    return (size_t)b->N *
+           (size_t)(n_ckpt(nsteps, ck) + ck + 3 + std::max(b->cfg.RNitermax, 1) + 3 + 3 + 6 + 3);
+}
+
+template <typename T>
+AdjView<T> adj_view(lsm_batch* b) {
+    AdjView<T> v;
+    const long long N = b->N;
+    T* p = (T*)b->adj;
+    v.ckpt = p;
+    p += (long long)n_ckpt(b->rec_steps, b->rec_ck) * N;
+    v.seg = p;
+    p += (long long)b->rec_ck * N;
+    for (int s = 0; s < 3; ++s) {
+        v.A[s] = p;
+        p += N;
+    }
+    v.D = p;
+    p += (long long)std::max(b->cfg.RNitermax, 1) * N;
+    v.lam = p;
+    p += N;
+    v.lam2 = p;
+    p += N;
+    v.lamPhin = p;
+    p += N;
+    for (int c = 0; c < 3; ++c) {
+        v.lamW[c] = p;
+        p += N;
+    }
+    v.coef = p;
+    p += 6 * N;
+    for (int c = 0; c < 3; ++c) {
+        v.lamU[c] = p;
+        p += N;
+    }
+    return v;
+}
+
+template <typename T>
+int forward_record_t(lsm_batch* b, int nsteps, int ck) {
+    const size_t bytes = adj_elems(b, nsteps, ck) * sizeof(T);
+    if (bytes > b->adj_bytes) {
+        if (b->adj) {
+            cudaStreamSynchronize(b->stream);
+            cudaFree(b->adj);
+            b->adj = nullptr;
+            b->adj_bytes = 0;
+        }
+        BCU(b, cudaMalloc(&b->adj, bytes));
+        b->adj_bytes = bytes;
+    }
+    b->rec_steps = nsteps;
+    b->rec_ck = ck;
+    AdjView<T> v = adj_view<T>(b);
+    FieldsT<T>& f = fields<T>(b);
+    BCU(b, cudaMemsetAsync(v.lam, 0, sizeof(T) * b->N, b->stream));
+    for (int n = 0; n < nsteps; ++n) {
+        if (n % ck == 0)
+            BCU(b, cudaMemcpyAsync(v.ckpt + (long long)(n / ck) * b->N, f.phi, sizeof(T) * b->N,
+                                   cudaMemcpyDeviceToDevice, b->stream));
+        BTRY(run_steps(b, 1));
+    }
+    BCU(b, cudaGetLastError());
+    unsigned flags = 0;
+    BCU(b, cudaMemcpyAsync(&flags, b->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream));
+    BCU(b, cudaStreamSynchronize(b->stream));
+    if (flags & lsm::kErrNonFinite) return fail(b, LSM_ERR_NONFINITE, "non-finite phi in the batch");
+    return LSM_OK;
+}
+
+// Reverse of one physical step; on entry lam holds the adjoint of phi^{n+1},
+// on exit the adjoint of phi^n (the pointers of `v` swap along the way).
+template <typename T>
+void adj_step(lsm_batch* b, AdjView<T>& v, const T* phin) {
+    namespace B = lsm::batch;
+    FieldsT<T>& f = fields<T>(b);
+    const B::BC bc = make_bc(b);
+    const long long N = b->N;
+    const Flat fl{b->d_inst, b->d_offs, b->ninst, N};
+    const int R = b->cfg.RNitermax;
+    auto faces = [&](int kind, const T* pn, const T* in, const T* out, double c1, double c2) {
+        for (int face = 5; face >= 0; --face)
+            B::adj_face<T>(fl, face, b->nplane[face >> 1], bc, kind, pn, in, out, c1, c2, v.lam, b->stream);
+    };
+    if (R > 0) {
+        faces(1, nullptr, nullptr, v.D + (long long)(R - 1) * N, 0.0, 0.0);
+        for (int k = R - 1; k >= 0; --k) {
+            const T* dk = k == 0 ? v.A[2] : v.D + (long long)(k - 1) * N;
+            B::adj_reinit<T>(fl, f, dk, v.lam, v.coef, v.lam2, b->stream);
+            std::swap(v.lam, v.lam2);
+        }
+    } else {
+        faces(1, nullptr, nullptr, v.A[2], 0.0, 0.0);
+    }
+    // stages 3, 2, 1: inputs A2, A1, phi^n; outputs A3, A2, A1
+    const T* ins[3] = {phin, v.A[0], v.A[1]};
+    for (int s = 2; s >= 0; --s) {
+        faces(0, phin, ins[s], v.A[s], kC[s][0], kC[s][1]);
+        B::adj_stage<T>(fl, f, ins[s], v.lam, v.lam2, v.lamPhin, v.lamW[0], v.lamW[1], v.lamW[2], kC[s][0], kC[s][1],
+                        kC[s][2], s == 0, b->stream);
+        std::swap(v.lam, v.lam2);
+    }
+}
+
+template <typename T>
+int backward_t(lsm_batch* b) {
+    if (!b->rec_steps) return fail(b, LSM_ERR_BAD_PARAM, "lsm_batch_backward needs lsm_batch_forward_record first");
+    AdjView<T> v = adj_view<T>(b);
+    const AdjView<T> canon = v;
+    const long long N = b->N;
+    T* const zero_fields[7] = {v.lamPhin, v.lamW[0], v.lamW[1], v.lamW[2], v.lamU[0], v.lamU[1], v.lamU[2]};
+    for (T* p : zero_fields) k_zero<T><<<cblocks(N), 256, 0, b->stream>>>(N, p);
+    const int ck = b->rec_ck, nsteps = b->rec_steps, nseg = n_ckpt(nsteps, ck);
+    Rec<T> rec;
+    for (int s = 0; s < 3; ++s) rec.A[s] = v.A[s];
+    rec.D = v.D;
+    for (int sg = nseg - 1; sg >= 0; --sg) {
+        const int c0 = sg * ck, L = std::min(c0 + ck, nsteps) - c0;
+        BCU(b, cudaMemcpyAsync(v.seg, v.ckpt + (long long)sg * N, sizeof(T) * N, cudaMemcpyDeviceToDevice, b->stream));
+        for (int q = 0; q + 1 < L; ++q)
+            enqueue_step_io<T>(b, v.seg + (long long)q * N, v.seg + (long long)(q + 1) * N, nullptr, false);
+        for (int q = L - 1; q >= 0; --q) {
+            const T* phin = v.seg + (long long)q * N;
+            enqueue_step_io<T>(b, phin, nullptr, &rec, false);
+            adj_step<T>(b, v, phin);
+        }
+    }
+    const Flat fl{b->d_inst, b->d_offs, b->ninst, N};
+    lsm::batch::adj_contra<T>(fl, fields<T>(b), v.lamW[0], v.lamW[1], v.lamW[2], v.lamU[0], v.lamU[1], v.lamU[2],
+                              b->stream);
+    if (v.lam != canon.lam)
+        BCU(b, cudaMemcpyAsync(canon.lam, v.lam, sizeof(T) * N, cudaMemcpyDeviceToDevice, b->stream));
+    BCU(b, cudaGetLastError());
+    BCU(b, cudaStreamSynchronize(b->stream));
+    return LSM_OK;
+}
+
+const void* adj_field(lsm_batch* b, int which) {  // 0: lam, 1..3: lam_u
+    if (b->prec) {
+        AdjView<double> v = adj_view<double>(b);
+        return which ? (const void*)v.lamU[which - 1] : (const void*)v.lam;
+    }
+    AdjView<float> v = adj_view<float>(b);
+    return which ? (const void*)v.lamU[which - 1] : (const void*)v.lam;
+}
+
 }  // namespace
 
 extern "C" {
@@ -229,7 +518,7 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
         if (inst[q].ni < 4 || inst[q].nj < 4 || inst[q].nk < 4) return LSM_ERR_BAD_SHAPE;
     for (int f = 0; f < 6; ++f)
         if (cfg->btype_lsm[f] < 0 || cfg->btype_lsm[f] > 2) return LSM_ERR_BAD_PARAM;
-    if (cfg->RNitermax < 0) return LSM_ERR_BAD_PARAM;
+    if (cfg->RNitermax < 0 || (cfg->precision != 0 && cfg->precision != 1)) return LSM_ERR_BAD_PARAM;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
         cudaGetLastError();
@@ -241,6 +530,8 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
     b->ninst = ninst;
     b->inst.assign(inst, inst + ninst);
     b->cfg = *cfg;
+    b->prec = cfg->precision;
+    b->esz = b->prec ? sizeof(double) : sizeof(float);
     if (stream) {
         b->stream = (cudaStream_t)stream;
     } else {
@@ -254,28 +545,49 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
         n += nq;
         b->max_inst_nodes = std::max(b->max_inst_nodes, nq);
     }
+    b->off.push_back(n);
     b->N = n;
-    auto cleanup = [&](int st) { lsm_batch_destroy(b); return st; };
+    auto cleanup = [&](int st) {
+        lsm_batch_destroy(b);
+        return st;
+    };
     for (auto& p : b->bufs)
-        if (cudaMalloc(&p, sizeof(float) * n) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
+        if (cudaMalloc(&p, b->esz * n) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     for (auto& p : b->comps)
-        if (cudaMalloc(&p, sizeof(float) * n) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
+        if (cudaMalloc(&p, b->esz * n) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->xyz, sizeof(double) * 3 * n) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
+    if (cudaMalloc(&b->cellfix, sizeof(long long) * n) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->staging, sizeof(double) * 4 * b->max_inst_nodes) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->d_inst, sizeof(Inst) * ninst) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
+    if (cudaMalloc(&b->d_offs, sizeof(long long) * (ninst + 1)) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->d_vols, sizeof(double) * 4 * ninst) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMallocHost(&b->h_vols, sizeof(double) * 4 * ninst) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->d_err, sizeof(unsigned)) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
+    cudaMemcpyAsync(b->d_offs, b->off.data(), sizeof(long long) * (ninst + 1), cudaMemcpyHostToDevice, b->stream);
     cudaMemsetAsync(b->d_err, 0, sizeof(unsigned), b->stream);
-    for (auto& p : b->bufs) cudaMemsetAsync(p, 0, sizeof(float) * n, b->stream);
-    for (auto& p : b->comps) cudaMemsetAsync(p, 0, sizeof(float) * n, b->stream);
+    cudaMemsetAsync(b->d_vols, 0, sizeof(double) * 4 * ninst, b->stream);
+    for (auto& p : b->bufs) cudaMemsetAsync(p, 0, b->esz * n, b->stream);
+    for (auto& p : b->comps) cudaMemsetAsync(p, 0, b->esz * n, b->stream);
     cudaMemsetAsync(b->xyz, 0, sizeof(double) * 3 * n, b->stream);
-    Fields& f = b->f;
-    f.phi = b->bufs[0]; f.stage[0] = b->bufs[1]; f.stage[1] = b->bufs[2];
-    f.d[0] = b->bufs[3]; f.d[1] = b->bufs[4]; f.sgn = b->bufs[5];
-    for (int c = 0; c < 3; ++c) { f.W[c] = b->comps[c]; f.u[c] = b->comps[12 + c]; }
-    for (int c = 0; c < 9; ++c) f.m[c] = b->comps[3 + c];
-    for (int c = 0; c < 3; ++c) f.xyz[c] = b->xyz + c * n;
+    cudaMemsetAsync(b->cellfix, 0, sizeof(long long) * n, b->stream);
+    auto wire = [&](auto& f, auto* tag) {
+        using T = std::remove_pointer_t<decltype(tag)>;
+        f.phi = (T*)b->bufs[0];
+        f.stage[0] = (T*)b->bufs[1];
+        f.stage[1] = (T*)b->bufs[2];
+        f.d[0] = (T*)b->bufs[3];
+        f.d[1] = (T*)b->bufs[4];
+        f.sgn = (T*)b->bufs[5];
+        for (int c = 0; c < 3; ++c) {
+            f.W[c] = (T*)b->comps[c];
+            f.u[c] = (T*)b->comps[12 + c];
+            f.xyz[c] = b->xyz + c * n;
+        }
+        for (int c = 0; c < 9; ++c) f.m[c] = (T*)b->comps[3 + c];
+        f.cellfix = b->cellfix;
+    };
+    if (b->prec) wire(b->f64, (double*)nullptr);
+    else wire(b->f32, (float*)nullptr);
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     *out = b;
     return LSM_OK;
@@ -286,17 +598,15 @@ int lsm_batch_destroy(lsm_batch_handle b) {
     Dev guard(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->exec) cudaGraphExecDestroy(b->exec);
-    for (auto p : b->bufs) if (p) cudaFree(p);
-    for (auto p : b->comps) if (p) cudaFree(p);
-    if (b->xyz) cudaFree(b->xyz);
-    if (b->staging) cudaFree(b->staging);
-    if (b->d_inst) cudaFree(b->d_inst);
-    if (b->d_brick) cudaFree(b->d_brick);
-    if (b->d_part) cudaFree(b->d_part);
-    if (b->d_vols) cudaFree(b->d_vols);
+    for (auto p : b->bufs)
+        if (p) cudaFree(p);
+    for (auto p : b->comps)
+        if (p) cudaFree(p);
+    for (void* p : {(void*)b->xyz, (void*)b->cellfix, (void*)b->staging, (void*)b->d_inst, (void*)b->d_offs,
+                    (void*)b->d_brick, (void*)b->d_part, (void*)b->d_vols, (void*)b->d_err, b->adj})
+        if (p) cudaFree(p);
     if (b->h_vols) cudaFreeHost(b->h_vols);
-    if (b->d_err) cudaFree(b->d_err);
-    if (b->own_stream) cudaStreamDestroy(b->stream);
+    if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return LSM_OK;
 }
@@ -304,7 +614,7 @@ int lsm_batch_destroy(lsm_batch_handle b) {
 int lsm_batch_set_geometry(lsm_batch_handle b, int q, const double* x, const double* y, const double* z,
                            const double* csi, const double* eta, const double* zet) {
     if (!b || !x || !y || !z || !csi || !eta || !zet) return LSM_ERR_NULL;
-    if (q < 0 || q >= b->ninst) return fail(b, LSM_ERR_BAD_PARAM, "instance index out of range");
+    BTRY(check_inst(b, q));
     Dev guard(b->device);
     const auto& I = b->inst[q];
     const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
@@ -314,10 +624,11 @@ int lsm_batch_set_geometry(lsm_batch_handle b, int q, const double* x, const dou
                                on_device(c3[c]) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, b->stream));
     const double* m3[3] = {csi, eta, zet};
     for (int d = 0; d < 3; ++d) {
-        int st = stage_in(b, m3[d], 3 * n);
-        if (st) return st;
-        for (int c = 0; c < 3; ++c) cvt(b, 3, c, n, b->f.m[3 * d + c] + o);
+        BTRY(stage_in(b, m3[d], 3 * n));
+        for (int c = 0; c < 3; ++c) cvt_in(b, 3, c, n, (char*)b->comps[3 + 3 * d + c] + b->esz * o);
     }
+    // cell_hex indexes from the packed base arrays with the instance offset o
+    lsm::batch::cell_hex(o, I.ni, I.nj, I.nk, b->xyz, b->xyz + b->N, b->xyz + 2 * b->N, b->cellfix, b->stream);
     BCU(b, cudaGetLastError());
     BCU(b, cudaStreamSynchronize(b->stream));
     return LSM_OK;
@@ -325,13 +636,12 @@ int lsm_batch_set_geometry(lsm_batch_handle b, int q, const double* x, const dou
 
 int lsm_batch_set_velocity(lsm_batch_handle b, int q, const double* qv) {
     if (!b || !qv) return LSM_ERR_NULL;
-    if (q < 0 || q >= b->ninst) return fail(b, LSM_ERR_BAD_PARAM, "instance index out of range");
+    BTRY(check_inst(b, q));
     Dev guard(b->device);
     const auto& I = b->inst[q];
     const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
-    int st = stage_in(b, qv, 4 * n);
-    if (st) return st;
-    for (int c = 0; c < 3; ++c) cvt(b, 4, c + 1, n, b->f.u[c] + o);
+    BTRY(stage_in(b, qv, 4 * n));
+    for (int c = 0; c < 3; ++c) cvt_in(b, 4, c + 1, n, (char*)b->comps[12 + c] + b->esz * o);
     BCU(b, cudaGetLastError());
     BCU(b, cudaStreamSynchronize(b->stream));
     return LSM_OK;
@@ -339,13 +649,12 @@ int lsm_batch_set_velocity(lsm_batch_handle b, int q, const double* qv) {
 
 int lsm_batch_set_phi(lsm_batch_handle b, int q, const double* phi) {
     if (!b || !phi) return LSM_ERR_NULL;
-    if (q < 0 || q >= b->ninst) return fail(b, LSM_ERR_BAD_PARAM, "instance index out of range");
+    BTRY(check_inst(b, q));
     Dev guard(b->device);
     const auto& I = b->inst[q];
     const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
-    int st = stage_in(b, phi, n);
-    if (st) return st;
-    cvt(b, 1, 0, n, b->f.phi + o);
+    BTRY(stage_in(b, phi, n));
+    cvt_in(b, 1, 0, n, (char*)b->bufs[0] + b->esz * o);
     BCU(b, cudaGetLastError());
     BCU(b, cudaStreamSynchronize(b->stream));
     return LSM_OK;
@@ -353,45 +662,86 @@ int lsm_batch_set_phi(lsm_batch_handle b, int q, const double* phi) {
 
 int lsm_batch_get_phi(lsm_batch_handle b, int q, double* phi) {
     if (!b || !phi) return LSM_ERR_NULL;
-    if (q < 0 || q >= b->ninst) return fail(b, LSM_ERR_BAD_PARAM, "instance index out of range");
+    BTRY(check_inst(b, q));
     Dev guard(b->device);
     const auto& I = b->inst[q];
     const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
-    {
-        lsm::ProfScope ps("k_cvt_f64", b->stream);
-        k_cvt_f64<<<(unsigned)std::min<long long>((n + 255) / 256, 152 * 8), 256, 0, b->stream>>>(b->f.phi + o, n,
-                                                                                                 b->staging);
-    }
+    cvt_out(b, (const char*)b->bufs[0] + b->esz * o, 1, 0, n);
     BCU(b, cudaGetLastError());
-    BCU(b, cudaMemcpyAsync(phi, b->staging, sizeof(double) * n,
-                           on_device(phi) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, b->stream));
-    BCU(b, cudaStreamSynchronize(b->stream));
-    return LSM_OK;
+    return copy_out(b, phi, n);
 }
 
 int lsm_batch_step(lsm_batch_handle b, int nsteps, double* volumes) {
     if (!b) return LSM_ERR_NULL;
     if (nsteps < 0) return fail(b, LSM_ERR_BAD_PARAM, "negative step count");
     Dev guard(b->device);
-    int st = prepare(b);
-    if (st) return st;
-    for (int s = 0; s < nsteps; ++s) {
-        if (b->exec) {
-            lsm::g_launches += (unsigned long long)lsm_batch_launches_per_step(b);
-            BCU(b, cudaGraphLaunch(b->exec, b->stream));
-        } else {
-            enqueue_step(b);
-        }
-    }
+    BTRY(prepare(b));
+    BTRY(run_steps(b, nsteps));
     BCU(b, cudaGetLastError());
     unsigned flags = 0;
     BCU(b, cudaMemcpyAsync(&flags, b->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream));
-    if (volumes) BCU(b, cudaMemcpyAsync(b->h_vols, b->d_vols, sizeof(double) * 4 * b->ninst, cudaMemcpyDeviceToHost,
-                                        b->stream));
+    if (volumes)
+        BCU(b, cudaMemcpyAsync(b->h_vols, b->d_vols, sizeof(double) * 4 * b->ninst, cudaMemcpyDeviceToHost,
+                               b->stream));
     BCU(b, cudaStreamSynchronize(b->stream));
     if (volumes) std::memcpy(volumes, b->h_vols, sizeof(double) * 4 * b->ninst);
     if (flags & lsm::kErrNonFinite) return fail(b, LSM_ERR_NONFINITE, "non-finite phi in the batch");
     return LSM_OK;
+}
+
+int lsm_batch_forward_record(lsm_batch_handle b, int nsteps, int checkpoint_every) {
+    if (!b) return LSM_ERR_NULL;
+    if (nsteps <= 0 || checkpoint_every <= 0)
+        return fail(b, LSM_ERR_BAD_PARAM, "step count and checkpoint interval must be positive");
+    Dev guard(b->device);
+    BTRY(prepare(b));
+    return b->prec ? forward_record_t<double>(b, nsteps, checkpoint_every)
+                   : forward_record_t<float>(b, nsteps, checkpoint_every);
+}
+
+int lsm_batch_set_grad_phi(lsm_batch_handle b, int q, const double* g) {
+    if (!b || !g) return LSM_ERR_NULL;
+    BTRY(check_inst(b, q));
+    if (!b->rec_steps) return fail(b, LSM_ERR_BAD_PARAM, "seed the gradient after lsm_batch_forward_record");
+    Dev guard(b->device);
+    const auto& I = b->inst[q];
+    const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
+    BTRY(stage_in(b, g, n));
+    cvt_in(b, 1, 0, n, (char*)adj_field(b, 0) + b->esz * o);
+    BCU(b, cudaGetLastError());
+    BCU(b, cudaStreamSynchronize(b->stream));
+    return LSM_OK;
+}
+
+int lsm_batch_backward(lsm_batch_handle b) {
+    if (!b) return LSM_ERR_NULL;
+    Dev guard(b->device);
+    return b->prec ? backward_t<double>(b) : backward_t<float>(b);
+}
+
+int lsm_batch_get_grad_phi0(lsm_batch_handle b, int q, double* g) {
+    if (!b || !g) return LSM_ERR_NULL;
+    BTRY(check_inst(b, q));
+    if (!b->rec_steps) return fail(b, LSM_ERR_BAD_PARAM, "no recorded steps");
+    Dev guard(b->device);
+    const auto& I = b->inst[q];
+    const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
+    cvt_out(b, (const char*)adj_field(b, 0) + b->esz * o, 1, 0, n);
+    BCU(b, cudaGetLastError());
+    return copy_out(b, g, n);
+}
+
+int lsm_batch_get_grad_velocity(lsm_batch_handle b, int q, double* gq) {
+    if (!b || !gq) return LSM_ERR_NULL;
+    BTRY(check_inst(b, q));
+    if (!b->rec_steps) return fail(b, LSM_ERR_BAD_PARAM, "no recorded steps");
+    Dev guard(b->device);
+    const auto& I = b->inst[q];
+    const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
+    BCU(b, cudaMemsetAsync(b->staging, 0, sizeof(double) * 4 * n, b->stream));
+    for (int c = 0; c < 3; ++c) cvt_out(b, (const char*)adj_field(b, 1 + c) + b->esz * o, 4, c + 1, n);
+    BCU(b, cudaGetLastError());
+    return copy_out(b, gq, 4 * n);
 }
 
 int lsm_batch_shape(lsm_batch_handle b, int* index, int* tx, int* ty, int* tz) {
@@ -408,7 +758,9 @@ long long lsm_batch_nodes(lsm_batch_handle b) { return b ? b->N : 0; }
 
 int lsm_batch_launches_per_step(lsm_batch_handle b) {
     if (!b) return 0;
-    return 2 + 1 + 6 + (b->cfg.RNitermax > 0 ? 1 + b->cfg.RNitermax : 0) + 1;
+    // volume 2, contra 1, three stages x (stencil + faces) 6, then sign +
+    // RNitermax pseudo-steps + final faces, or one full bcond pass
+    return 2 + 1 + 6 + (b->cfg.RNitermax > 0 ? 1 + b->cfg.RNitermax + 1 : 1);
 }
 
 const char* lsm_batch_last_error(lsm_batch_handle b) { return b ? b->err.c_str() : ""; }

@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(VOL_THREADS) volume_kernel(DevGrid g, CellBox 
                 C[v][0] = __ldg(x + o[v]); C[v][1] = __ldg(y + o[v]); C[v][2] = __ldg(z + o[v]);
             }
             if (allw) B = hex_volume(C);
-            else cell_analysis(P, C, &K, &S, err);
+            else cell_analysis<true>(P, C, &K, &S, err);
         }
         if (cellvol) cellvol[l] = K + S + B;
     }

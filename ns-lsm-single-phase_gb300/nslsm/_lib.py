@@ -54,7 +54,8 @@ class LsmBatchInstance(C.Structure):
 class LsmBatchConfig(C.Structure):
     """struct lsm_batch_config"""
     _fields_ = [("RNitermax", C.c_int), ("btype_lsm", C.c_int * 6), ("BigPhi", C.c_double),
-                ("use_graph", C.c_int), ("autotune", C.c_int), ("shape", C.c_int)]
+                ("use_graph", C.c_int), ("autotune", C.c_int), ("shape", C.c_int),
+                ("precision", C.c_int)]
 
 
 EXCHANGE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.POINTER(LsmGrid))
@@ -100,6 +101,11 @@ SIGNATURES = {
     "lsm_batch_set_phi": (_i, [_vp, _i, _vp]),
     "lsm_batch_get_phi": (_i, [_vp, _i, _vp]),
     "lsm_batch_step": (_i, [_vp, _i, _vp]),
+    "lsm_batch_forward_record": (_i, [_vp, _i, _i]),
+    "lsm_batch_set_grad_phi": (_i, [_vp, _i, _vp]),
+    "lsm_batch_backward": (_i, [_vp]),
+    "lsm_batch_get_grad_phi0": (_i, [_vp, _i, _vp]),
+    "lsm_batch_get_grad_velocity": (_i, [_vp, _i, _vp]),
     "lsm_batch_shape": (_i, [_vp] + [C.POINTER(_i)] * 4),
     "lsm_batch_nodes": (C.c_longlong, [_vp]),
     "lsm_batch_launches_per_step": (_i, [_vp]),

@@ -1,9 +1,17 @@
-"""Batched FP32 level-set transport (include/lsm_batch.h) from Python.
+"""Batched level-set transport (include/lsm_batch.h) from Python.
 
     b = LevelSetBatch(instances, RNitermax=5, btype=(1,)*6, BigPhi=5.0)
     b.set_geometry(k, x, y, z, csi, eta, zet); b.set_velocity(k, q); b.set_phi(k, phi)
     vols = b.step(100)          # (ninst, 4) pre-advection volumes of the last step
     phi_k = b.get_phi(k)
+
+    # adjoint: dL/dphi0 and dL/dq through `nsteps` steps
+    b.forward_record(nsteps, checkpoint_every=4)
+    b.set_grad_phi(k, dL_dphi_k); b.backward()
+    g_phi0, g_q = b.get_grad_phi0(k), b.get_grad_velocity(k)
+
+    # the same through torch.autograd
+    outs = transport(b, nsteps, phi0_list, q_list)
 
 Arrays follow the same conventions as nslsm.api: numpy in the reference's
 Fortran layout or CUDA tensors with the reversed shape.
@@ -22,8 +30,10 @@ from .api import _addr, _is_torch, Grid
 class LevelSetBatch:
     def __init__(self, instances: Sequence[Tuple[int, int, int, float, float, float]], RNitermax: int = 5,
                  btype: Sequence[int] = (1, 1, 1, 1, 1, 1), BigPhi: float = 5.0, device: int = 0, stream=None,
-                 use_graph: bool = True, autotune: bool = True, shape: int = 0):
-        """instances: (ni, nj, nk, dt, dtau, eps) per instance."""
+                 use_graph: bool = True, autotune: bool = True, shape: int = 0, precision: str = "fp32"):
+        """instances: (ni, nj, nk, dt, dtau, eps) per instance; precision "fp32" or "fp64"."""
+        if precision not in ("fp32", "fp64"):
+            raise ValueError("precision must be 'fp32' or 'fp64'")
         self.lib = _lib.load()
         n = len(instances)
         arr = (_lib.LsmBatchInstance * n)()
@@ -36,6 +46,8 @@ class LevelSetBatch:
             cfg.btype_lsm[f] = int(btype[f])
         cfg.BigPhi = float(BigPhi)
         cfg.use_graph, cfg.autotune, cfg.shape = int(use_graph), int(autotune), int(shape)
+        cfg.precision = 1 if precision == "fp64" else 0
+        self.precision = precision
         h = C.c_void_p()
         st = self.lib.lsm_batch_create(C.byref(h), int(device), stream, n, arr, C.byref(cfg))
         if st != 0:
@@ -90,6 +102,38 @@ class LevelSetBatch:
                   "lsm_batch_step")
         return v
 
+    # ------------------------------------------------------------ adjoint
+    def forward_record(self, nsteps: int, checkpoint_every: int = 4):
+        self._chk(self.lib.lsm_batch_forward_record(self.h, int(nsteps), int(checkpoint_every)),
+                  "lsm_batch_forward_record")
+
+    def set_grad_phi(self, k, grad):
+        g = self.grids[k]
+        self._chk(self.lib.lsm_batch_set_grad_phi(self.h, k, _addr(grad, g, 1, np.float64)), "lsm_batch_set_grad_phi")
+
+    def backward(self):
+        self._chk(self.lib.lsm_batch_backward(self.h), "lsm_batch_backward")
+
+    def _out(self, k, ncomp, like):
+        g = self.grids[k]
+        if like is not None and _is_torch(like):
+            import torch
+            shp = (g.nk, g.nj, g.ni) + ((ncomp,) if ncomp > 1 else ())
+            return torch.zeros(shp, dtype=torch.float64, device=like.device)
+        return np.zeros(((ncomp,) if ncomp > 1 else ()) + g.shape, order="F")
+
+    def get_grad_phi0(self, k, like=None):
+        out = self._out(k, 1, like)
+        self._chk(self.lib.lsm_batch_get_grad_phi0(self.h, k, _addr(out, self.grids[k], 1, np.float64)),
+                  "lsm_batch_get_grad_phi0")
+        return out
+
+    def get_grad_velocity(self, k, like=None):
+        out = self._out(k, 4, like)
+        self._chk(self.lib.lsm_batch_get_grad_velocity(self.h, k, _addr(out, self.grids[k], 4, np.float64)),
+                  "lsm_batch_get_grad_velocity")
+        return out
+
     @property
     def nodes(self) -> int:
         return int(self.lib.lsm_batch_nodes(self.h))
@@ -103,3 +147,52 @@ class LevelSetBatch:
         i, x, y, z = C.c_int(), C.c_int(), C.c_int(), C.c_int()
         self._chk(self.lib.lsm_batch_shape(self.h, C.byref(i), C.byref(x), C.byref(y), C.byref(z)), "shape")
         return i.value, (x.value, y.value, z.value)
+
+
+def _transport_function():
+    import torch
+
+    class _Transport(torch.autograd.Function):
+        """phi^0 (per instance), q (per instance) -> phi^nsteps through the
+        batch's level-set steps; backward runs the hand-written adjoint."""
+
+        @staticmethod
+        def forward(ctx, batch, nsteps, ckpt, *tensors):
+            n = batch.ninst
+            phis, qs = tensors[:n], tensors[n:]
+            for k in range(n):
+                batch.set_velocity(k, qs[k].detach().contiguous())
+                batch.set_phi(k, phis[k].detach().contiguous())
+            batch.forward_record(nsteps, ckpt)
+            ctx.batch = batch
+            ctx.like = phis[0]
+            return tuple(batch.get_phi(k, like=phis[k]) for k in range(n))
+
+        @staticmethod
+        def backward(ctx, *grads):
+            b = ctx.batch
+            for k, g in enumerate(grads):
+                if g is None:
+                    g = torch.zeros((b.grids[k].nk, b.grids[k].nj, b.grids[k].ni), dtype=torch.float64,
+                                    device=ctx.like.device)
+                b.set_grad_phi(k, g.detach().to(torch.float64).contiguous())
+            b.backward()
+            gphi = [b.get_grad_phi0(k, like=ctx.like) for k in range(b.ninst)]
+            gq = [b.get_grad_velocity(k, like=ctx.like) for k in range(b.ninst)]
+            return (None, None, None, *gphi, *gq)
+
+    return _Transport
+
+
+_TRANSPORT = None
+
+
+def transport(batch: LevelSetBatch, nsteps: int, phi0, q, checkpoint_every: int = 4):
+    """Differentiable batched transport: lists of CUDA float64 tensors phi0[k]
+    (nk, nj, ni) and q[k] (nk, nj, ni, 4) -> list of phi^nsteps[k].  The
+    geometry must already be set on `batch`; its state is overwritten."""
+    global _TRANSPORT
+    if _TRANSPORT is None:
+        _TRANSPORT = _transport_function()
+    outs = _TRANSPORT.apply(batch, int(nsteps), int(checkpoint_every), *phi0, *q)
+    return list(outs)
