@@ -1,27 +1,41 @@
 """Benchmark of the level-set transport step on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload batched|fp64]
+                    [--workload fwdadj|batched|fp64]
 
-Default workload ("batched"): 64 independent instances with per-axis sizes
-drawn from {32..96} (numpy seed 0), identity-plus-random-shear grids,
-phi0 = z - 0.5 - 4 random Fourier modes, divergence-free curl velocity,
-CFL 0.5, 5 reinitialisation pseudo-steps per step -- the whole batch
-advanced by the FP32 batched kernels (one launch per pass, CUDA graph per
-step, autotuned tile shape) with the FP64 water volume every step.
+Default workload ("fwdadj"): the large free-surface case, 512 x 256 x 256
+curvilinear nodes (x = 16 xi + 0.05 sin(2 pi eta), y = 4 eta, z = 2 zeta^1.3),
+phi0 = z - 1 - 0.08 sech^2(k(x-4)) (1 + 0.2 cos(2 pi y / 4)), solitary-wave
+velocity, CFL 0.4, 10 reinitialisation pseudo-steps per step, FP64 water
+volume every step.  One benchmark step = one 20-step checkpoint segment of
+the FP32 batched path forward (CUDA graph per physical step, autotuned tile
+shape) followed by its hand-written adjoint (segment recomputed once from
+its checkpoint, then reversed), seeded with dL/dphi_T of a linear loss with
+seeded weights; successive benchmark steps continue the trajectory (10
+steps = the 200-step run).  Beside it: the plain FP64 GPU path
+(lsm_levelsetmethod, the reference's arithmetic) on the same grid, timed,
+and used as the FP64 reference for the FP32 path's narrow-band phi error
+and volume difference after 20 steps.
+
+"batched" workload: 64 independent instances with per-axis sizes drawn from
+{32..96} (numpy seed 0), identity-plus-random-shear grids, Fourier phi0,
+divergence-free curl velocity, CFL 0.5, 5 reinitialisation pseudo-steps per
+step, forward only.
 
 "fp64" workload: the curvilinear solitary-wave case, 256 x 128 x 96 nodes,
 10 reinitialisation pseudo-steps per step, through `lsm_levelsetmethod` in
 the reference's FP64 arithmetic.
 
-Metric: Gcell-steps/s = grid nodes x physical steps / second (whole job).
+Metric: Gcell-steps/s = grid nodes x physical steps / second (whole job;
+for "fwdadj" each cell-step is forward + adjoint).
   value : device-resident inputs, CUDA events on the launching stream.
-  e2e   : the same steps with the per-step inputs (velocity) copied in from
-          pinned host memory and phi read back every step.
+  e2e   : the same through the C-ABI with host arrays: phi0, q and the
+          loss seed copied in, phi_T and both gradients copied out.
 Synthetic inputs with the workloads' shapes and value distributions (the
 reference ships no input decks).  The reference arm (--impl reference)
 times the CPU FP64 restatement of the reference (the Fortran/MPI original
-cannot be built: no Fortran compiler) with all host threads.
+cannot be built: no Fortran compiler) with all host threads; the reference
+has no adjoint, so its figure is forward only.
 """
 from __future__ import annotations
 
@@ -474,9 +488,247 @@ def batch_cpu_baseline(meta, R):
 
 # ---------------------------------------------------------------- FP64 arm
 def run_ours(args):
+    if args.workload == "fwdadj":
+        return run_fwdadj(args)
     if args.workload == "batched":
         return run_batched(args)
     return run_fp64(args)
+
+
+# ------------------------------------------------- FP32 forward + adjoint arm
+FWDADJ = dict(ni=512, nj=256, nk=256, reinit_iters=10, segment=20, compare_steps=20)
+
+# algorithmic HBM bytes per node for one launch of the FP32 batched kernels
+# (each distinct array read once and written once; halos not counted)
+FWDADJ_BYTES = {
+    "k_contra": 15 * 4,            # u(3), metrics(9); W(3)
+    "k_stage": 17.0 / 3.0 * 4,     # phi_prev, phi^n (stages 2-3), W(3); stage output
+    "k_sign": 11 * 4,              # phi0, metrics(9); s
+    "k_reinit": 12 * 4,            # d, s, metrics(9); d
+    "k_volume": 4 + 8,             # phi (FP32) + fixed-point cell volume (interface-cell coordinates not counted)
+    "k_bc_full": 2 * 4,            # phi in, phi out
+    "k_adj_stage": 14 * 4,         # in, W(3), lamP0, lamPhin (rmw), lamW(3, rmw); lam_in
+    "k_adj_reinit_coef": 18 * 4,   # d, s, metrics(9), lam; coefficients(6)
+    "k_adj_reinit_apply": 8 * 4,   # lam, coefficients(6); lam_out
+    "k_adj_contra": 18 * 4,        # lamW(3), metrics(9), lam_u(3, rmw)
+    "k_cvt_in": 8 + 4,
+    "k_cvt_out": 4 + 8,
+}
+
+
+def _roofline(prof, n, peaks, table, dtype_note):
+    name, (cnt, tms) = max(prof.items(), key=lambda kv: kv[1][1])
+    byt = table.get(name)
+    avg = tms / 1e3 / max(cnt, 1)
+    peak = float(peaks.get("hbm_gbs", 6800.0)) if peaks else 6800.0
+    ach = None if byt is None else byt * n / avg / 1e9
+    total = sum(v[1] for v in prof.values())
+    return {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak, "unit": "GB/s",
+            "frac": None if ach is None else ach / peak, "traffic": read_traffic(name, n),
+            "algorithmic_bytes_per_launch": None if byt is None else byt * n, "avg_launch_us": avg * 1e6,
+            "share": tms / total if total else None,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s",
+            "bytes_note": dtype_note,
+            "per_kernel_frac": {k: (table[k] * n / (v[1] / 1e3 / v[0]) / 1e9 / peak)
+                                for k, v in prof.items() if k in table}}
+
+
+def run_fwdadj(args):
+    import torch
+    from nslsm import LevelSet, LsmParams, configs, _lib
+    from nslsm._lib import KernelTimer
+    from nslsm.batch import LevelSetBatch
+
+    rank, world = dist_setup(args.gpus)
+    dev_index = torch.cuda.current_device()
+    W = dict(FWDADJ)
+    if args.grid:
+        W["ni"], W["nj"], W["nk"] = (int(v) for v in args.grid.lower().split("x"))
+    R, S = W["reinit_iters"], W["segment"]
+    case = configs.large_free_surface(W["ni"], W["nj"], W["nk"], reinit_iters=R)
+    g = case.grid
+    n = g.n
+
+    def dev(a):
+        return torch.from_numpy(np.ascontiguousarray(np.asfortranarray(a).T)).cuda()
+
+    ls = LevelSet(device=dev_index)
+    stream = torch.cuda.Stream()
+    x, y, z = dev(case.x), dev(case.y), dev(case.z)
+    csi, eta, zet, aj = ls.mg_metrics(g, x, y, z)
+    q = dev(case.q(0.0))
+    phi0 = dev(case.phi0)
+    smax = max(float((m * q[..., 1:4]).sum(-1).abs().max()) for m in (csi, eta, zet))
+    dt = case.cfl / smax
+    cp = case.params
+    eps, dtau = cp.epslsm, cp.RNtimestep
+
+    # ---- plain FP64 GPU path on the same grid: timed, and the FP64 reference
+    # for the FP32 path's accuracy after `compare_steps` steps
+    p64 = LsmParams(epslsm=eps, delti_lsm=dt, RNitermax=R, RNtimestep=dtau, isnarrow=1, narrowcoef=4.0, BigPhi=5.0)
+    ls.set_stream(torch.cuda.current_stream().cuda_stream)
+    phi64, phin64 = phi0.clone(), phi0.clone()
+    nc = W["compare_steps"]
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    vol64 = None
+    for it in range(1, nc + 1):
+        if it == 2:
+            e0.record()
+        phin64.copy_(phi64)
+        vol64 = ls.levelsetmethod(g, p64, q, csi, eta, zet, aj, phi64, phin64, x, y, z, it)
+    e1.record()
+    torch.cuda.synchronize()
+    v64 = n * (nc - 1) / (e0.elapsed_time(e1) / 1e3) / 1e9
+    ls.set_stream(None)
+
+    # ---- the FP32 batch (one instance of the whole grid)
+    b = LevelSetBatch([(g.ni, g.nj, g.nk, dt, dtau, eps)], RNitermax=R, btype=(1,) * 6, BigPhi=5.0,
+                      stream=stream.cuda_stream)
+    b.set_geometry(0, x, y, z, csi, eta, zet)
+    b.set_velocity(0, q)
+    b.set_phi(0, phi0)
+    vols32 = b.step(nc)
+    phi32 = b.get_phi(0, like=phi0)
+    band = phi64.abs() < 4.0 * eps
+    band_err = float((phi32 - phi64).abs()[band].max())
+    vol_err = abs(float(vols32[0, 3]) - float(vol64[3])) / abs(float(vol64[3]))
+    del phi32, band
+    b.set_phi(0, phi0)
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    wts = torch.randn(phi0.shape, generator=gen, dtype=torch.float64, device="cuda")
+
+    def bench_step():
+        b.forward_record(S, S)
+        b.set_grad_phi(0, wts)
+        b.backward()
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            bench_step()
+    torch.cuda.synchronize()
+    dist_barrier(world)
+    lib = _lib.load()
+    l0 = lib.lsm_kernel_launch_count(None)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev_index) as clocks:
+        time.sleep(0.5)
+        torch.cuda.synchronize()
+        t_start = time.time()
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            for _ in range(args.steps):
+                bench_step()
+            ev1.record(stream)
+        torch.cuda.synchronize()
+        clocks.mark(t_start, time.time())
+        time.sleep(0.2)
+    launches = lib.lsm_kernel_launch_count(None) - l0
+    dist_barrier(world)
+    ms = ev0.elapsed_time(ev1)
+    ms_max = dist_max(ms, world)
+    value = world * n * S * args.steps / (ms_max / 1e3) / 1e9
+    shape = b.shape
+
+    # ---- per-kernel attribution: a batch without the graph, one shorter
+    # segment (4 steps) forward + adjoint under the library's event timer
+    b2 = LevelSetBatch([(g.ni, g.nj, g.nk, dt, dtau, eps)], RNitermax=R, btype=(1,) * 6, BigPhi=5.0,
+                       stream=stream.cuda_stream, use_graph=False, autotune=False, shape=shape[0])
+    b2.set_geometry(0, x, y, z, csi, eta, zet)
+    b2.set_velocity(0, q)
+    b2.set_phi(0, phi0)
+    b2.forward_record(2, 2)
+    b2.set_grad_phi(0, wts)
+    b2.backward()
+    torch.cuda.synchronize()
+    with KernelTimer() as kt:
+        b2.forward_record(4, 4)
+        b2.set_grad_phi(0, wts)
+        b2.backward()
+        torch.cuda.synchronize()
+        prof = kt.read()
+    b2.close()
+    peaks = load_peaks()
+    roof = _roofline(prof, n, peaks, FWDADJ_BYTES, "FP32 words x 4 B per node (FP64 cell volume 8 B)")
+    # whole-step roofline: algorithmic bytes of every launch of the profiled
+    # 4-step segment, per cell-step, at the measured throughput
+    seg_bytes = sum(FWDADJ_BYTES[k] * n * v[0] for k, v in prof.items() if k in FWDADJ_BYTES)
+    per_cell_step = seg_bytes / (4.0 * n)
+    step_roof = {"algorithmic_bytes_per_cell_step": per_cell_step,
+                 "achieved_gbs": per_cell_step * value,
+                 "frac": per_cell_step * value / roof["peak"],
+                 "note": "segment of 4 steps profiled; the 20-step segment's checkpoint copy is 0.4 B/cell-step"}
+
+    # ---- end to end through the C-ABI with host (pinned) arrays
+    def pinned(a):
+        a = np.asfortranarray(a)
+        t = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
+        v = t.numpy().reshape(a.shape, order="F")
+        v[...] = a
+        return v, t
+
+    h_phi, t1 = pinned(case.phi0)
+    h_q, t2 = pinned(case.q(0.0))
+    h_w, t3 = pinned(wts.cpu().numpy().T)
+    h_phiT, t4 = pinned(np.zeros(g.shape))
+    h_gphi, t5 = pinned(np.zeros(g.shape))
+    h_gq, t6 = pinned(np.zeros((4,) + g.shape))
+    keep = (t1, t2, t3, t4, t5, t6)
+    e2e_steps = 2
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        b.set_phi(0, h_phi)
+        b.set_velocity(0, h_q)
+        b.forward_record(S, S)
+        b._chk(b.lib.lsm_batch_get_phi(b.h, 0, h_phiT.ctypes.data), "get_phi")
+        b.set_grad_phi(0, h_w)
+        b.backward()
+        b._chk(b.lib.lsm_batch_get_grad_phi0(b.h, 0, h_gphi.ctypes.data), "get_grad_phi0")
+        b._chk(b.lib.lsm_batch_get_grad_velocity(b.h, 0, h_gq.ctypes.data), "get_grad_velocity")
+    torch.cuda.synchronize()
+    e2e_s = dist_max(time.perf_counter() - t0, world)
+    e2e_value = world * n * S * e2e_steps / e2e_s / 1e9
+    del keep
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sec, used = cpu_oracle_time(case, 1, host_threads())
+        cpu = {"value": n / sec / 1e9, "unit": "Gcell-steps/s", "cores": used, "kind": "port",
+               "sample": "1 physical forward step of the full %dx%dx%d grid (CPU FP64 oracle, OpenMP, %d threads; "
+                         "the reference has no adjoint)" % (g.ni, g.nj, g.nk, used)}
+    if rank == 0:
+        line = {
+            "metric": "Gcell-steps/s (batched FP32 level-set forward + adjoint: WENO3-RK3 + %d reinit pseudo-steps + "
+                      "FP64 volume; vs the plain FP64 GPU path)" % R,
+            "value": value, "unit": "Gcell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (analytic 3-D free surface and solitary-wave velocity; the reference "
+                                    "ships no decks)",
+            "config": {"workload": "large_free_surface %dx%dx%d curvilinear, CFL 0.4, %d reinit pseudo-steps/step, "
+                                   "volume each step; one step = %d-step segment forward (CUDA graph) + adjoint with "
+                                   "a checkpoint every %d steps" % (g.ni, g.nj, g.nk, R, S, S),
+                       "nodes": n, "physical_steps_per_step": S, "tile_shape": shape[1],
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "loss": "linear, seeded N(0,1) weights on phi_T",
+                       "l2": "inputs larger than L2 (phi alone %.2f GB > 129 MB)" % (n * 4 / 1e9)},
+            "roofline": roof,
+            "step_roofline": step_roof,
+            "cpu_baseline": cpu,
+            "fp64_gpu_path": {"value": v64, "unit": "Gcell-steps/s", "sample": "%d forward steps of the same grid, "
+                              "lsm_levelsetmethod (reference FP64 arithmetic)" % (nc - 1),
+                              "speedup_fp32_fwd_adj": value / v64},
+            "accuracy_vs_fp64": {"steps": nc, "band_linf_phi_err": band_err, "band": "|phi64| < 4 epslsm (6 cells)",
+                                 "volume_rel_diff": vol_err},
+            "e2e": {"value": e2e_value, "unit": "Gcell-steps/s", "h2d_bytes_per_step": 8 * n * (1 + 4 + 1),
+                    "d2h_bytes_per_step": 8 * n * (1 + 1 + 4), "steps": e2e_steps},
+            "clocks": clocks.summary(),
+            "gpu_launches": launches,
+            "kernel_times_ms": {k: {"launches": v[0], "total_ms": round(v[1], 4)} for k, v in prof.items()},
+        }
+        print(json.dumps(line))
+    b.close()
+    ls.close()
 
 
 def run_fp64(args):
@@ -604,6 +856,8 @@ def run_reference(args):
         return
     if args.workload == "batched":
         return run_reference_batched(args, world)
+    if args.workload == "fwdadj":
+        return run_reference_fwdadj(args, world)
     W = workload(args)
     case = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"])
     threads = host_threads()
@@ -680,6 +934,38 @@ def run_reference_batched(args, world):
     print(json.dumps(line))
 
 
+def run_reference_fwdadj(args, world):
+    """The CPU FP64 restatement of the reference (all host threads) on the
+    large free-surface grid: each timed step is one physical forward step of
+    the whole grid (the reference has no adjoint)."""
+    from nslsm import configs
+    W = dict(FWDADJ)
+    if args.grid:
+        W["ni"], W["nj"], W["nk"] = (int(v) for v in args.grid.lower().split("x"))
+    R = W["reinit_iters"]
+    case = configs.large_free_surface(W["ni"], W["nj"], W["nk"], reinit_iters=R)
+    threads = host_threads()
+    steps = max(1, min(args.steps, 2))
+    sec, used = cpu_oracle_time(case, steps, threads)
+    v = case.grid.n / sec / 1e9
+    line = {
+        "impl": "reference",
+        "metric": "Gcell-steps/s (batched FP32 level-set forward + adjoint: WENO3-RK3 + %d reinit pseudo-steps + "
+                  "FP64 volume; vs the plain FP64 GPU path)" % R,
+        "value": v, "unit": "Gcell-steps/s", "n_gpus": world, "steps": steps, "warmup": 0,
+        "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "large_free_surface %dx%dx%d curvilinear, %d reinit pseudo-steps/step"
+                               % (W["ni"], W["nj"], W["nk"], R)},
+        "cpu_baseline": {"value": v, "unit": "Gcell-steps/s", "cores": used, "kind": "port",
+                         "sample": "%d physical forward steps of the whole grid; CPU FP64 restatement of the "
+                                   "reference (the Fortran/MPI original cannot be built here: no Fortran compiler); "
+                                   "the reference has no adjoint, so forward only" % steps},
+        "e2e": {"value": v, "unit": "Gcell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
 def workload(args):
     W = dict(WORKLOAD)
     if args.grid:
@@ -690,15 +976,17 @@ def workload(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=None, help="timed steps (default 10 for fwdadj, else 30)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--grid", default=None, help="NIxNJxNK instead of the 256x128x96 workload (profiling runs)")
-    ap.add_argument("--workload", choices=["batched", "fp64"], default="batched")
+    ap.add_argument("--grid", default=None, help="NIxNJxNK instead of the workload's grid (profiling runs)")
+    ap.add_argument("--workload", choices=["fwdadj", "batched", "fp64"], default="fwdadj")
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--n-inst", type=int, default=None, help="instances of the batched workload (profiling runs)")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 10 if args.workload == "fwdadj" else 30
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":

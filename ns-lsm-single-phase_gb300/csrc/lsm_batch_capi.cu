@@ -220,24 +220,26 @@ FieldsT<float>& fields<float>(lsm_batch* b) { return b->f32; }
 template <>
 FieldsT<double>& fields<double>(lsm_batch* b) { return b->f64; }
 
-// Recorded internals of one step (adjoint): the three stage outputs and the
-// RNitermax raw reinitialisation outputs (D + k N).
+// Recorded internals of one step (adjoint): the three stage outputs, the
+// RNitermax raw pseudo-step outputs (D + k N) and the sign field.
 template <typename T>
 struct Rec {
     T* A[3];
     T* D;
+    T* sgn;
 };
 
-// One physical step phin -> phi_out (phi_out may alias phin).  With `rec`
-// the stage outputs and the pseudo-step outputs are kept and the final
-// bcond_lsm is skipped (phi_out unused); `vol` adds the pre-advection water
-// volume.
+// One physical step phin -> phi_out (phi_out may alias phin; nullptr skips
+// the final bcond_lsm).  With `rec` the stage outputs, the pseudo-step
+// outputs (before the final bcond_lsm) and the sign field are kept; `vol`
+// adds the pre-advection water volume.
 template <typename T>
 void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec, bool vol) {
     namespace B = lsm::batch;
     const int sh = b->shape, gr = b->grid, nb = b->nbricks;
     const B::BC bc = make_bc(b);
-    FieldsT<T>& f = fields<T>(b);
+    FieldsT<T> f = fields<T>(b);
+    if (rec) f.sgn = rec->sgn;
     const long long N = b->N;
     if (vol) {
         B::volume<T>(sh, gr, b->d_inst, b->d_brick, nb, f, phin, b->d_part, b->stream);
@@ -265,8 +267,10 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
             if (last && !rec) B::bc_reinit<T>(b->d_inst, b->ninst, b->nface, f, bc, cur, phi_out, b->stream);
             cur = o;
         }
-    } else if (!rec) {
-        B::bc_full<T>(sh, gr, b->d_inst, b->d_brick, nb, bc, S[2], phi_out, b->d_err, b->stream);
+        // recorded steps keep the raw last pseudo-step and write phi^{n+1} apart
+        if (rec && phi_out) B::bc_full<T>(sh, gr, b->d_inst, b->d_brick, nb, bc, cur, phi_out, nullptr, b->stream);
+    } else if (phi_out) {
+        B::bc_full<T>(sh, gr, b->d_inst, b->d_brick, nb, bc, S[2], phi_out, rec ? nullptr : b->d_err, b->stream);
     }
 }
 
@@ -350,19 +354,30 @@ int check_inst(lsm_batch* b, int q) {
 }
 
 // ------------------------------------------------------------ adjoint state
-// Checkpoints (nck N), segment states (ck N), stage outputs (3 N),
-// pseudo-step outputs (R N), adjoint fields lam, lam2, lamPhin (3 N), lamW
-// (3 N), reinitialisation coefficients (6 N), lam_u (3 N).
+// Checkpoints (nck N), segment states (ck N), the recorded internals of
+// every step of a segment (ck (4 + R) N: A1..A3, D1..DR, sign), adjoint
+// fields lam, lam2, lamPhin (3 N), lamW (3 N), reinitialisation
+// coefficients (6 N), lam_u (3 N).
 template <typename T>
 struct AdjView {
-    T *ckpt, *seg, *A[3], *D, *lam, *lam2, *lamPhin, *lamW[3], *coef, *lamU[3];
+    T *ckpt, *seg, *slots, *lam, *lam2, *lamPhin, *lamW[3], *coef, *lamU[3];
 };
 
 int n_ckpt(int nsteps, int ck) { return (nsteps + ck - 1) / ck; }
+long long slot_elems(const lsm_batch* b) { return (long long)(4 + b->cfg.RNitermax) * b->N; }
 
 size_t adj_elems(const lsm_batch* b, int nsteps, int ck) {
-    return (size_t)b->N *
-           (size_t)(n_ckpt(nsteps, ck) + ck + 3 + std::max(b->cfg.RNitermax, 1) + 3 + 3 + 6 + 3);
+    return (size_t)b->N * (size_t)(n_ckpt(nsteps, ck) + ck + 3 + 3 + 6 + 3) + (size_t)ck * (size_t)slot_elems(b);
+}
+
+template <typename T>
+Rec<T> slot(lsm_batch* b, const AdjView<T>& v, int q) {
+    T* p = v.slots + (long long)q * slot_elems(b);
+    Rec<T> r;
+    for (int s = 0; s < 3; ++s) r.A[s] = p + (long long)s * b->N;
+    r.D = p + 3 * b->N;
+    r.sgn = p + (long long)(3 + b->cfg.RNitermax) * b->N;
+    return r;
 }
 
 template <typename T>
@@ -374,12 +389,8 @@ AdjView<T> adj_view(lsm_batch* b) {
     p += (long long)n_ckpt(b->rec_steps, b->rec_ck) * N;
     v.seg = p;
     p += (long long)b->rec_ck * N;
-    for (int s = 0; s < 3; ++s) {
-        v.A[s] = p;
-        p += N;
-    }
-    v.D = p;
-    p += (long long)std::max(b->cfg.RNitermax, 1) * N;
+    v.slots = p;
+    p += (long long)b->rec_ck * slot_elems(b);
     v.lam = p;
     p += N;
     v.lam2 = p;
@@ -431,12 +442,14 @@ int forward_record_t(lsm_batch* b, int nsteps, int ck) {
     return LSM_OK;
 }
 
-// Reverse of one physical step; on entry lam holds the adjoint of phi^{n+1},
-// on exit the adjoint of phi^n (the pointers of `v` swap along the way).
+// Reverse of one physical step from its recorded internals `r`; on entry
+// lam holds the adjoint of phi^{n+1}, on exit the adjoint of phi^n (the
+// pointers of `v` swap along the way).
 template <typename T>
-void adj_step(lsm_batch* b, AdjView<T>& v, const T* phin) {
+void adj_step(lsm_batch* b, AdjView<T>& v, const Rec<T>& r, const T* phin) {
     namespace B = lsm::batch;
-    FieldsT<T>& f = fields<T>(b);
+    FieldsT<T> f = fields<T>(b);
+    f.sgn = r.sgn;
     const B::BC bc = make_bc(b);
     const long long N = b->N;
     const Flat fl{b->d_inst, b->d_offs, b->ninst, N};
@@ -446,19 +459,19 @@ void adj_step(lsm_batch* b, AdjView<T>& v, const T* phin) {
             B::adj_face<T>(fl, face, b->nplane[face >> 1], bc, kind, pn, in, out, c1, c2, v.lam, b->stream);
     };
     if (R > 0) {
-        faces(1, nullptr, nullptr, v.D + (long long)(R - 1) * N, 0.0, 0.0);
+        faces(1, nullptr, nullptr, r.D + (long long)(R - 1) * N, 0.0, 0.0);
         for (int k = R - 1; k >= 0; --k) {
-            const T* dk = k == 0 ? v.A[2] : v.D + (long long)(k - 1) * N;
+            const T* dk = k == 0 ? r.A[2] : r.D + (long long)(k - 1) * N;
             B::adj_reinit<T>(fl, f, dk, v.lam, v.coef, v.lam2, b->stream);
             std::swap(v.lam, v.lam2);
         }
     } else {
-        faces(1, nullptr, nullptr, v.A[2], 0.0, 0.0);
+        faces(1, nullptr, nullptr, r.A[2], 0.0, 0.0);
     }
     // stages 3, 2, 1: inputs A2, A1, phi^n; outputs A3, A2, A1
-    const T* ins[3] = {phin, v.A[0], v.A[1]};
+    const T* ins[3] = {phin, r.A[0], r.A[1]};
     for (int s = 2; s >= 0; --s) {
-        faces(0, phin, ins[s], v.A[s], kC[s][0], kC[s][1]);
+        faces(0, phin, ins[s], r.A[s], kC[s][0], kC[s][1]);
         B::adj_stage<T>(fl, f, ins[s], v.lam, v.lam2, v.lamPhin, v.lamW[0], v.lamW[1], v.lamW[2], kC[s][0], kC[s][1],
                         kC[s][2], s == 0, b->stream);
         std::swap(v.lam, v.lam2);
@@ -474,19 +487,17 @@ int backward_t(lsm_batch* b) {
     T* const zero_fields[7] = {v.lamPhin, v.lamW[0], v.lamW[1], v.lamW[2], v.lamU[0], v.lamU[1], v.lamU[2]};
     for (T* p : zero_fields) k_zero<T><<<cblocks(N), 256, 0, b->stream>>>(N, p);
     const int ck = b->rec_ck, nsteps = b->rec_steps, nseg = n_ckpt(nsteps, ck);
-    Rec<T> rec;
-    for (int s = 0; s < 3; ++s) rec.A[s] = v.A[s];
-    rec.D = v.D;
     for (int sg = nseg - 1; sg >= 0; --sg) {
         const int c0 = sg * ck, L = std::min(c0 + ck, nsteps) - c0;
+        // recompute the segment once from its checkpoint, keeping every
+        // step's internals, then reverse it step by step
         BCU(b, cudaMemcpyAsync(v.seg, v.ckpt + (long long)sg * N, sizeof(T) * N, cudaMemcpyDeviceToDevice, b->stream));
-        for (int q = 0; q + 1 < L; ++q)
-            enqueue_step_io<T>(b, v.seg + (long long)q * N, v.seg + (long long)(q + 1) * N, nullptr, false);
-        for (int q = L - 1; q >= 0; --q) {
-            const T* phin = v.seg + (long long)q * N;
-            enqueue_step_io<T>(b, phin, nullptr, &rec, false);
-            adj_step<T>(b, v, phin);
+        for (int q = 0; q < L; ++q) {
+            const Rec<T> r = slot<T>(b, v, q);
+            enqueue_step_io<T>(b, v.seg + (long long)q * N, q + 1 < L ? v.seg + (long long)(q + 1) * N : nullptr, &r,
+                               false);
         }
+        for (int q = L - 1; q >= 0; --q) adj_step<T>(b, v, slot<T>(b, v, q), v.seg + (long long)q * N);
     }
     const Flat fl{b->d_inst, b->d_offs, b->ninst, N};
     lsm::batch::adj_contra<T>(fl, fields<T>(b), v.lamW[0], v.lamW[1], v.lamW[2], v.lamU[0], v.lamU[1], v.lamU[2],

@@ -13,6 +13,11 @@ run small (parity tests) or at full size (benchmarks).
                        y = 2 eta, z = zeta^1.3, phi0 = z - (0.5 + A sech^2(k(x-2))),
                        uniform flow + solitary-wave perturbation, CFL 0.4, 10
                        reinit pseudo-steps per step.
+  large_free_surface   512x256x256, the same mapping on a 16x4x2 domain, 3-D
+                       free surface phi0 = z - 1 - 0.08 sech^2(k(x-4)) (1 + 0.2
+                       cos(2 pi y / 4)), k = sqrt(3 A / (4 d^3)) with A = 0.08,
+                       depth d = 1; velocity (1,0,0) + A sqrt(g d) sech^2 in u
+                       and w; CFL 0.4, 10 reinit pseudo-steps per step.
 """
 from __future__ import annotations
 
@@ -120,6 +125,35 @@ def solitary_wave(ni: int = 256, nj: int = 128, nk: int = 96, steps: int = 200, 
                 phi0, p, steps, 0.4, velocity, redistance_iters, h)
 
 
+def large_free_surface(ni: int = 512, nj: int = 256, nk: int = 256, steps: int = 200,
+                       reinit_iters: int = 10) -> Case:
+    Lx, Ly, Lz, x0, A, depth, g = 16.0, 4.0, 2.0, 4.0, 0.08, 1.0, 9.81
+    XI, ET, ZE = _mesh(ni, nj, nk)
+    X = Lx * XI + 0.05 * np.sin(2 * np.pi * ET)
+    Y = Ly * ET
+    Z = Lz * ZE ** 1.3
+    k = math.sqrt(3.0 * A / (4.0 * depth ** 3))
+    sech2 = 1.0 / np.cosh(k * (X - x0)) ** 2
+    phi0 = _fortran(Z - depth - A * sech2 * (1.0 + 0.2 * np.cos(2 * np.pi * Y / 4.0)))
+    c = A * math.sqrt(g * depth)
+    q0 = np.zeros((4, ni, nj, nk), order="F")
+    q0[1] = 1.0 + c * sech2
+    q0[3] = c * sech2
+    del XI, ET, ZE, sech2
+
+    def velocity(t: float) -> np.ndarray:
+        return q0
+
+    dx, dy = Lx / (ni - 1), Ly / (nj - 1)
+    dz_min = Lz * (1.0 / (nk - 1)) ** 1.3
+    h = max(dx, dy)
+    p = LsmParams(epslsm=1.5 * h, numiter_lsm=1, delti_lsm=0.0, RNitermax=reinit_iters,
+                  RNtimestep=0.5 * min(dx, dy, dz_min), RNfreq=1, btype_lsm=(1,) * 6, isnarrow=1,
+                  narrowcoef=4.0, orderAD=1, BigPhi=5.0, M_Sphi0=1)
+    return Case("large_free_surface_%dx%dx%d" % (ni, nj, nk), Grid(ni, nj, nk), _fortran(X), _fortran(Y),
+                _fortran(Z), phi0, p, steps, 0.4, velocity, 0, h)
+
+
 @dc.dataclass
 class Instance:
     """One instance of a batched workload (single zone, all faces physical)."""
@@ -182,4 +216,5 @@ def batched_instances(n_inst: int = 64, lo: int = 32, hi: int = 96, seed: int = 
     return out
 
 
-CASES = {"sphere_deformation": sphere_deformation, "solitary_wave": solitary_wave}
+CASES = {"sphere_deformation": sphere_deformation, "solitary_wave": solitary_wave,
+         "large_free_surface": large_free_surface}
