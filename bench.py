@@ -507,9 +507,10 @@ FWDADJ_BYTES = {
     "k_reinit": 12 * 4,            # d, s, metrics(9); d
     "k_volume": 4 + 8,             # phi (FP32) + fixed-point cell volume (interface-cell coordinates not counted)
     "k_bc_full": 2 * 4,            # phi in, phi out
-    "k_adj_stage": 14 * 4,         # in, W(3), lamP0, lamPhin (rmw), lamW(3, rmw); lam_in
-    "k_adj_reinit_coef": 18 * 4,   # d, s, metrics(9), lam; coefficients(6)
-    "k_adj_reinit_apply": 8 * 4,   # lam, coefficients(6); lam_out
+    "k_adj_stage_x": 8 * 4,        # in, W_x, lamP0, lamPhin (rmw), lamW_x (rmw); lam_in
+    "k_adj_stage_y": 7 * 4,        # in, W_y, lamP0, lam_in (rmw), lamW_y (rmw)
+    "k_adj_stage_z": 7 * 4,        # in, W_z, lamP0, lam_in (rmw), lamW_z (rmw)
+    "k_adj_reinit": 13 * 4,        # d, s, metrics(9), lam; lam_out
     "k_adj_contra": 18 * 4,        # lamW(3), metrics(9), lam_u(3, rmw)
     "k_cvt_in": 8 + 4,
     "k_cvt_out": 4 + 8,

@@ -81,7 +81,7 @@ int lsm_batch_step(lsm_batch_handle h, int nsteps, double* volumes);
    keeping a checkpoint every `checkpoint_every` steps.  lsm_batch_backward
    recomputes each segment once from its checkpoint, keeping every step's
    internals, and reverses it.  Device memory: N (ceil(nsteps / k) +
-   k (5 + RNitermax) + 15) elements of the batch precision, k =
+   k (5 + RNitermax) + 9) elements of the batch precision, k =
    checkpoint_every. */
 int lsm_batch_forward_record(lsm_batch_handle h, int nsteps, int checkpoint_every);
 /* Seed dL/dphi at the end of the recorded steps for one instance (FP64, host

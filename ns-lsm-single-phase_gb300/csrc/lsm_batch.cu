@@ -47,6 +47,8 @@ template <typename T> __device__ __forceinline__ T vfma(T a, T b, T c) { return 
 template <> __device__ __forceinline__ float vfma<float>(float a, float b, float c) { return fmaf(a, b, c); }
 template <typename T> __device__ __forceinline__ T vsqrt(T a) { return sqrt(a); }
 template <> __device__ __forceinline__ float vsqrt<float>(float a) { return sqrtf(a); }
+template <typename T> __device__ __forceinline__ T vrsqrt(T a) { return T(1) / sqrt(a); }
+template <> __device__ __forceinline__ float vrsqrt<float>(float a) { return rsqrtf(a); }
 template <typename T> __device__ __forceinline__ T vsin(T a) { return sin(a); }
 template <> __device__ __forceinline__ float vsin<float>(float a) { return sinf(a); }
 template <typename T> __device__ __forceinline__ bool vfinite(T a) { return isfinite(a); }
@@ -62,17 +64,15 @@ struct Node {
 };
 
 template <int TX, int TY, int TZ>
-__device__ __forceinline__ Node brick_node(const Inst* __restrict__ inst, const int* __restrict__ brick_inst,
-                                           int blk) {
+__device__ __forceinline__ Node brick_node(const Inst* __restrict__ inst, const Brick* __restrict__ bricks, int blk) {
     Node b;
-    b.inst = __ldg(brick_inst + blk);
+    const int4 bk = __ldg(reinterpret_cast<const int4*>(bricks) + blk);
+    b.inst = bk.x;
     const Inst& I = inst[b.inst];
-    const int local = blk - I.brick0;
-    const int bx = local % I.nbx, by = (local / I.nbx) % I.nby, bz = local / (I.nbx * I.nby);
     const int t = threadIdx.x;
-    b.i = bx * TX + t % TX;
-    b.j = by * TY + (t / TX) % TY;
-    b.k = bz * TZ + t / (TX * TY);
+    b.i = bk.y * TX + t % TX;
+    b.j = bk.z * TY + (t / TX) % TY;
+    b.k = bk.w * TZ + t / (TX * TY);
     b.valid = b.i < I.ni && b.j < I.nj && b.k < I.nk;
     return b;
 }
@@ -155,9 +155,9 @@ __device__ __forceinline__ void weno_diff_grad(const T (&s)[5], T w, bool lo, bo
 // ------------------------------------------------------------ contra
 template <typename T, int TX, int TY, int TZ>
 __global__ void __launch_bounds__(TX * TY * TZ) k_contra(const Inst* __restrict__ inst,
-        const int* __restrict__ brick_inst, int nbricks, FieldsT<T> f) {
+        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f) {
     for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const Node b = brick_node<TX, TY, TZ>(inst, brick_inst, blk);
+        const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
         if (!b.valid) continue;
         const Inst& I = inst[b.inst];
         const long long l = I.off + b.i + (long long)I.ni * (b.j + (long long)I.nj * b.k);
@@ -205,10 +205,10 @@ __device__ __forceinline__ T stage_rhs(const FieldsT<T>& f, const T* __restrict_
 
 template <typename T, int TX, int TY, int TZ>
 __global__ void __launch_bounds__(TX * TY * TZ) k_stage(const Inst* __restrict__ inst,
-        const int* __restrict__ brick_inst, int nbricks, FieldsT<T> f, const T* __restrict__ phin,
+        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phin,
         const T* __restrict__ phi1, T* __restrict__ out, T c1, T c2, T c3) {
     for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const Node b = brick_node<TX, TY, TZ>(inst, brick_inst, blk);
+        const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
         if (!b.valid) continue;
         const Inst& I = inst[b.inst];
         const long long l = I.off + b.i + (long long)I.ni * (b.j + (long long)I.nj * b.k);
@@ -308,10 +308,10 @@ __global__ void k_bc_stage(const Inst* __restrict__ inst, int ninst, long long n
 
 template <typename T, int TX, int TY, int TZ>
 __global__ void __launch_bounds__(TX * TY * TZ) k_bc_full(const Inst* __restrict__ inst,
-        const int* __restrict__ brick_inst, int nbricks, BC bc, const T* __restrict__ src, T* __restrict__ dst,
+        const Brick* __restrict__ bricks, int nbricks, BC bc, const T* __restrict__ src, T* __restrict__ dst,
         unsigned* err) {
     for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const Node b = brick_node<TX, TY, TZ>(inst, brick_inst, blk);
+        const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
         if (!b.valid) continue;
         const Inst& I = inst[b.inst];
         const long long sj = I.ni, sk = (long long)I.ni * I.nj;
@@ -374,9 +374,9 @@ __device__ __forceinline__ T godunov(const FieldsT<T>& f, const T* __restrict__ 
 // |phi0| < eps and |grad phi0| > 0 (the lambda correction pins d to phi0).
 template <typename T, int TX, int TY, int TZ>
 __global__ void __launch_bounds__(TX * TY * TZ) k_sign(const Inst* __restrict__ inst,
-        const int* __restrict__ brick_inst, int nbricks, FieldsT<T> f, const T* __restrict__ phi0) {
+        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phi0) {
     for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const Node b = brick_node<TX, TY, TZ>(inst, brick_inst, blk);
+        const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
         if (!b.valid) continue;
         const Inst& I = inst[b.inst];
         const long long l = I.off + b.i + (long long)I.ni * (b.j + (long long)I.nj * b.k);
@@ -396,19 +396,19 @@ __global__ void __launch_bounds__(TX * TY * TZ) k_sign(const Inst* __restrict__ 
 template <typename T>
 __device__ __forceinline__ T reinit_node(const FieldsT<T>& f, const T* __restrict__ din, const Inst& I, long long l,
                                          int i, int j, int k) {
+    // every load is issued before the frozen-node test (one memory round trip)
     const T s = __ldg(f.sgn + l);
     const T d = __ldg(din + l);
-    if (s == T(0)) return d;
     const T g = godunov(f, din, I, l, i, j, k, s);
-    return d - ipar<T>(I.dtau, I.dtau64) * s * (g - T(1));
+    return s == T(0) ? d : d - ipar<T>(I.dtau, I.dtau64) * s * (g - T(1));
 }
 
 template <typename T, int TX, int TY, int TZ>
 __global__ void __launch_bounds__(TX * TY * TZ) k_reinit(const Inst* __restrict__ inst,
-        const int* __restrict__ brick_inst, int nbricks, FieldsT<T> f, const T* __restrict__ din,
+        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ din,
         T* __restrict__ dout, unsigned* err) {
     for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const Node b = brick_node<TX, TY, TZ>(inst, brick_inst, blk);
+        const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
         if (!b.valid) continue;
         const Inst& I = inst[b.inst];
         const long long l = I.off + b.i + (long long)I.ni * (b.j + (long long)I.nj * b.k);
@@ -559,7 +559,7 @@ __device__ __forceinline__ long long warp_sum_ll(long long v) {
 
 template <typename T, int TX, int TY, int TZ>
 __global__ void __launch_bounds__(TX * TY * TZ) k_volume(const Inst* __restrict__ inst,
-        const int* __restrict__ brick_inst, int nbricks, FieldsT<T> f, const T* __restrict__ phi,
+        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phi,
         long long* __restrict__ partials) {
     constexpr int NT = TX * TY * TZ, NW = NT / 32;
     const T eps = T(2.220446049250313e-16);
@@ -568,7 +568,7 @@ __global__ void __launch_bounds__(TX * TY * TZ) k_volume(const Inst* __restrict_
     __shared__ int wcount[NW];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const Node b = brick_node<TX, TY, TZ>(inst, brick_inst, blk);
+        const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
         const Inst& I = inst[b.inst];
         const long long sj = I.ni, sk = (long long)I.ni * I.nj;
         long long Kq = 0, Sq = 0, Bq = 0;
@@ -725,150 +725,365 @@ __global__ void k_adj_face(Flat fl, int face, long long nplane, BC bc, int kind,
     lam[l] = T(0);
 }
 
-// Reverse of one RK stage: node j gathers from the interior nodes i whose
-// WENO stencils contain it (i = j + o e_m, |o| <= 2).
+// value and gradient of rec3 (one reciprocal)
 template <typename T>
-__global__ void k_adj_stage(Flat fl, FieldsT<T> f, const T* __restrict__ in, const T* __restrict__ lamP0,
-                            T* __restrict__ lam_in, T* __restrict__ lamPhin, T* __restrict__ lamW0,
-                            T* __restrict__ lamW1, T* __restrict__ lamW2, T c1, T c2, T c3, int last) {
-    const long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    Node nd;
-    if (!flat_node(fl, l, &nd)) return;
-    const Inst& I = fl.inst[nd.inst];
-    const int n3[3] = {I.ni, I.nj, I.nk};
-    const int c3d[3] = {nd.i, nd.j, nd.k};
-    const long long st[3] = {1, (long long)I.ni, (long long)I.ni * I.nj};
-    T* lamW[3] = {lamW0, lamW1, lamW2};
-    const T lp = lamP0[l];
-    T acc = T(0);
-    const bool jint = interior(I, nd.i, nd.j, nd.k);
-#pragma unroll
-    for (int m = 0; m < 3; ++m) {
-        const int cm = c3d[m], nm = n3[m];
-        const long long s = st[m];
-        // the other two coordinates must be interior for any node on this line to be interior
-        bool line_ok = true;
-#pragma unroll
-        for (int q = 0; q < 3; ++q)
-            if (q != m && (c3d[q] < 1 || c3d[q] > n3[q] - 2)) line_ok = false;
-        // values of `in` along the line at offsets -4..4 (zero outside)
-        T v[9];
-#pragma unroll
-        for (int q = -4; q <= 4; ++q) {
-            const int cq = cm + q;
-            v[q + 4] = (line_ok && cq >= 0 && cq < nm) ? __ldg(in + l + q * s) : T(0);
-        }
-        if (line_ok) {
-#pragma unroll
-            for (int o = -2; o <= 2; ++o) {
-                const int ci = cm + o;
-                if (ci < 1 || ci > nm - 2) continue;
-                const long long li = l + o * s;
-                const T w = __ldg(f.W[m] + li);
-                const T lpi = __ldg(lamP0 + li);
-                // stencil of node i (positions ci-2..ci+2); the forward zeroes
-                // the unused outer value on the forced faces
-                T sv[5] = {v[o + 2], v[o + 3], v[o + 4], v[o + 5], v[o + 6]};
-                if (ci <= 1) sv[0] = T(0);
-                if (ci >= nm - 2) sv[4] = T(0);
-                T g[5];
-                weno_diff_grad(sv, w, ci == 1, ci == nm - 2, g);
-                acc = vfma(lpi * w, g[2 - o], acc);    // j sits at offset -o in node i's stencil
-            }
-        }
-        if (jint) {
-            T sv[5] = {v[2], v[3], v[4], v[5], v[6]};
-            if (cm <= 1) sv[0] = T(0);
-            if (cm >= nm - 2) sv[4] = T(0);
-            const T w = __ldg(f.W[m] + l);
-            const T D = weno_diff(sv[0], sv[1], sv[2], sv[3], sv[4], w, cm == 1, cm == nm - 2);
-            lamW[m][l] -= c3 * lp * D;
-        }
-    }
-    T r = c2 * lp - c3 * acc;
-    if (last) {
-        r += lamPhin[l] + c1 * lp;
-        lamPhin[l] = T(0);
-    } else {
-        lamPhin[l] += c1 * lp;
-    }
-    lam_in[l] = r;
+__device__ __forceinline__ T rec3_vg(T fL, T fC, T fR, T* dL, T* dC, T* dR) {
+    const T eL = fL - fC, eR = fC - fR;
+    const T t0 = eR * eR + T(1.0e-6), t1 = eL * eL + T(1.0e-6);
+    const T a0 = T(2) * t1 * t1, a1 = t0 * t0;
+    const T r = vdiv(T(1), a0 + a1);
+    const T w0 = a0 * r;
+    const T g = T(0.5) * (fL + fR) - fC;
+    // d w0 / d t1 = 4 t1 a1 r^2, d w0 / d t0 = -2 t0 a0 r^2
+    const T q1 = T(4) * t1 * a1 * r * r * g, q0 = T(-2) * t0 * a0 * r * r * g;
+    *dL = T(-0.5) + T(0.5) * w0 + q1 * (T(2) * eL);
+    *dC = T(1.5) - w0 - q1 * (T(2) * eL) + q0 * (T(2) * eR);
+    *dR = T(0.5) * w0 - q0 * (T(2) * eR);
+    return vfma(w0, g, T(1.5) * fC - T(0.5) * fL);
 }
 
-// Reinitialisation adjoint, pass 1: per node i with s != 0, w = dtau s lam(i)
-// and the Godunov selections of the forward pass; A_m = w dG/dmen_m,
-// B_m = w dG/dmas_m (a physical face's single difference goes to B on the
-// low face, to A on the high face).
+// D = Phi+ - Phi- of a node (stencil s, orientation frozen by w) and the
+// gradient G = lp w dD/ds of lp w D, branch-free
 template <typename T>
-__global__ void k_adj_reinit_coef(Flat fl, FieldsT<T> f, const T* __restrict__ d, const T* __restrict__ lam,
-                                  T* __restrict__ coef) {
-    const long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    Node nd;
-    if (!flat_node(fl, l, &nd)) return;
-    const Inst& I = fl.inst[nd.inst];
-    const T s = __ldg(f.sgn + l);
-    T A[3] = {T(0), T(0), T(0)}, B[3] = {T(0), T(0), T(0)};
-    if (s != T(0)) {
-        T mas[3], men[3];
-        godunov_diffs(d, I, l, nd.i, nd.j, nd.k, mas, men);
-        T db[3], df[3], acc = T(0);
-        T M[3][3];
+__device__ __forceinline__ T stage_node_grad(const T (&s)[5], T w, T lp, bool lo, bool hi, T (&G)[5]) {
+    const bool up = w > T(0);
+    const bool P = up || hi, M = up && !lo;
+    T a, b, c, a2, b2, c2;
+    const T vp = rec3_vg(P ? s[1] : s[4], P ? s[2] : s[3], P ? s[3] : s[2], &a, &b, &c);
+    const T vm = rec3_vg(M ? s[0] : s[3], M ? s[1] : s[2], M ? s[2] : s[1], &a2, &b2, &c2);
+    const T k = lp * w;
+    G[0] = -k * (M ? a2 : T(0));
+    G[1] = k * ((P ? a : T(0)) - (M ? b2 : c2));
+    G[2] = k * ((P ? b : c) - (M ? c2 : b2));
+    G[3] = k * ((P ? c : b) - (M ? T(0) : a2));
+    G[4] = k * (P ? T(0) : a);
+    return vp - vm;
+}
+
+// Adjoint brick of block `blk` in adjoint map `map`: instance and origin.
+struct ABrick {
+    int inst, i0, j0, k0;
+};
+__device__ __forceinline__ ABrick adj_brick(const Brick* __restrict__ bmap, int map, int blk) {
+    const int4 bk = __ldg(reinterpret_cast<const int4*>(bmap) + blk);
+    const AdjShape sh = adj_shape(map);
+    ABrick b;
+    b.inst = bk.x;
+    b.i0 = bk.y * sh.ox;
+    b.j0 = bk.z * sh.oy;
+    b.k0 = bk.w * sh.oz;
+    return b;
+}
+
+// Stage adjoint, x part (adjoint map 0: bricks of 8 whole rows of one
+// plane, one warp per row) plus the pointwise terms.  The warp marches its
+// row in aligned chunks of 32 nodes: it evaluates G_x of chunk c + 1, then
+// writes chunk c, gathering the five contributions of each node by warp
+// shuffles from chunks c - 1, c, c + 1 held in registers.  Each warp starts
+// at its own chunk (rows hashed over the row length) and wraps around, so
+// that the warps of the GPU do not all stream the same columns at once.
+// Writes lam_in = c2 lamP0 - c3 acc_x (+ lamPhin + c1 lamP0 when last),
+// updates lamPhin and lamW_x.
+template <typename T>
+__global__ void __launch_bounds__(256) k_adj_stage_x(const Inst* __restrict__ inst, const Brick* __restrict__ bmap,
+        int nb, FieldsT<T> f, const T* __restrict__ in, const T* __restrict__ lamP0, T* __restrict__ lam_in,
+        T* __restrict__ lamPhin, T* __restrict__ lamW0, T c1, T c2, T c3, int last) {
+    const int lane = threadIdx.x & 31, row = threadIdx.x >> 5;
+    for (int blk = blockIdx.x; blk < nb; blk += gridDim.x) {
+        const ABrick ab = adj_brick(bmap, 0, blk);
+        const Inst& I = inst[ab.inst];
+        const int ni = I.ni, nj = I.nj, nk = I.nk;
+        const int j = ab.j0 + row, k = ab.k0;
+        if (j >= nj) continue;   // whole warp
+        const bool jk_int = j >= 1 && j <= nj - 2 && k >= 1 && k <= nk - 2;
+        const long long rowbase = I.off + (long long)ni * (j + (long long)nj * k);
+        const int nc = (ni + 31) >> 5;
+        // G_x of chunk c (zero outside the row and at non-interior nodes)
+        auto eval = [&](int c, T (&G)[5], T& D, T& lp) {
 #pragma unroll
-        for (int x = 0; x < 3; ++x) {
-            M[0][x] = __ldg(f.m[x] + l); M[1][x] = __ldg(f.m[3 + x] + l); M[2][x] = __ldg(f.m[6 + x] + l);
-            const T bb = M[0][x] * men[0] + M[1][x] * men[1] + M[2][x] * men[2];
-            const T ff = M[0][x] * mas[0] + M[1][x] * mas[1] + M[2][x] * mas[2];
-            const T P = s > T(0) ? vmax(bb, T(0)) : vmin(bb, T(0));
-            const T Q = s > T(0) ? vmin(ff, T(0)) : vmax(ff, T(0));
-            const bool takeP = P * P >= Q * Q;
-            acc += takeP ? P * P : Q * Q;
-            db[x] = takeP ? T(2) * P : T(0);     // d e_x / d b_x (the clip is inside P)
-            df[x] = takeP ? T(0) : T(2) * Q;
+            for (int p = 0; p < 5; ++p) G[p] = T(0);
+            D = lp = T(0);
+            const int ii = (c << 5) + lane;
+            if (c >= 0 && c < nc && ii < ni) {
+                const long long l = rowbase + ii;
+                lp = __ldg(lamP0 + l);
+                if (jk_int && ii >= 1 && ii <= ni - 2) {
+                    const T sv[5] = {ii >= 2 ? __ldg(in + l - 2) : T(0), __ldg(in + l - 1), __ldg(in + l),
+                                     __ldg(in + l + 1), ii <= ni - 3 ? __ldg(in + l + 2) : T(0)};
+                    D = stage_node_grad(sv, __ldg(f.W[0] + l), lp, ii == 1, ii == ni - 2, G);
+                }
+            }
+        };
+        // march chunks a .. b-1 (outputs), with chunk a-1 primed
+        auto segment = [&](int a, int b) {
+            T Gp[5], Gc[5], Gn[5], Dc, Dn, lpc, lpn;
+            eval(a - 1, Gc, Dc, lpc);
+#pragma unroll
+            for (int p = 0; p < 5; ++p) Gp[p] = T(0);
+            for (int c = a; c <= b; ++c) {
+                // read-modify-write values of the output chunk c - 1 first, so
+                // that their loads are in flight together with chunk c's
+                const int io = ((c - 1) << 5) + lane;
+                const bool wo = c > a && io < ni;
+                const long long lo = rowbase + io;
+                T phin_old = T(0), w_old = T(0);
+                if (wo) {
+                    phin_old = lamPhin[lo];
+                    w_old = lamW0[lo];
+                }
+                eval(c, Gn, Dn, lpn);
+                if (c > a) {
+                    // node lane + o of chunk c - 1 contributes component 2 - o;
+                    // across the chunk edges it lies in chunk c - 2 (Gp) or c (Gn)
+                    const unsigned FM = 0xffffffffu;
+                    const T m2c = __shfl_sync(FM, Gc[4], (lane - 2) & 31), m2p = __shfl_sync(FM, Gp[4], (lane - 2) & 31);
+                    const T m1c = __shfl_sync(FM, Gc[3], (lane - 1) & 31), m1p = __shfl_sync(FM, Gp[3], (lane - 1) & 31);
+                    const T p1c = __shfl_sync(FM, Gc[1], (lane + 1) & 31), p1n = __shfl_sync(FM, Gn[1], (lane + 1) & 31);
+                    const T p2c = __shfl_sync(FM, Gc[0], (lane + 2) & 31), p2n = __shfl_sync(FM, Gn[0], (lane + 2) & 31);
+                    const T acc = (lane >= 2 ? m2c : m2p) + (lane >= 1 ? m1c : m1p) + Gc[2] +
+                                  (lane <= 30 ? p1c : p1n) + (lane <= 29 ? p2c : p2n);
+                    if (wo) {
+                        lamW0[lo] = w_old - c3 * lpc * Dc;
+                        T r = c2 * lpc - c3 * acc;
+                        if (last) {
+                            r += phin_old + c1 * lpc;
+                            lamPhin[lo] = T(0);
+                        } else {
+                            lamPhin[lo] = phin_old + c1 * lpc;
+                        }
+                        lam_in[lo] = r;
+                    }
+                }
+#pragma unroll
+                for (int p = 0; p < 5; ++p) {
+                    Gp[p] = Gc[p];
+                    Gc[p] = Gn[p];
+                }
+                Dc = Dn;
+                lpc = lpn;
+            }
+        };
+        const int s0 = (int)(((unsigned)(j + 7 * k) * 2654435761u >> 16) % (unsigned)nc);
+        segment(s0, nc);
+        if (s0 > 0) segment(0, s0);
+    }
+}
+
+// Stage adjoint, y (AX = 1, adjoint map 1) or z (AX = 2, map 2) part: each
+// thread marches one line along AX over adj_shape(map) outputs, keeping
+// windows of five G, lamP0 and D values in registers; lam_in -= c3 acc,
+// lamW_AX -= c3 lamP0 D.
+template <typename T, int AX>
+__global__ void __launch_bounds__(256) k_adj_stage_m(const Inst* __restrict__ inst, const Brick* __restrict__ bmap,
+        int nb, FieldsT<T> f, const T* __restrict__ in, const T* __restrict__ lamP0, T* __restrict__ lam_in,
+        T* __restrict__ lamW, T c3) {
+    constexpr int MAP = AX;
+    const int tx = threadIdx.x & 31, tq = threadIdx.x >> 5;
+    for (int blk = blockIdx.x; blk < nb; blk += gridDim.x) {
+        const ABrick ab = adj_brick(bmap, MAP, blk);
+        const Inst& I = inst[ab.inst];
+        const int ni = I.ni, nj = I.nj, nk = I.nk;
+        const long long sj = ni, sk = (long long)ni * nj;
+        const int i = ab.i0 + tx;
+        // the other coordinate (k for AX = 1, j for AX = 2) and the march range
+        const int c2 = AX == 1 ? ab.k0 + tq : ab.j0 + tq;
+        const int n2 = AX == 1 ? nk : nj, nm = AX == 1 ? nj : nk;
+        const int m0 = AX == 1 ? ab.j0 : ab.k0;
+        const int m1 = min(m0 + (AX == 1 ? adj_shape(1).oy : adj_shape(2).oz), nm);
+        const bool col = i < ni && c2 < n2;
+        const bool line = col && i >= 1 && i <= ni - 2 && c2 >= 1 && c2 <= n2 - 2;
+        const long long st = AX == 1 ? sj : sk;
+        const long long base = I.off + i + (AX == 1 ? sk * c2 : sj * c2);
+        // windows over march positions q-4 .. q (index 0..4)
+        T g[5][5], lpw[5], dw[5];
+#pragma unroll
+        for (int a = 0; a < 5; ++a) {
+            lpw[a] = dw[a] = T(0);
+#pragma unroll
+            for (int p = 0; p < 5; ++p) g[a][p] = T(0);
         }
-        const T G = vsqrt(acc);
-        if (G > T(0)) {
-            const T wgt = ipar<T>(I.dtau, I.dtau64) * s * __ldg(lam + l) / (T(2) * G);
-            const int c3d[3] = {nd.i, nd.j, nd.k};
-            const int n3[3] = {I.ni, I.nj, I.nk};
+        for (int q = m0 - 2; q < m1 + 2; ++q) {
+            const int jo = q - 2;   // output position: window index 2 after the shift
+            const bool wo = col && jo >= m0 && jo < m1;
+            const long long lo = base + st * jo;
+            T lin_old = T(0), w_old = T(0);
+            if (wo) {
+                lin_old = lam_in[lo];
+                w_old = lamW[lo];
+            }
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                lpw[a] = lpw[a + 1];
+                dw[a] = dw[a + 1];
+#pragma unroll
+                for (int p = 0; p < 5; ++p) g[a][p] = g[a + 1][p];
+            }
+            T G[5] = {T(0), T(0), T(0), T(0), T(0)};
+            T D = T(0), lp = T(0);
+            if (col && q >= 0 && q < nm) {
+                const long long l = base + st * q;
+                lp = __ldg(lamP0 + l);
+                if (line && q >= 1 && q <= nm - 2) {
+                    const T sv[5] = {q >= 2 ? __ldg(in + l - 2 * st) : T(0), __ldg(in + l - st), __ldg(in + l),
+                                     __ldg(in + l + st), q <= nm - 3 ? __ldg(in + l + 2 * st) : T(0)};
+                    D = stage_node_grad(sv, __ldg(f.W[AX] + l), lp, q == 1, q == nm - 2, G);
+                }
+            }
+            lpw[4] = lp;
+            dw[4] = D;
+#pragma unroll
+            for (int p = 0; p < 5; ++p) g[4][p] = G[p];
+            if (wo) {
+                T acc = T(0);
+#pragma unroll
+                for (int o = -2; o <= 2; ++o) acc += g[2 + o][2 - o];
+                lam_in[lo] = lin_old - c3 * acc;
+                lamW[lo] = w_old - c3 * lpw[2] * dw[2];
+            }
+        }
+    }
+}
+
+// Reinitialisation adjoint coefficients of node (i, j, k) from its inputs:
+// with w = dtau s lam / (2 G) and the Godunov selections of the forward
+// pass, A_m = w dG^2/dmen_m, B_m = w dG^2/dmas_m (a physical face's single
+// difference goes to B on the low face, to A on the high face).
+template <typename T>
+struct CoefIn {
+    T d[7];     // d at the node, -x, +x, -y, +y, -z, +z (one-sided on faces)
+    T s, lam;
+    T M[9];
+};
+
+template <typename T>
+__device__ __forceinline__ void coef_load(const FieldsT<T>& f, const T* __restrict__ d, const T* __restrict__ lam,
+                                          const Inst& I, int i, int j, int k, bool ok, CoefIn<T>& c) {
+    if (!ok) {
+        c.s = T(0);
+        c.lam = T(0);
+        return;
+    }
+    const long long sj = I.ni, sk = (long long)I.ni * I.nj;
+    const long long l = I.off + i + sj * j + sk * k;
+    c.s = __ldg(f.sgn + l);
+    c.lam = __ldg(lam + l);
+    c.d[0] = __ldg(d + l);
+    c.d[1] = i > 0 ? __ldg(d + l - 1) : c.d[0];
+    c.d[2] = i < I.ni - 1 ? __ldg(d + l + 1) : c.d[0];
+    c.d[3] = j > 0 ? __ldg(d + l - sj) : c.d[0];
+    c.d[4] = j < I.nj - 1 ? __ldg(d + l + sj) : c.d[0];
+    c.d[5] = k > 0 ? __ldg(d + l - sk) : c.d[0];
+    c.d[6] = k < I.nk - 1 ? __ldg(d + l + sk) : c.d[0];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) c.M[q] = __ldg(f.m[q] + l);
+}
+
+template <typename T>
+__device__ __forceinline__ void coef_eval(const CoefIn<T>& c, T dtau, int i, int j, int k, int ni, int nj, int nk,
+                                          T (&A)[3], T (&B)[3]) {
+#pragma unroll
+    for (int m = 0; m < 3; ++m) A[m] = B[m] = T(0);
+    if (c.s == T(0)) return;
+    const int c3d[3] = {i, j, k};
+    const int n3[3] = {ni, nj, nk};
+    T mas[3], men[3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        const T fwd = c.d[2 + 2 * m] - c.d[0], bwd = c.d[0] - c.d[1 + 2 * m];
+        mas[m] = c3d[m] < n3[m] - 1 ? fwd : bwd;
+        men[m] = c3d[m] > 0 ? bwd : fwd;
+    }
+    T db[3], df[3], acc = T(0);
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+        const T bb = c.M[x] * men[0] + c.M[3 + x] * men[1] + c.M[6 + x] * men[2];
+        const T ff = c.M[x] * mas[0] + c.M[3 + x] * mas[1] + c.M[6 + x] * mas[2];
+        const T P = c.s > T(0) ? vmax(bb, T(0)) : vmin(bb, T(0));
+        const T Q = c.s > T(0) ? vmin(ff, T(0)) : vmax(ff, T(0));
+        const bool takeP = P * P >= Q * Q;
+        acc += takeP ? P * P : Q * Q;
+        db[x] = takeP ? T(2) * P : T(0);
+        df[x] = takeP ? T(0) : T(2) * Q;
+    }
+    if (!(acc > T(0))) return;
+    const T wgt = T(0.5) * dtau * c.s * c.lam * vrsqrt(acc);   // dtau s lam / (2 G)
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        const T gmen = c.M[3 * m] * db[0] + c.M[3 * m + 1] * db[1] + c.M[3 * m + 2] * db[2];
+        const T gmas = c.M[3 * m] * df[0] + c.M[3 * m + 1] * df[1] + c.M[3 * m + 2] * df[2];
+        if (c3d[m] == 0) B[m] = wgt * (gmen + gmas);
+        else if (c3d[m] == n3[m] - 1) A[m] = wgt * (gmen + gmas);
+        else {
+            A[m] = wgt * gmen;
+            B[m] = wgt * gmas;
+        }
+    }
+}
+
+// Reverse of one reinitialisation pseudo-step d' = d - dtau s (G(d) - 1):
+//   lam_out(j) = lam(j) - sum_m [A_m(j) - B_m(j) - A_m(j+e_m) + B_m(j-e_m)]
+// (adjoint map 3).  A block of 32 x kReinRY threads covers nodes i0-1 ..
+// i0+30, j0-1 .. j0+kReinRY-2 and writes the inner 30 x (kReinRY-2); it
+// marches in k: iteration k loads the inputs of plane k+1 (prefetch),
+// evaluates the coefficients of plane k and writes plane k-1.  x neighbours
+// come by warp shuffles, y neighbours through shared memory (three plane
+// buffers, one barrier per plane), z neighbours stay in registers.
+template <typename T>
+__global__ void __launch_bounds__(32 * kReinRY) k_adj_reinit(const Inst* __restrict__ inst,
+        const Brick* __restrict__ bmap, int nb, FieldsT<T> f, const T* __restrict__ d, const T* __restrict__ lam,
+        T* __restrict__ lam_out) {
+    constexpr int RY = kReinRY;
+    __shared__ T sA1[3][RY][32], sB1[3][RY][32];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int blk = blockIdx.x; blk < nb; blk += gridDim.x) {
+        const ABrick ab = adj_brick(bmap, 3, blk);
+        const Inst& I = inst[ab.inst];
+        const int ni = I.ni, nj = I.nj, nk = I.nk;
+        const int i = ab.i0 - 1 + tx, j = ab.j0 - 1 + ty;
+        const int k0 = ab.k0, k1 = min(k0 + adj_shape(3).oz, nk);
+        const bool node = i >= 0 && i < ni && j >= 0 && j < nj;
+        const bool out = node && tx >= 1 && tx <= 30 && ty >= 1 && ty <= RY - 2;
+        const T dtau = ipar<T>(I.dtau, I.dtau64);
+        CoefIn<T> nxt;
+        coef_load(f, d, lam, I, i, j, k0 - 1, node && k0 >= 1, nxt);
+        T Ap[3] = {T(0), T(0), T(0)}, Bp[3] = {T(0), T(0), T(0)}, Bz2 = T(0), lamp = T(0);
+#pragma unroll 2
+        for (int k = k0 - 1; k <= k1; ++k) {
+            const CoefIn<T> cur = nxt;
+            coef_load(f, d, lam, I, i, j, k + 1, node && k + 1 >= 0 && k + 1 < nk && k + 1 <= k1, nxt);
+            T A[3], B[3];
+            coef_eval(cur, dtau, i, j, k, ni, nj, nk, A, B);
+            const int b = (k + 3) % 3;
+            sA1[b][ty][tx] = A[1];
+            sB1[b][ty][tx] = B[1];
+            // x neighbours of plane k-1
+            const T ax = __shfl_down_sync(0xffffffffu, Ap[0], 1);
+            const T bx = __shfl_up_sync(0xffffffffu, Bp[0], 1);
+            __syncthreads();
+            const int ko = k - 1;
+            if (out && ko >= k0 && ko < k1) {
+                const int q = (ko + 3) % 3;
+                T t0 = Ap[0] - Bp[0];
+                if (i < ni - 1) t0 -= ax;
+                if (i > 0) t0 += bx;
+                T t1 = Ap[1] - Bp[1];
+                if (j < nj - 1) t1 -= sA1[q][ty + 1][tx];
+                if (j > 0) t1 += sB1[q][ty - 1][tx];
+                T t2 = Ap[2] - Bp[2];
+                if (ko < nk - 1) t2 -= A[2];
+                if (ko > 0) t2 += Bz2;
+                const long long l = I.off + i + (long long)ni * (j + (long long)nj * ko);
+                lam_out[l] = lamp - t0 - t1 - t2;
+            }
+            Bz2 = Bp[2];
 #pragma unroll
             for (int m = 0; m < 3; ++m) {
-                const T gmen = M[m][0] * db[0] + M[m][1] * db[1] + M[m][2] * db[2];
-                const T gmas = M[m][0] * df[0] + M[m][1] * df[1] + M[m][2] * df[2];
-                if (c3d[m] == 0) { A[m] = T(0); B[m] = wgt * (gmen + gmas); }
-                else if (c3d[m] == n3[m] - 1) { A[m] = wgt * (gmen + gmas); B[m] = T(0); }
-                else { A[m] = wgt * gmen; B[m] = wgt * gmas; }
+                Ap[m] = A[m];
+                Bp[m] = B[m];
             }
+            lamp = cur.lam;
         }
     }
-#pragma unroll
-    for (int m = 0; m < 3; ++m) {
-        coef[(2 * m) * fl.n + l] = A[m];
-        coef[(2 * m + 1) * fl.n + l] = B[m];
-    }
-}
-
-// pass 2: lam_out(j) = lam(j) - sum_m [A_m(j) - B_m(j) - A_m(j+e_m) + B_m(j-e_m)]
-template <typename T>
-__global__ void k_adj_reinit_apply(Flat fl, const T* __restrict__ lam, const T* __restrict__ coef,
-                                   T* __restrict__ lam_out) {
-    const long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    Node nd;
-    if (!flat_node(fl, l, &nd)) return;
-    const Inst& I = fl.inst[nd.inst];
-    const int c3d[3] = {nd.i, nd.j, nd.k};
-    const int n3[3] = {I.ni, I.nj, I.nk};
-    const long long st[3] = {1, (long long)I.ni, (long long)I.ni * I.nj};
-    T r = __ldg(lam + l);
-#pragma unroll
-    for (int m = 0; m < 3; ++m) {
-        const T* A = coef + (2 * m) * fl.n;
-        const T* B = coef + (2 * m + 1) * fl.n;
-        T t = __ldg(A + l) - __ldg(B + l);
-        if (c3d[m] < n3[m] - 1) t -= __ldg(A + l + st[m]);
-        if (c3d[m] > 0) t += __ldg(B + l - st[m]);
-        r -= t;
-    }
-    lam_out[l] = r;
 }
 
 template <typename T>
@@ -912,25 +1127,25 @@ void dispatch(int shape, A... a) {
     };
 
 LSM_BATCH_RUNNER(RunContra, k_contra,
-                 (int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, cudaStream_t s),
+                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, cudaStream_t s),
                  (inst, bi, nb, f))
 LSM_BATCH_RUNNER(RunStage, k_stage,
-                 (int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, const T* pn, const T* p1, T* out,
+                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* pn, const T* p1, T* out,
                   double c1, double c2, double c3, cudaStream_t s),
                  (inst, bi, nb, f, pn, p1, out, T(c1), T(c2), T(c3)))
 LSM_BATCH_RUNNER(RunBcFull, k_bc_full,
-                 (int grid, const Inst* inst, const int* bi, int nb, BC bc, const T* src, T* dst, unsigned* err,
+                 (int grid, const Inst* inst, const Brick* bi, int nb, BC bc, const T* src, T* dst, unsigned* err,
                   cudaStream_t s),
                  (inst, bi, nb, bc, src, dst, err))
 LSM_BATCH_RUNNER(RunSign, k_sign,
-                 (int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, const T* p0, cudaStream_t s),
+                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* p0, cudaStream_t s),
                  (inst, bi, nb, f, p0))
 LSM_BATCH_RUNNER(RunReinit, k_reinit,
-                 (int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, const T* din, T* dout,
+                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* din, T* dout,
                   unsigned* err, cudaStream_t s),
                  (inst, bi, nb, f, din, dout, err))
 LSM_BATCH_RUNNER(RunVolume, k_volume,
-                 (int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, const T* phi, long long* part,
+                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi, long long* part,
                   cudaStream_t s),
                  (inst, bi, nb, f, phi, part))
 
@@ -952,11 +1167,11 @@ inline unsigned flat_blocks(long long n) { return (unsigned)((n + 255) / 256); }
 
 // ------------------------------------------------------------ launchers
 template <typename T>
-void contra(int shape, int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, cudaStream_t s) {
+void contra(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, cudaStream_t s) {
     dispatch<RunContra, T>(shape, grid, inst, bi, nb, f, s);
 }
 template <typename T>
-void stage(int shape, int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, const T* phin, const T* phi1,
+void stage(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phin, const T* phi1,
            T* out, double c1, double c2, double c3, cudaStream_t s) {
     dispatch<RunStage, T>(shape, grid, inst, bi, nb, f, phin, phi1, out, c1, c2, c3, s);
 }
@@ -967,16 +1182,16 @@ void bc_stage(const Inst* inst, int ninst, long long nface, BC bc, const T* phin
     k_bc_stage<T><<<flat_blocks(nface), 256, 0, s>>>(inst, ninst, nface, bc, phin, phi1, out, T(c1), T(c2));
 }
 template <typename T>
-void bc_full(int shape, int grid, const Inst* inst, const int* bi, int nb, BC bc, const T* src, T* dst, unsigned* err,
+void bc_full(int shape, int grid, const Inst* inst, const Brick* bi, int nb, BC bc, const T* src, T* dst, unsigned* err,
              cudaStream_t s) {
     dispatch<RunBcFull, T>(shape, grid, inst, bi, nb, bc, src, dst, err, s);
 }
 template <typename T>
-void sign(int shape, int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, const T* phi0, cudaStream_t s) {
+void sign(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi0, cudaStream_t s) {
     dispatch<RunSign, T>(shape, grid, inst, bi, nb, f, phi0, s);
 }
 template <typename T>
-void reinit(int shape, int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, const T* din, T* dout,
+void reinit(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* din, T* dout,
             unsigned* err, cudaStream_t s) {
     dispatch<RunReinit, T>(shape, grid, inst, bi, nb, f, din, dout, err, s);
 }
@@ -987,11 +1202,11 @@ void bc_reinit(const Inst* inst, int ninst, long long nface, FieldsT<T> f, BC bc
     k_bc_reinit<T><<<flat_blocks(nface), 256, 0, s>>>(inst, ninst, nface, bc, f, din, dout);
 }
 template <typename T>
-void volume(int shape, int grid, const Inst* inst, const int* bi, int nb, FieldsT<T> f, const T* phi,
+void volume(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi,
             long long* partials, cudaStream_t s) {
     dispatch<RunVolume, T>(shape, grid, inst, bi, nb, f, phi, partials, s);
 }
-void volume_final(const Inst* inst, int ninst, const int* bi, int nb, const long long* partials, double* vols,
+void volume_final(const Inst* inst, int ninst, const Brick* bi, int nb, const long long* partials, double* vols,
                   cudaStream_t s) {
     (void)bi;
     ProfScope ps_("k_volume_final", s);
@@ -1017,20 +1232,37 @@ void adj_face(const Flat& fl, int face, long long nplane, BC bc, int kind, const
     k_adj_face<T><<<flat_blocks(nplane), 256, 0, s>>>(fl, face, nplane, bc, kind, phin, in, out, T(c1), T(c2), lam);
 }
 template <typename T>
-void adj_stage(const Flat& fl, FieldsT<T> f, const T* in, const T* lamP0, T* lam_in, T* lamPhin, T* lamW0, T* lamW1,
-               T* lamW2, double c1, double c2, double c3, bool last, cudaStream_t s) {
-    ProfScope ps_("k_adj_stage", s);
-    k_adj_stage<T><<<flat_blocks(fl.n), 256, 0, s>>>(fl, f, in, lamP0, lam_in, lamPhin, lamW0, lamW1, lamW2, T(c1), T(c2), T(c3),
-                                                     last ? 1 : 0);
+void adj_stage(const int* grid, const Inst* inst, const Brick* const* bmap, const int* nb, FieldsT<T> f, const T* in,
+               const T* lamP0, T* lam_in, T* lamPhin, T* lamW0, T* lamW1, T* lamW2, double c1, double c2, double c3,
+               bool last, cudaStream_t s) {
+    {
+        ProfScope ps_("k_adj_stage_x", s);
+        k_adj_stage_x<T><<<grid[0], 256, 0, s>>>(inst, bmap[0], nb[0], f, in, lamP0, lam_in, lamPhin, lamW0, T(c1),
+                                                 T(c2), T(c3), last ? 1 : 0);
+    }
+    {
+        ProfScope ps_("k_adj_stage_y", s);
+        k_adj_stage_m<T, 1><<<grid[1], 256, 0, s>>>(inst, bmap[1], nb[1], f, in, lamP0, lam_in, lamW1, T(c3));
+    }
+    ProfScope ps_("k_adj_stage_z", s);
+    k_adj_stage_m<T, 2><<<grid[2], 256, 0, s>>>(inst, bmap[2], nb[2], f, in, lamP0, lam_in, lamW2, T(c3));
 }
 template <typename T>
-void adj_reinit(const Flat& fl, FieldsT<T> f, const T* d, const T* lam, T* coef, T* lam_out, cudaStream_t s) {
-    {
-        ProfScope ps_("k_adj_reinit_coef", s);
-        k_adj_reinit_coef<T><<<flat_blocks(fl.n), 256, 0, s>>>(fl, f, d, lam, coef);
+void adj_reinit(int grid, const Inst* inst, const Brick* bmap, int nb, FieldsT<T> f, const T* d, const T* lam,
+                T* lam_out, cudaStream_t s) {
+    ProfScope ps_("k_adj_reinit", s);
+    k_adj_reinit<T><<<grid, 32 * kReinRY, 0, s>>>(inst, bmap, nb, f, d, lam, lam_out);
+}
+template <typename T>
+int adj_blocks_per_sm(int map) {
+    int n = 0;
+    switch (map) {
+    case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adj_stage_x<T>, 256, 0); break;
+    case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adj_stage_m<T, 1>, 256, 0); break;
+    case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adj_stage_m<T, 2>, 256, 0); break;
+    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adj_reinit<T>, 32 * kReinRY, 0); break;
     }
-    ProfScope ps_("k_adj_reinit_apply", s);
-    k_adj_reinit_apply<T><<<flat_blocks(fl.n), 256, 0, s>>>(fl, lam, coef, lam_out);
+    return n;
 }
 template <typename T>
 void adj_contra(const Flat& fl, FieldsT<T> f, const T* w0, const T* w1, const T* w2, T* u0, T* u1, T* u2,
@@ -1040,21 +1272,23 @@ void adj_contra(const Flat& fl, FieldsT<T> f, const T* w0, const T* w1, const T*
 }
 
 #define LSM_BATCH_INSTANTIATE(T)                                                                                      \
-    template void contra<T>(int, int, const Inst*, const int*, int, FieldsT<T>, cudaStream_t);                       \
-    template void stage<T>(int, int, const Inst*, const int*, int, FieldsT<T>, const T*, const T*, T*, double,       \
+    template void contra<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, cudaStream_t);                       \
+    template void stage<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, const T*, T*, double,       \
                            double, double, cudaStream_t);                                                                     \
     template void bc_stage<T>(const Inst*, int, long long, BC, const T*, const T*, T*, double, double, cudaStream_t);   \
-    template void bc_full<T>(int, int, const Inst*, const int*, int, BC, const T*, T*, unsigned*, cudaStream_t);      \
-    template void sign<T>(int, int, const Inst*, const int*, int, FieldsT<T>, const T*, cudaStream_t);               \
-    template void reinit<T>(int, int, const Inst*, const int*, int, FieldsT<T>, const T*, T*, unsigned*,             \
+    template void bc_full<T>(int, int, const Inst*, const Brick*, int, BC, const T*, T*, unsigned*, cudaStream_t);      \
+    template void sign<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, cudaStream_t);               \
+    template void reinit<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, unsigned*,             \
                             cudaStream_t);                                                                            \
     template void bc_reinit<T>(const Inst*, int, long long, FieldsT<T>, BC, const T*, T*, cudaStream_t);              \
-    template void volume<T>(int, int, const Inst*, const int*, int, FieldsT<T>, const T*, long long*, cudaStream_t);  \
+    template void volume<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, long long*, cudaStream_t);  \
     template void adj_face<T>(const Flat&, int, long long, BC, int, const T*, const T*, const T*, double, double, T*, \
                               cudaStream_t);                                                                          \
-    template void adj_stage<T>(const Flat&, FieldsT<T>, const T*, const T*, T*, T*, T*, T*, T*, double, double, double, \
-                               bool, cudaStream_t);                                                                   \
-    template void adj_reinit<T>(const Flat&, FieldsT<T>, const T*, const T*, T*, T*, cudaStream_t);                   \
+    template void adj_stage<T>(const int*, const Inst*, const Brick* const*, const int*, FieldsT<T>, const T*,      \
+                               const T*, T*, T*, T*, T*, T*, double, double, double, bool, cudaStream_t);      \
+    template void adj_reinit<T>(int, const Inst*, const Brick*, int, FieldsT<T>, const T*, const T*, T*,            \
+                                cudaStream_t);                                                                \
+    template int adj_blocks_per_sm<T>(int);                                                                     \
     template void adj_contra<T>(const Flat&, FieldsT<T>, const T*, const T*, const T*, T*, T*, T*, cudaStream_t);
 
 LSM_BATCH_INSTANTIATE(float)

@@ -27,6 +27,7 @@ struct Inst {
     long long face0;   // first boundary-face node of the instance (forward bc kernels)
     long long fpre[3]; // first node of the instance's i-, j-, k-face planes (adjoint face kernels)
     double dt64, dtau64, eps64;  // the same three parameters for the FP64 kernels
+    int am[4][3];                // adjoint brick maps (adj_shape): first brick, bricks per row, per plane
 };
 
 // Packed fields of one batch (device pointers), scalar type T.
@@ -56,6 +57,11 @@ struct BC {
     float BigPhi;
 };
 
+// One brick of a brick table: its instance and brick coordinates.
+struct __align__(16) Brick {
+    int inst, bx, by, bz;
+};
+
 // tile shapes the autotuner chooses from (threads per brick = TX*TY*TZ)
 constexpr int kNumShapes = 5;
 struct Shape { int tx, ty, tz; };
@@ -64,22 +70,22 @@ constexpr Shape kShapes[kNumShapes] = {{32, 4, 2}, {32, 8, 1}, {64, 4, 1}, {32, 
 // ------------------------------------------------------------ forward
 // (shape = index into kShapes; FP64 instantiations exist for shape 0 only)
 template <typename T>
-void contra(int shape, int grid, const Inst* inst, const int* brick_inst, int nbricks, FieldsT<T> f,
+void contra(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f,
             cudaStream_t s);
 template <typename T>
-void stage(int shape, int grid, const Inst* inst, const int* brick_inst, int nbricks, FieldsT<T> f, const T* phin,
+void stage(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f, const T* phin,
            const T* phi1, T* out, double c1, double c2, double c3, cudaStream_t s);
 template <typename T>
 void bc_stage(const Inst* inst, int ninst, long long nface, BC bc, const T* phin, const T* phi1, T* out, double c1,
               double c2, cudaStream_t s);
 template <typename T>
-void bc_full(int shape, int grid, const Inst* inst, const int* brick_inst, int nbricks, BC bc, const T* src, T* dst,
+void bc_full(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, BC bc, const T* src, T* dst,
              unsigned* err, cudaStream_t s);
 template <typename T>
-void sign(int shape, int grid, const Inst* inst, const int* brick_inst, int nbricks, FieldsT<T> f, const T* phi0,
+void sign(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f, const T* phi0,
           cudaStream_t s);
 template <typename T>
-void reinit(int shape, int grid, const Inst* inst, const int* brick_inst, int nbricks, FieldsT<T> f, const T* din,
+void reinit(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f, const T* din,
             T* dout, unsigned* err, cudaStream_t s);
 // bcond_lsm on the output of the last reinitialisation pseudo-step (dout):
 // boundary values are recomputed pointwise from that step's input din.
@@ -87,9 +93,9 @@ template <typename T>
 void bc_reinit(const Inst* inst, int ninst, long long nface, FieldsT<T> f, BC bc, const T* din, T* dout,
                cudaStream_t s);
 template <typename T>
-void volume(int shape, int grid, const Inst* inst, const int* brick_inst, int nbricks, FieldsT<T> f, const T* phi,
+void volume(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f, const T* phi,
             long long* partials, cudaStream_t s);
-void volume_final(const Inst* inst, int ninst, const int* brick_inst, int nbricks, const long long* partials,
+void volume_final(const Inst* inst, int ninst, const Brick* bricks, int nbricks, const long long* partials,
                   double* vols, cudaStream_t s);
 // fixed-point hexahedron volume of every cell of one instance (static
 // geometry); x, y, z and cellfix are the packed base arrays, `off` the
@@ -99,8 +105,19 @@ void cell_hex(long long off, int ni, int nj, int nk, const double* x, const doub
 int max_blocks_per_sm(int shape, int kernel);
 
 // ------------------------------------------------------------ adjoint
-// All adjoint kernels walk the packed nodes with one thread per node
-// (instance found by binary search over the node offsets `offs`).
+// The stencil adjoints run on their own brick maps (output nodes per brick
+// ox x oy x oz, adj_shape): 0 stage x part (8 whole rows, one warp marching
+// each), 1 stage y march, 2 stage z march, 3 reinitialisation (overlapped
+// 32 x kReinRY tile marching in k).
+// The face and velocity adjoints walk the packed nodes with one thread per
+// node (instance found by binary search over the node offsets `offs`).
+struct AdjShape { int ox, oy, oz; };
+constexpr int kReinRY = 12;
+// (map 0: ox = 0 means a brick spans whole rows)
+__host__ __device__ constexpr AdjShape adj_shape(int map) {
+    return map == 0 ? AdjShape{0, 8, 1}
+                    : map == 1 ? AdjShape{32, 32, 8} : map == 2 ? AdjShape{32, 8, 32} : AdjShape{30, kReinRY - 2, 32};
+}
 struct Flat {
     const Inst* inst;
     const long long* offs;  // ninst + 1 node offsets
@@ -115,18 +132,23 @@ struct Flat {
 template <typename T>
 void adj_face(const Flat& fl, int face, long long nface_nodes, BC bc, int kind, const T* phin, const T* in,
               const T* out, double c1, double c2, T* lam, cudaStream_t s);
-// Reverse of one RK stage (stencil part gathered per node).  lamP0: adjoint
-// of the stage's pre-BC field; writes lam_in = c2 lamP0 - c3 (dR/din)^T lamP0
+// Reverse of one RK stage in three passes (x on adjoint map 0 by warp
+// shuffles, y and z marches on maps 1 and 2).  lamP0: adjoint of the
+// stage's pre-BC field; writes lam_in = c2 lamP0 - c3 (dR/din)^T lamP0
 // (+ lamPhin + c1 lamP0 when last, which also clears lamPhin), otherwise
 // accumulates lamPhin += c1 lamP0; and lamW_m -= c3 lamP0 D_m.
 template <typename T>
-void adj_stage(const Flat& fl, FieldsT<T> f, const T* in, const T* lamP0, T* lam_in, T* lamPhin, T* lamW0,
-               T* lamW1, T* lamW2, double c1, double c2, double c3, bool last, cudaStream_t s);
-// Reverse of one reinitialisation pseudo-step d' = d - dtau s (G(d) - 1):
-// coefficients (A_m, B_m) per node, then the gather lam_out = lam - sum(...).
+void adj_stage(const int* grid, const Inst* inst, const Brick* const* bmap, const int* nb, FieldsT<T> f, const T* in,
+               const T* lamP0, T* lam_in, T* lamPhin, T* lamW0, T* lamW1, T* lamW2, double c1, double c2, double c3,
+               bool last, cudaStream_t s);
+// Reverse of one reinitialisation pseudo-step d' = d - dtau s (G(d) - 1)
+// from its input d: lam_out = (dd'/dd)^T lam (adjoint map 3).
 template <typename T>
-void adj_reinit(const Flat& fl, FieldsT<T> f, const T* d, const T* lam, T* coef /*6*n*/, T* lam_out,
-                cudaStream_t s);
+void adj_reinit(int grid, const Inst* inst, const Brick* bmap, int nb, FieldsT<T> f, const T* d, const T* lam,
+                T* lam_out, cudaStream_t s);
+// resident blocks per SM of the kernel of adjoint map `map`
+template <typename T>
+int adj_blocks_per_sm(int map);
 // lam_u_c += sum_m M[m][c] dt lamW_m  (the W = dt M u chain rule)
 template <typename T>
 void adj_contra(const Flat& fl, FieldsT<T> f, const T* lamW0, const T* lamW1, const T* lamW2, T* lu0, T* lu1,

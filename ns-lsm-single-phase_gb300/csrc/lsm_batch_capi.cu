@@ -35,15 +35,24 @@ struct lsm_batch {
     long long N = 0, nface = 0, max_inst_nodes = 0, nplane[3] = {0, 0, 0};
     FieldsT<float> f32{};
     FieldsT<double> f64{};
+    // Per-node arrays live in arenas with a stride between arrays that is a
+    // 4 KiB multiple plus 2304 B, so that the same node of different arrays
+    // does not fall on the same DRAM channel (power-of-two node counts would
+    // otherwise put every array at a multiple of a large power of two).
+    void* field_arena = nullptr; // bufs and comps
+    size_t ld = 0;               // elements between consecutive arrays (batch precision)
+    size_t ld8 = 0;              // the same for 8-byte arrays
     void* bufs[6] = {};          // phi, stage0, stage1, d0, d1, sgn
     void* comps[15] = {};        // W[3], m[9], u[3]
-    double* xyz = nullptr;       // 3*N FP64 coordinates
+    double* xyz = nullptr;       // FP64 coordinates x, y, z (stride ld8); cellfix follows
     long long* cellfix = nullptr;  // N fixed-point cell hexahedron volumes
     double* staging = nullptr;   // FP64 scratch for conversions (4 * max instance nodes)
     Inst* d_inst = nullptr;
     long long* d_offs = nullptr;
-    int* d_brick = nullptr;
+    lsm::batch::Brick* d_brick = nullptr;
     int nbricks = 0;
+    lsm::batch::Brick* d_amap[4] = {};  // brick tables of the adjoint stencil kernels (lsm::batch::adj_shape)
+    int namap[4] = {0, 0, 0, 0}, agrid[4] = {1, 1, 1, 1};
     long long* d_part = nullptr;
     size_t part_cap = 0;
     double* d_vols = nullptr;
@@ -107,6 +116,12 @@ __global__ void k_zero(long long n, T* __restrict__ a) {
 
 inline unsigned cblocks(long long n) { return (unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 8)); }
 
+// bytes between consecutive per-node arrays of n elements of esz bytes
+size_t array_stride(long long n, size_t esz) {
+    const size_t raw = (size_t)n * esz;
+    return (raw + 4095) / 4096 * 4096 + 2304;
+}
+
 bool on_device(const void* p) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
@@ -143,7 +158,14 @@ int build_bricks(lsm_batch* b, int shape) {
     if (b->prec) shape = 0;     // FP64 kernels exist for tile shape 0 only
     const auto sh = lsm::batch::kShapes[shape];
     std::vector<Inst> hi(b->ninst);
-    std::vector<int> brick;
+    using lsm::batch::Brick;
+    std::vector<Brick> brick, amap[4];
+    // bricks in x-fastest order, each with its instance and coordinates
+    auto add = [](std::vector<Brick>& v, int q, int bx, int by, int bz) {
+        for (int z = 0; z < bz; ++z)
+            for (int y = 0; y < by; ++y)
+                for (int x = 0; x < bx; ++x) v.push_back(Brick{q, x, y, z});
+    };
     long long face = 0, pre[3] = {0, 0, 0};
     for (int q = 0; q < b->ninst; ++q) {
         const auto& I = b->inst[q];
@@ -166,10 +188,19 @@ int build_bricks(lsm_batch* b, int shape) {
         d.face0 = face;
         face += 2LL * ((long long)I.nj * I.nk + (long long)I.ni * I.nk + (long long)I.ni * I.nj);
         for (int a = 0; a < 3; ++a) d.fpre[a] = pre[a];
+        for (int m = 0; m < 4; ++m) {
+            const auto a = lsm::batch::adj_shape(m);
+            const int bx = a.ox > 0 ? (I.ni + a.ox - 1) / a.ox : 1;
+            const int by = (I.nj + a.oy - 1) / a.oy, bz = (I.nk + a.oz - 1) / a.oz;
+            d.am[m][0] = (int)amap[m].size();
+            d.am[m][1] = bx;
+            d.am[m][2] = by;
+            add(amap[m], q, bx, by, bz);
+        }
         pre[0] += (long long)I.nj * I.nk;
         pre[1] += (long long)I.ni * I.nk;
         pre[2] += (long long)I.ni * I.nj;
-        brick.insert(brick.end(), (size_t)d.nbx * d.nby * nbz, q);
+        add(brick, q, d.nbx, d.nby, nbz);
     }
     b->nface = face;
     for (int a = 0; a < 3; ++a) b->nplane[a] = pre[a];
@@ -179,8 +210,18 @@ int build_bricks(lsm_batch* b, int shape) {
         cudaFree(b->d_brick);
         b->d_brick = nullptr;
     }
-    BCU(b, cudaMalloc(&b->d_brick, sizeof(int) * brick.size()));
-    BCU(b, cudaMemcpyAsync(b->d_brick, brick.data(), sizeof(int) * brick.size(), cudaMemcpyHostToDevice, b->stream));
+    for (int m = 0; m < 4; ++m) {
+        if (b->d_amap[m]) {
+            cudaFree(b->d_amap[m]);
+            b->d_amap[m] = nullptr;
+        }
+        b->namap[m] = (int)amap[m].size();
+        BCU(b, cudaMalloc(&b->d_amap[m], sizeof(Brick) * amap[m].size()));
+        BCU(b, cudaMemcpyAsync(b->d_amap[m], amap[m].data(), sizeof(Brick) * amap[m].size(), cudaMemcpyHostToDevice,
+                               b->stream));
+    }
+    BCU(b, cudaMalloc(&b->d_brick, sizeof(Brick) * brick.size()));
+    BCU(b, cudaMemcpyAsync(b->d_brick, brick.data(), sizeof(Brick) * brick.size(), cudaMemcpyHostToDevice, b->stream));
     BCU(b, cudaMemcpyAsync(b->d_inst, hi.data(), sizeof(Inst) * hi.size(), cudaMemcpyHostToDevice, b->stream));
     const size_t need = 3 * (size_t)b->nbricks;
     if (need > b->part_cap) {
@@ -196,6 +237,11 @@ int build_bricks(lsm_batch* b, int shape) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
     const int per = std::max(1, lsm::batch::max_blocks_per_sm(shape, 0));
     b->grid = std::max(1, std::min(b->nbricks, sms * per));
+    for (int m = 0; m < 4; ++m) {
+        const int pa = std::max(1, b->prec ? lsm::batch::adj_blocks_per_sm<double>(m)
+                                           : lsm::batch::adj_blocks_per_sm<float>(m));
+        b->agrid[m] = std::max(1, std::min(b->namap[m], sms * pa));
+    }
     b->shape = shape;
     BCU(b, cudaStreamSynchronize(b->stream));
     return LSM_OK;
@@ -221,13 +267,19 @@ template <>
 FieldsT<double>& fields<double>(lsm_batch* b) { return b->f64; }
 
 // Recorded internals of one step (adjoint): the three stage outputs, the
-// RNitermax raw pseudo-step outputs (D + k N) and the sign field.
+// RNitermax raw pseudo-step outputs (D + k ld) and the sign field.
 template <typename T>
 struct Rec {
     T* A[3];
     T* D;
     T* sgn;
 };
+
+// the pseudo-step outputs of a recorded step are b->ld elements apart
+template <typename T>
+T* rec_d(const lsm_batch* b, const Rec<T>& r, int k) {
+    return r.D + (long long)k * (long long)b->ld;
+}
 
 // One physical step phin -> phi_out (phi_out may alias phin; nullptr skips
 // the final bcond_lsm).  With `rec` the stage outputs, the pseudo-step
@@ -240,7 +292,6 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
     const B::BC bc = make_bc(b);
     FieldsT<T> f = fields<T>(b);
     if (rec) f.sgn = rec->sgn;
-    const long long N = b->N;
     if (vol) {
         B::volume<T>(sh, gr, b->d_inst, b->d_brick, nb, f, phin, b->d_part, b->stream);
         B::volume_final(b->d_inst, b->ninst, b->d_brick, nb, b->d_part, b->d_vols, b->stream);
@@ -261,7 +312,7 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
         const T* cur = S[2];
         for (int it = 0; it < R; ++it) {
             const bool last = it == R - 1;
-            T* o = rec ? rec->D + (long long)it * N : (last ? phi_out : f.d[it & 1]);
+            T* o = rec ? rec_d(b, *rec, it) : (last ? phi_out : f.d[it & 1]);
             B::reinit<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, (last && !rec) ? b->d_err : nullptr,
                          b->stream);
             if (last && !rec) B::bc_reinit<T>(b->d_inst, b->ninst, b->nface, f, bc, cur, phi_out, b->stream);
@@ -354,36 +405,37 @@ int check_inst(lsm_batch* b, int q) {
 }
 
 // ------------------------------------------------------------ adjoint state
-// Checkpoints (nck N), segment states (ck N), the recorded internals of
-// every step of a segment (ck (4 + R) N: A1..A3, D1..DR, sign), adjoint
-// fields lam, lam2, lamPhin (3 N), lamW (3 N), reinitialisation
-// coefficients (6 N), lam_u (3 N).
+// Checkpoints (nck arrays), segment states (ck), the recorded internals of
+// every step of a segment (ck (4 + R): A1..A3, D1..DR, sign), adjoint
+// fields lam, lam2, lamPhin (3), lamW (3), lam_u (3); arrays b->ld apart.
 template <typename T>
 struct AdjView {
-    T *ckpt, *seg, *slots, *lam, *lam2, *lamPhin, *lamW[3], *coef, *lamU[3];
+    T *ckpt, *seg, *slots, *lam, *lam2, *lamPhin, *lamW[3], *lamU[3];
 };
 
 int n_ckpt(int nsteps, int ck) { return (nsteps + ck - 1) / ck; }
-long long slot_elems(const lsm_batch* b) { return (long long)(4 + b->cfg.RNitermax) * b->N; }
+// arrays of one recorded step, each b->ld elements apart
+long long slot_elems(const lsm_batch* b) { return (long long)(4 + b->cfg.RNitermax) * (long long)b->ld; }
 
 size_t adj_elems(const lsm_batch* b, int nsteps, int ck) {
-    return (size_t)b->N * (size_t)(n_ckpt(nsteps, ck) + ck + 3 + 3 + 6 + 3) + (size_t)ck * (size_t)slot_elems(b);
+    return b->ld * (size_t)(n_ckpt(nsteps, ck) + ck + 3 + 3 + 3) + (size_t)ck * (size_t)slot_elems(b);
 }
 
 template <typename T>
 Rec<T> slot(lsm_batch* b, const AdjView<T>& v, int q) {
+    const long long L = (long long)b->ld;
     T* p = v.slots + (long long)q * slot_elems(b);
     Rec<T> r;
-    for (int s = 0; s < 3; ++s) r.A[s] = p + (long long)s * b->N;
-    r.D = p + 3 * b->N;
-    r.sgn = p + (long long)(3 + b->cfg.RNitermax) * b->N;
+    for (int s = 0; s < 3; ++s) r.A[s] = p + s * L;
+    r.D = p + 3 * L;
+    r.sgn = p + (3 + b->cfg.RNitermax) * L;
     return r;
 }
 
 template <typename T>
 AdjView<T> adj_view(lsm_batch* b) {
     AdjView<T> v;
-    const long long N = b->N;
+    const long long N = (long long)b->ld;
     T* p = (T*)b->adj;
     v.ckpt = p;
     p += (long long)n_ckpt(b->rec_steps, b->rec_ck) * N;
@@ -401,8 +453,6 @@ AdjView<T> adj_view(lsm_batch* b) {
         v.lamW[c] = p;
         p += N;
     }
-    v.coef = p;
-    p += 6 * N;
     for (int c = 0; c < 3; ++c) {
         v.lamU[c] = p;
         p += N;
@@ -430,7 +480,7 @@ int forward_record_t(lsm_batch* b, int nsteps, int ck) {
     BCU(b, cudaMemsetAsync(v.lam, 0, sizeof(T) * b->N, b->stream));
     for (int n = 0; n < nsteps; ++n) {
         if (n % ck == 0)
-            BCU(b, cudaMemcpyAsync(v.ckpt + (long long)(n / ck) * b->N, f.phi, sizeof(T) * b->N,
+            BCU(b, cudaMemcpyAsync(v.ckpt + (long long)(n / ck) * (long long)b->ld, f.phi, sizeof(T) * b->N,
                                    cudaMemcpyDeviceToDevice, b->stream));
         BTRY(run_steps(b, 1));
     }
@@ -459,10 +509,10 @@ void adj_step(lsm_batch* b, AdjView<T>& v, const Rec<T>& r, const T* phin) {
             B::adj_face<T>(fl, face, b->nplane[face >> 1], bc, kind, pn, in, out, c1, c2, v.lam, b->stream);
     };
     if (R > 0) {
-        faces(1, nullptr, nullptr, r.D + (long long)(R - 1) * N, 0.0, 0.0);
+        faces(1, nullptr, nullptr, rec_d(b, r, R - 1), 0.0, 0.0);
         for (int k = R - 1; k >= 0; --k) {
-            const T* dk = k == 0 ? r.A[2] : r.D + (long long)(k - 1) * N;
-            B::adj_reinit<T>(fl, f, dk, v.lam, v.coef, v.lam2, b->stream);
+            const T* dk = k == 0 ? r.A[2] : rec_d(b, r, k - 1);
+            B::adj_reinit<T>(b->agrid[3], b->d_inst, b->d_amap[3], b->namap[3], f, dk, v.lam, v.lam2, b->stream);
             std::swap(v.lam, v.lam2);
         }
     } else {
@@ -472,8 +522,8 @@ void adj_step(lsm_batch* b, AdjView<T>& v, const Rec<T>& r, const T* phin) {
     const T* ins[3] = {phin, r.A[0], r.A[1]};
     for (int s = 2; s >= 0; --s) {
         faces(0, phin, ins[s], r.A[s], kC[s][0], kC[s][1]);
-        B::adj_stage<T>(fl, f, ins[s], v.lam, v.lam2, v.lamPhin, v.lamW[0], v.lamW[1], v.lamW[2], kC[s][0], kC[s][1],
-                        kC[s][2], s == 0, b->stream);
+        B::adj_stage<T>(b->agrid, b->d_inst, b->d_amap, b->namap, f, ins[s], v.lam, v.lam2, v.lamPhin, v.lamW[0],
+                        v.lamW[1], v.lamW[2], kC[s][0], kC[s][1], kC[s][2], s == 0, b->stream);
         std::swap(v.lam, v.lam2);
     }
 }
@@ -487,17 +537,18 @@ int backward_t(lsm_batch* b) {
     T* const zero_fields[7] = {v.lamPhin, v.lamW[0], v.lamW[1], v.lamW[2], v.lamU[0], v.lamU[1], v.lamU[2]};
     for (T* p : zero_fields) k_zero<T><<<cblocks(N), 256, 0, b->stream>>>(N, p);
     const int ck = b->rec_ck, nsteps = b->rec_steps, nseg = n_ckpt(nsteps, ck);
+    const long long LD = (long long)b->ld;
     for (int sg = nseg - 1; sg >= 0; --sg) {
         const int c0 = sg * ck, L = std::min(c0 + ck, nsteps) - c0;
         // recompute the segment once from its checkpoint, keeping every
         // step's internals, then reverse it step by step
-        BCU(b, cudaMemcpyAsync(v.seg, v.ckpt + (long long)sg * N, sizeof(T) * N, cudaMemcpyDeviceToDevice, b->stream));
+        BCU(b, cudaMemcpyAsync(v.seg, v.ckpt + (long long)sg * LD, sizeof(T) * N, cudaMemcpyDeviceToDevice, b->stream));
         for (int q = 0; q < L; ++q) {
             const Rec<T> r = slot<T>(b, v, q);
-            enqueue_step_io<T>(b, v.seg + (long long)q * N, q + 1 < L ? v.seg + (long long)(q + 1) * N : nullptr, &r,
+            enqueue_step_io<T>(b, v.seg + (long long)q * LD, q + 1 < L ? v.seg + (long long)(q + 1) * LD : nullptr, &r,
                                false);
         }
-        for (int q = L - 1; q >= 0; --q) adj_step<T>(b, v, slot<T>(b, v, q), v.seg + (long long)q * N);
+        for (int q = L - 1; q >= 0; --q) adj_step<T>(b, v, slot<T>(b, v, q), v.seg + (long long)q * LD);
     }
     const Flat fl{b->d_inst, b->d_offs, b->ninst, N};
     lsm::batch::adj_contra<T>(fl, fields<T>(b), v.lamW[0], v.lamW[1], v.lamW[2], v.lamU[0], v.lamU[1], v.lamU[2],
@@ -562,12 +613,13 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
         lsm_batch_destroy(b);
         return st;
     };
-    for (auto& p : b->bufs)
-        if (cudaMalloc(&p, b->esz * n) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
-    for (auto& p : b->comps)
-        if (cudaMalloc(&p, b->esz * n) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
-    if (cudaMalloc(&b->xyz, sizeof(double) * 3 * n) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
-    if (cudaMalloc(&b->cellfix, sizeof(long long) * n) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
+    b->ld = array_stride(n, b->esz) / b->esz;
+    b->ld8 = array_stride(n, 8) / 8;
+    if (cudaMalloc(&b->field_arena, b->esz * b->ld * 21) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
+    for (int a = 0; a < 6; ++a) b->bufs[a] = (char*)b->field_arena + b->esz * b->ld * a;
+    for (int a = 0; a < 15; ++a) b->comps[a] = (char*)b->field_arena + b->esz * b->ld * (6 + a);
+    if (cudaMalloc(&b->xyz, 8 * b->ld8 * 4) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
+    b->cellfix = (long long*)(b->xyz + 3 * b->ld8);
     if (cudaMalloc(&b->staging, sizeof(double) * 4 * b->max_inst_nodes) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->d_inst, sizeof(Inst) * ninst) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->d_offs, sizeof(long long) * (ninst + 1)) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
@@ -577,10 +629,8 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
     cudaMemcpyAsync(b->d_offs, b->off.data(), sizeof(long long) * (ninst + 1), cudaMemcpyHostToDevice, b->stream);
     cudaMemsetAsync(b->d_err, 0, sizeof(unsigned), b->stream);
     cudaMemsetAsync(b->d_vols, 0, sizeof(double) * 4 * ninst, b->stream);
-    for (auto& p : b->bufs) cudaMemsetAsync(p, 0, b->esz * n, b->stream);
-    for (auto& p : b->comps) cudaMemsetAsync(p, 0, b->esz * n, b->stream);
-    cudaMemsetAsync(b->xyz, 0, sizeof(double) * 3 * n, b->stream);
-    cudaMemsetAsync(b->cellfix, 0, sizeof(long long) * n, b->stream);
+    cudaMemsetAsync(b->field_arena, 0, b->esz * b->ld * 21, b->stream);
+    cudaMemsetAsync(b->xyz, 0, 8 * b->ld8 * 4, b->stream);
     auto wire = [&](auto& f, auto* tag) {
         using T = std::remove_pointer_t<decltype(tag)>;
         f.phi = (T*)b->bufs[0];
@@ -592,7 +642,7 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
         for (int c = 0; c < 3; ++c) {
             f.W[c] = (T*)b->comps[c];
             f.u[c] = (T*)b->comps[12 + c];
-            f.xyz[c] = b->xyz + c * n;
+            f.xyz[c] = b->xyz + c * b->ld8;
         }
         for (int c = 0; c < 9; ++c) f.m[c] = (T*)b->comps[3 + c];
         f.cellfix = b->cellfix;
@@ -609,12 +659,9 @@ int lsm_batch_destroy(lsm_batch_handle b) {
     Dev guard(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->exec) cudaGraphExecDestroy(b->exec);
-    for (auto p : b->bufs)
-        if (p) cudaFree(p);
-    for (auto p : b->comps)
-        if (p) cudaFree(p);
-    for (void* p : {(void*)b->xyz, (void*)b->cellfix, (void*)b->staging, (void*)b->d_inst, (void*)b->d_offs,
-                    (void*)b->d_brick, (void*)b->d_part, (void*)b->d_vols, (void*)b->d_err, b->adj})
+    for (void* p : {b->field_arena, (void*)b->xyz, (void*)b->staging, (void*)b->d_inst, (void*)b->d_offs,
+                    (void*)b->d_brick, (void*)b->d_amap[0], (void*)b->d_amap[1], (void*)b->d_amap[2],
+                    (void*)b->d_amap[3], (void*)b->d_part, (void*)b->d_vols, (void*)b->d_err, b->adj})
         if (p) cudaFree(p);
     if (b->h_vols) cudaFreeHost(b->h_vols);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
@@ -631,7 +678,7 @@ int lsm_batch_set_geometry(lsm_batch_handle b, int q, const double* x, const dou
     const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
     const double* c3[3] = {x, y, z};
     for (int c = 0; c < 3; ++c)
-        BCU(b, cudaMemcpyAsync(b->xyz + c * b->N + o, c3[c], sizeof(double) * n,
+        BCU(b, cudaMemcpyAsync(b->xyz + c * b->ld8 + o, c3[c], sizeof(double) * n,
                                on_device(c3[c]) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, b->stream));
     const double* m3[3] = {csi, eta, zet};
     for (int d = 0; d < 3; ++d) {
@@ -639,7 +686,7 @@ int lsm_batch_set_geometry(lsm_batch_handle b, int q, const double* x, const dou
         for (int c = 0; c < 3; ++c) cvt_in(b, 3, c, n, (char*)b->comps[3 + 3 * d + c] + b->esz * o);
     }
     // cell_hex indexes from the packed base arrays with the instance offset o
-    lsm::batch::cell_hex(o, I.ni, I.nj, I.nk, b->xyz, b->xyz + b->N, b->xyz + 2 * b->N, b->cellfix, b->stream);
+    lsm::batch::cell_hex(o, I.ni, I.nj, I.nk, b->xyz, b->xyz + b->ld8, b->xyz + 2 * b->ld8, b->cellfix, b->stream);
     BCU(b, cudaGetLastError());
     BCU(b, cudaStreamSynchronize(b->stream));
     return LSM_OK;
