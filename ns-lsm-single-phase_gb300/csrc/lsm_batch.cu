@@ -212,8 +212,9 @@ __global__ void __launch_bounds__(TX * TY * TZ) k_stage(const Inst* __restrict__
         if (!b.valid) continue;
         const Inst& I = inst[b.inst];
         const long long l = I.off + b.i + (long long)I.ni * (b.j + (long long)I.nj * b.k);
+        const T pn = __ldg(phin + l), p1 = __ldg(phi1 + l);   // issued with the stencil loads
         const T R = interior(I, b.i, b.j, b.k) ? stage_rhs(f, phi1, I, l, b.i, b.j, b.k) : T(0);
-        out[l] = c1 * __ldg(phin + l) + c2 * __ldg(phi1 + l) - c3 * R;
+        out[l] = c1 * pn + c2 * p1 - c3 * R;
     }
 }
 
