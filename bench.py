@@ -505,6 +505,7 @@ FWDADJ_BYTES = {
     "k_stage": 17.0 / 3.0 * 4,     # phi_prev, phi^n (stages 2-3), W(3); stage output
     "k_sign": 11 * 4,              # phi0, metrics(9); s
     "k_reinit": 12 * 4,            # d, s, metrics(9); d
+    "k_sign_reinit": 12 * 4,       # phi0, metrics(9); s, d
     "k_volume": 4 + 8,             # phi (FP32) + fixed-point cell volume (interface-cell coordinates not counted)
     "k_bc_full": 2 * 4,            # phi in, phi out
     "k_adj_stage_x": 8 * 4,        # in, W_x, lamP0, lamPhin (rmw), lamW_x (rmw); lam_in

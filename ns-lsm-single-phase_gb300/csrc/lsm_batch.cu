@@ -372,7 +372,16 @@ __device__ __forceinline__ T godunov(const FieldsT<T>& f, const T* __restrict__ 
 }
 
 // calc_sign_ini (Kang sign) with the frozen band folded in: s = 0 where
-// |phi0| < eps and |grad phi0| > 0 (the lambda correction pins d to phi0).
+// |phi0| < eps and |grad phi0| > 0 (the lambda correction pins d to phi0);
+// g is the Godunov norm of phi0 chosen by sign(phi0).
+template <typename T>
+__device__ __forceinline__ T sign_of(T p, T g, T eps) {
+    if (p >= eps) return T(1);
+    if (p <= -eps) return T(-1);
+    if (p != T(0) && g > T(0)) return T(0);
+    return p / eps - T(1.0 / kPi) * vsin(T(kPi) * p / eps);
+}
+
 template <typename T, int TX, int TY, int TZ>
 __global__ void __launch_bounds__(TX * TY * TZ) k_sign(const Inst* __restrict__ inst,
         const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phi0) {
@@ -382,14 +391,8 @@ __global__ void __launch_bounds__(TX * TY * TZ) k_sign(const Inst* __restrict__ 
         const Inst& I = inst[b.inst];
         const long long l = I.off + b.i + (long long)I.ni * (b.j + (long long)I.nj * b.k);
         const T p = __ldg(phi0 + l);
-        const T eps = ipar<T>(I.eps, I.eps64);
         const T g = godunov(f, phi0, I, l, b.i, b.j, b.k, p > T(0) ? T(1) : T(-1));
-        T s;
-        if (p >= eps) s = T(1);
-        else if (p <= -eps) s = T(-1);
-        else if (p != T(0) && g > T(0)) s = T(0);
-        else s = p / eps - T(1.0 / kPi) * vsin(T(kPi) * p / eps);
-        f.sgn[l] = s;
+        f.sgn[l] = sign_of(p, g, ipar<T>(I.eps, I.eps64));
     }
 }
 
@@ -414,6 +417,30 @@ __global__ void __launch_bounds__(TX * TY * TZ) k_reinit(const Inst* __restrict_
         const Inst& I = inst[b.inst];
         const long long l = I.off + b.i + (long long)I.ni * (b.j + (long long)I.nj * b.k);
         const T r = reinit_node(f, din, I, l, b.i, b.j, b.k);
+        dout[l] = r;
+        if (err && !vfinite(r)) atomicOr(err, (unsigned)kErrNonFinite);
+    }
+}
+
+// calc_sign_ini fused with the first pseudo-step: both use the Godunov norm
+// of the advected field phi0 chosen by sign(phi0) (a node whose s is not 0
+// has the sign of phi0: p / eps - sin(pi p / eps) / pi has the sign of p),
+// so one evaluation and one read of phi0 and the metrics give s and
+// d1 = phi0 - dtau s (|grad phi0|_G - 1).
+template <typename T, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(TX * TY * TZ) k_sign_reinit(const Inst* __restrict__ inst,
+        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phi0,
+        T* __restrict__ dout, unsigned* err) {
+    for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
+        const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
+        if (!b.valid) continue;
+        const Inst& I = inst[b.inst];
+        const long long l = I.off + b.i + (long long)I.ni * (b.j + (long long)I.nj * b.k);
+        const T p = __ldg(phi0 + l);
+        const T g = godunov(f, phi0, I, l, b.i, b.j, b.k, p > T(0) ? T(1) : T(-1));
+        const T s = sign_of(p, g, ipar<T>(I.eps, I.eps64));
+        f.sgn[l] = s;
+        const T r = s == T(0) ? p : p - ipar<T>(I.dtau, I.dtau64) * s * (g - T(1));
         dout[l] = r;
         if (err && !vfinite(r)) atomicOr(err, (unsigned)kErrNonFinite);
     }
@@ -1145,6 +1172,10 @@ LSM_BATCH_RUNNER(RunReinit, k_reinit,
                  (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* din, T* dout,
                   unsigned* err, cudaStream_t s),
                  (inst, bi, nb, f, din, dout, err))
+LSM_BATCH_RUNNER(RunSignReinit, k_sign_reinit,
+                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* p0, T* dout,
+                  unsigned* err, cudaStream_t s),
+                 (inst, bi, nb, f, p0, dout, err))
 LSM_BATCH_RUNNER(RunVolume, k_volume,
                  (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi, long long* part,
                   cudaStream_t s),
@@ -1195,6 +1226,11 @@ template <typename T>
 void reinit(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* din, T* dout,
             unsigned* err, cudaStream_t s) {
     dispatch<RunReinit, T>(shape, grid, inst, bi, nb, f, din, dout, err, s);
+}
+template <typename T>
+void sign_reinit(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi0,
+                 T* dout, unsigned* err, cudaStream_t s) {
+    dispatch<RunSignReinit, T>(shape, grid, inst, bi, nb, f, phi0, dout, err, s);
 }
 template <typename T>
 void bc_reinit(const Inst* inst, int ninst, long long nface, FieldsT<T> f, BC bc, const T* din, T* dout,
@@ -1282,6 +1318,8 @@ void adj_contra(const Flat& fl, FieldsT<T> f, const T* w0, const T* w1, const T*
     template void reinit<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, unsigned*,             \
                             cudaStream_t);                                                                            \
     template void bc_reinit<T>(const Inst*, int, long long, FieldsT<T>, BC, const T*, T*, cudaStream_t);              \
+    template void sign_reinit<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, unsigned*,      \
+                                 cudaStream_t);                                                                   \
     template void volume<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, long long*, cudaStream_t);  \
     template void adj_face<T>(const Flat&, int, long long, BC, int, const T*, const T*, const T*, double, double, T*, \
                               cudaStream_t);                                                                          \

@@ -87,6 +87,10 @@ void sign(int shape, int grid, const Inst* inst, const Brick* bricks, int nbrick
 template <typename T>
 void reinit(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f, const T* din,
             T* dout, unsigned* err, cudaStream_t s);
+// sign field of phi0 and the first pseudo-step from phi0 in one pass
+template <typename T>
+void sign_reinit(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f,
+                 const T* phi0, T* dout, unsigned* err, cudaStream_t s);
 // bcond_lsm on the output of the last reinitialisation pseudo-step (dout):
 // boundary values are recomputed pointwise from that step's input din.
 template <typename T>

@@ -308,13 +308,15 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
         // reinitialization (src/reinitialization.F90:55-104); the last
         // pseudo-step writes phi and gets the final bcond_lsm
         // (src/levelsetmethod.F90:318-321)
-        B::sign<T>(sh, gr, b->d_inst, b->d_brick, nb, f, S[2], b->stream);
+        // the sign field and the first pseudo-step in one pass, then one
+        // launch per pseudo-step
         const T* cur = S[2];
         for (int it = 0; it < R; ++it) {
             const bool last = it == R - 1;
             T* o = rec ? rec_d(b, *rec, it) : (last ? phi_out : f.d[it & 1]);
-            B::reinit<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, (last && !rec) ? b->d_err : nullptr,
-                         b->stream);
+            unsigned* err = (last && !rec) ? b->d_err : nullptr;
+            if (it == 0) B::sign_reinit<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, err, b->stream);
+            else B::reinit<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, err, b->stream);
             if (last && !rec) B::bc_reinit<T>(b->d_inst, b->ninst, b->nface, f, bc, cur, phi_out, b->stream);
             cur = o;
         }
@@ -816,9 +818,11 @@ long long lsm_batch_nodes(lsm_batch_handle b) { return b ? b->N : 0; }
 
 int lsm_batch_launches_per_step(lsm_batch_handle b) {
     if (!b) return 0;
-    // volume 2, contra 1, three stages x (stencil + faces) 6, then sign +
-    // RNitermax pseudo-steps + final faces, or one full bcond pass
-    return 2 + 1 + 6 + (b->cfg.RNitermax > 0 ? 1 + b->cfg.RNitermax + 1 : 1);
+    // volume 2, contra 1, three stages x (stencil + faces) 6, then
+    // RNitermax pseudo-steps (the first with the sign field) + final faces,
+    // or one full bcond pass
+    const int R = b->cfg.RNitermax;
+    return 2 + 1 + 6 + (R > 0 ? R + 1 : 1);
 }
 
 const char* lsm_batch_last_error(lsm_batch_handle b) { return b ? b->err.c_str() : ""; }
