@@ -88,10 +88,16 @@ typedef struct lsm_params {
     int    TotalVolumeComputation;   /* informational (volume is always computed) */
     int    GlobalMassCorrection;     /* 1: post-advection volume pass as in the reference */
     double BigPhi;                   /* |phi| cut-off for BC order and ghost-fluid list */
-    double epsReinitialisation;      /* carried for the live Sussman variant */
+    double epsReinitialisation;      /* convergence threshold of reinitialisation_test2 */
     int    M_Sphi0;                  /* sign model in calc_sign_ini: 1 Kang piecewise, 0 phi/sqrt(phi^2+(|grad|eps)^2) */
-    int    reinit_scheme;            /* 0: `reinitialization` (Sussman-Fatemi, forward Euler + lambda) */
+    int    reinit_scheme;            /* 0: `reinitialization` (Sussman-Fatemi, forward Euler + lambda);
+                                        1: `reinitialisation_test2` (the reference's live call,
+                                           src/levelsetmethod.F90:313: ENO2 gradients, TVD-RK3 in
+                                           pseudo time, convergence mask and early exit) */
     int    write_global_volume;      /* 1: append pre-advection volume to GlobalVolume.txt */
+    int    OrderReinitialisationBoundaries; /* 1, 2 or 3: one-sided derivative order on physical faces
+                                               in calc_NormGrad_d (BiasedDerivative) */
+    int    ENOBCReinitialisation;    /* 1: with order 2, ENO2Boundary instead of the 2nd-order formula */
 } lsm_params;
 
 /* Fill a params struct with the values of the reference's example deck
@@ -189,6 +195,29 @@ int lsm_calc_lambda_rn(lsm_handle h, const lsm_grid* g, const lsm_params* p,
 int lsm_reinitialization(lsm_handle h, const lsm_grid* g, const lsm_params* p,
                          const double* phi0, const double* csi, const double* eta,
                          const double* zet, double* phi_out);
+
+/* calc_NormGrad_d (src/calc_NormGrad_d.F90:1-2448): |grad phi_rn| by ENO2 in
+   every direction (stencil choice by the sign of phizero), one-sided
+   BiasedDerivative of order OrderReinitialisationBoundaries (ENO2Boundary
+   when ENOBCReinitialisation and order 2) along a direction whose face is
+   physical at the node; 0 on ghost nodes.  Kept from the reference: the two
+   i-face blocks choose their ENO2 stencils with phizero at the last
+   interior node, because they never assign phi0. */
+int lsm_calc_normgrad_d(lsm_handle h, const lsm_grid* g, const lsm_params* p,
+                        const double* phi_rn, const double* phizero, const double* csi,
+                        const double* eta, const double* zet, double* normgrad);
+
+/* reinitialisation_test2 (src/reinitialisation_test2.F90:1-221, non-hybrid):
+   the reinitialisation the reference calls (src/levelsetmethod.F90:313).
+   Up to RNitermax pseudo-time iterations of TVD-RK3 with step RNtimestep on
+   the nodes whose |grad d| at the start of the iteration exceeds
+   1 + epsReinitialisation, with the GetLambdaMassCorrection term; stops
+   when max and min of |grad d| are both within epsReinitialisation of 1.
+   No halo exchange inside, as in the reference.  *iterations (nullable)
+   receives the iterations run.  phi_out = d (no bcond_lsm). */
+int lsm_reinitialisation_test2(lsm_handle h, const lsm_grid* g, const lsm_params* p,
+                               const double* phizero, const double* csi, const double* eta,
+                               const double* zet, double* phi_out, int* iterations);
 
 /* narrowband (src/narrowband.F90:2-19): nband = |phi_n| < narrowcoef*epslsm + 1.0E-5
    on every node (ghosts included); every node 1 when isnarrow == 0. */

@@ -314,6 +314,52 @@ int reinit_device(lsm_context* c, const lsm_grid* g, const DevGrid& dg, const ls
     return LSM_OK;
 }
 
+// reinitialisation_test2 (src/reinitialisation_test2.F90:1-221, non-hybrid)
+// from phizero into dn1 (dn: scratch); *iters = pseudo-time iterations run.
+// The convergence test needs the field's maximum and minimum on the host
+// once per iteration (the reference's maxval/minval, then `exit`).
+int sussman_device(lsm_context* c, const DevGrid& dg, const lsm_params* p, const double* phizero,
+                   const double* csi, const double* eta, const double* zet, double* dn1, double* dn, int* iters) {
+    if (p->OrderReinitialisationBoundaries < 1 || p->OrderReinitialisationBoundaries > 3)
+        return set_err(c, LSM_ERR_BAD_PARAM, "OrderReinitialisationBoundaries must be 1, 2 or 3");
+    cudaError_t e;
+    const long long N = (long long)dg.ni * dg.nj * dg.nk;
+    double* sg = (double*)pool_get(c, "ss_sign", 8 * N, &e);
+    double* ng = sg ? (double*)pool_get(c, "ss_ng", 8 * N, &e) : nullptr;
+    double* ngc = ng ? (double*)pool_get(c, "ss_ngc", 8 * N, &e) : nullptr;
+    double* part = ngc ? (double*)pool_get(c, "ss_part", 16 * (size_t)lsm::minmax_partials(N) + 16, &e) : nullptr;
+    if (!part) return cuda_fail(c, e, "cudaMalloc(reinitialisation_test2)");
+    double* res = part + 2 * lsm::minmax_partials(N);
+    // the i-face blocks of calc_NormGrad_d take phizero at the last node of
+    // the interior loop (src/calc_NormGrad_d.F90:41-56, 186-376)
+    const long long stale = lsm::gid(dg, dg.ib - (dg.pf ? 1 : 0), dg.jb - (dg.pr ? 1 : 0), dg.kb - (dg.pu ? 1 : 0));
+    const int order = p->OrderReinitialisationBoundaries, enobc = p->ENOBCReinitialisation ? 1 : 0;
+    const double C[3][3] = {{1.0, 0.0, 1.0}, {3.0 / 4.0, 1.0 / 4.0, 1.0 / 4.0}, {1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0}};
+    lsm::launch_sign_phi0(N, phizero, p->epslsm, sg, c->stream);
+    lsm::launch_copy(phizero, dn1, N, c->stream);
+    lsm::launch_normgrad_d(dg, order, enobc, dn1, phizero, stale, csi, eta, zet, ng, c->stream);
+    LSM_TRY(after_launch(c));
+    int done = 0;
+    for (int it = 1; it <= p->RNitermax; ++it) {
+        double mm[2];
+        lsm::launch_minmax(N, ng, part, res, c->stream);
+        LSM_CU(c, cudaMemcpyAsync(mm, res, sizeof(mm), cudaMemcpyDeviceToHost, c->stream));
+        LSM_CU(c, cudaStreamSynchronize(c->stream));
+        if (std::fabs(mm[0] - 1.0) < p->epsReinitialisation && std::fabs(mm[1] - 1.0) < p->epsReinitialisation) break;
+        lsm::launch_copy(dn1, dn, N, c->stream);
+        lsm::launch_normgrad_d(dg, order, enobc, dn, phizero, stale, csi, eta, zet, ngc, c->stream);
+        for (int rk = 0; rk < 3; ++rk) {
+            lsm::launch_normgrad_d(dg, order, enobc, dn1, phizero, stale, csi, eta, zet, ng, c->stream);
+            lsm::launch_sussman_rk(dg, dn, dn1, ng, ngc, sg, p->epslsm, p->epsReinitialisation, p->RNtimestep,
+                                   C[rk][0], C[rk][1], C[rk][2], c->stream);
+        }
+        LSM_TRY(after_launch(c));
+        done = it;
+    }
+    if (iters) *iters = done;
+    return LSM_OK;
+}
+
 // list-directed REAL(8) output in the shape gfortran gives it
 void format_real8(double v, char* buf, size_t n) {
     const double a = v < 0 ? -v : v;
@@ -359,6 +405,8 @@ void lsm_params_default(lsm_params* p) {
     p->M_Sphi0 = 1;
     p->reinit_scheme = 0;
     p->write_global_volume = 0;
+    p->OrderReinitialisationBoundaries = 1;  // control.dat
+    p->ENOBCReinitialisation = 0;            // control.dat: .false.
 }
 
 int lsm_create(lsm_handle* h, int device, void* stream) {
@@ -604,6 +652,57 @@ int lsm_reinitialization(lsm_handle h, const lsm_grid* g, const lsm_params* p, c
     return S.finish();
 }
 
+// ------------------------------------------------------------------ L0
+int lsm_calc_normgrad_d(lsm_handle h, const lsm_grid* g, const lsm_params* p, const double* phi_rn,
+                        const double* phizero, const double* csi, const double* eta, const double* zet,
+                        double* normgrad) {
+    LSM_PROLOGUE(h, g);
+    LSM_TRY(check_params(c, p));
+    if (p->OrderReinitialisationBoundaries < 1 || p->OrderReinitialisationBoundaries > 3)
+        return set_err(c, LSM_ERR_BAD_PARAM, "OrderReinitialisationBoundaries must be 1, 2 or 3");
+    if (!phi_rn || !phizero || !csi || !eta || !zet || !normgrad) return set_err(c, LSM_ERR_NULL, "array is NULL");
+    void *dp, *dz0, *dcsi, *deta, *dzet, *dout;
+    Staging S(c);
+    S.add(phi_rn, 8 * N, Staging::IN, &dp);
+    S.add(phizero, 8 * N, Staging::IN, &dz0);
+    S.add(csi, 24 * N, Staging::IN, &dcsi);
+    S.add(eta, 24 * N, Staging::IN, &deta);
+    S.add(zet, 24 * N, Staging::IN, &dzet);
+    S.add(normgrad, 8 * N, Staging::OUT, &dout);
+    LSM_TRY(S.resolve());
+    const long long stale = lsm::gid(dg, dg.ib - (dg.pf ? 1 : 0), dg.jb - (dg.pr ? 1 : 0), dg.kb - (dg.pu ? 1 : 0));
+    lsm::launch_normgrad_d(dg, p->OrderReinitialisationBoundaries, p->ENOBCReinitialisation ? 1 : 0,
+                           (const double*)dp, (const double*)dz0, stale, (const double*)dcsi, (const double*)deta,
+                           (const double*)dzet, (double*)dout, c->stream);
+    LSM_TRY(after_launch(c));
+    return S.finish();
+}
+
+int lsm_reinitialisation_test2(lsm_handle h, const lsm_grid* g, const lsm_params* p, const double* phizero,
+                               const double* csi, const double* eta, const double* zet, double* out,
+                               int* iterations) {
+    LSM_PROLOGUE(h, g);
+    LSM_TRY(check_params(c, p));
+    if (!phizero || !csi || !eta || !zet || !out) return set_err(c, LSM_ERR_NULL, "array is NULL");
+    void *dp, *dcsi, *deta, *dzet, *dout;
+    Staging S(c);
+    S.add(phizero, 8 * N, Staging::IN, &dp);
+    S.add(csi, 24 * N, Staging::IN, &dcsi);
+    S.add(eta, 24 * N, Staging::IN, &deta);
+    S.add(zet, 24 * N, Staging::IN, &dzet);
+    S.add(out, 8 * N, Staging::OUT, &dout);
+    LSM_TRY(S.resolve());
+    cudaError_t e;
+    double* D1 = (double*)pool_get(c, "rn_d1", 8 * N, &e);
+    double* D2 = D1 ? (double*)pool_get(c, "rn_d2", 8 * N, &e) : nullptr;
+    if (!D2) return cuda_fail(c, e, "cudaMalloc(reinitialisation_test2)");
+    LSM_TRY(sussman_device(c, dg, p, (const double*)dp, (const double*)dcsi, (const double*)deta,
+                           (const double*)dzet, D1, D2, iterations));
+    lsm::launch_copy(D1, (double*)dout, (long long)N, c->stream);
+    LSM_TRY(after_launch(c));
+    return S.finish();
+}
+
 // ------------------------------------------------------------------ N1
 int lsm_narrowband(lsm_handle h, const lsm_grid* g, const lsm_params* p, const double* phin, int* nb) {
     LSM_PROLOGUE(h, g);
@@ -738,7 +837,8 @@ int lsm_levelsetmethod(lsm_handle h, const lsm_grid* g, const lsm_params* p, con
     LSM_TRY(check_params(c, p));
     if (p->hybrid_reinitialisation)
         return set_err(c, LSM_ERR_UNSUPPORTED, "hybrid (geometric) reinitialisation is outside the path");
-    if (p->reinit_scheme != 0) return set_err(c, LSM_ERR_UNSUPPORTED, "reinit_scheme must be 0");
+    if (p->reinit_scheme != 0 && p->reinit_scheme != 1)
+        return set_err(c, LSM_ERR_UNSUPPORTED, "reinit_scheme must be 0 or 1");
     if (p->sussman_correction_method != 0)
         return set_err(c, LSM_ERR_UNSUPPORTED, "sussman_correction_method 1 (testfilter) is outside the path");
     if (!q || !csi || !eta || !zet || !aj || !phi || !phi_n || !x || !y || !z)
@@ -800,8 +900,15 @@ int lsm_levelsetmethod(lsm_handle h, const lsm_grid* g, const lsm_params* p, con
             if (!X) X = b; else if (!Y) Y = b;
         }
         double* res = nullptr;
-        LSM_TRY(reinit_device(c, g, dg, p, cur, (const double*)dcsi, (const double*)deta, (const double*)dzet, X, Y,
-                              &res));
+        if (p->reinit_scheme == 1) {
+            // the reference's live call, src/levelsetmethod.F90:313
+            LSM_TRY(sussman_device(c, dg, p, cur, (const double*)dcsi, (const double*)deta, (const double*)dzet, X,
+                                   Y, nullptr));
+            res = X;
+        } else {
+            LSM_TRY(reinit_device(c, g, dg, p, cur, (const double*)dcsi, (const double*)deta, (const double*)dzet,
+                                  X, Y, &res));
+        }
         lsm::launch_bc_full(dg, make_bc(p), res, (double*)dphi, c->d_err, c->stream);
         LSM_TRY(after_launch(c));
         LSM_TRY(exchange(c, (double*)dphi, g));

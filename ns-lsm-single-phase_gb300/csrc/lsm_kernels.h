@@ -38,6 +38,17 @@ void launch_metrics(const DevGrid& g, const double* x, const double* y, const do
                     double* csi, double* eta, double* zet, double* aj, cudaStream_t s);
 void launch_copy(const double* src, double* dst, long long n, cudaStream_t s);
 
+// reinitialisation_test2 and calc_NormGrad_d (lsm_sussman.cu)
+void launch_sign_phi0(long long n, const double* phi0, double eps, double* sg, cudaStream_t s);
+void launch_normgrad_d(const DevGrid& g, int order, int enobc, const double* phi, const double* phizero,
+                       long long stale, const double* csi, const double* eta, const double* zet, double* out,
+                       cudaStream_t s);
+void launch_sussman_rk(const DevGrid& g, const double* dn, double* dn1, const double* ng, const double* ngc,
+                       const double* sg, double eps, double epsr, double dt, double c1, double c2, double c3,
+                       cudaStream_t s);
+int minmax_partials(long long n);
+void launch_minmax(long long n, const double* a, double* part, double* res, cudaStream_t s);
+
 // ---- water volume, band and ghost-fluid list (lsm_volume.cu, --fmad=false)
 // Number of per-block partial slots the volume kernel needs for this grid.
 int volume_partial_blocks(const DevGrid& g);

@@ -42,7 +42,8 @@ class LsmParams(C.Structure):
                 ("TotalVolumeComputation", C.c_int), ("GlobalMassCorrection", C.c_int),
                 ("BigPhi", C.c_double), ("epsReinitialisation", C.c_double),
                 ("M_Sphi0", C.c_int), ("reinit_scheme", C.c_int),
-                ("write_global_volume", C.c_int)]
+                ("write_global_volume", C.c_int), ("OrderReinitialisationBoundaries", C.c_int),
+                ("ENOBCReinitialisation", C.c_int)]
 
 
 class LsmBatchInstance(C.Structure):
@@ -86,6 +87,8 @@ SIGNATURES = {
     "lsm_calc_rh_rn": (_i, [_vp, _G] + [_vp] * 6),
     "lsm_calc_lambda_rn": (_i, [_vp, _G, _P, _vp, _vp, _vp, _d, _vp]),
     "lsm_reinitialization": (_i, [_vp, _G, _P] + [_vp] * 5),
+    "lsm_calc_normgrad_d": (_i, [_vp, _G, _P] + [_vp] * 6),
+    "lsm_reinitialisation_test2": (_i, [_vp, _G, _P] + [_vp] * 5 + [C.POINTER(_i)]),
     "lsm_narrowband": (_i, [_vp, _G, _P, _vp, _vp]),
     "lsm_total_water_volume": (_i, [_vp, _G] + [_vp] * 6),
     "lsm_cell_water_volumes": (_i, [_vp, _G] + [_vp] * 5),

@@ -234,6 +234,27 @@ class LevelSet:
                    _addr(zet, grid, 3, np.float64), _addr(out, grid, 1, np.float64))
         return out
 
+    # ------------------------------------------------------------ L0
+    def calc_normgrad_d(self, grid: Grid, p: LsmParams, phi_rn, phizero, csi, eta, zet):
+        self._sync_stream(phi_rn)
+        out = _new(phi_rn, grid)
+        g, cp = grid.to_c(), p.to_c()
+        self._call("lsm_calc_normgrad_d", C.byref(g), C.byref(cp), _addr(phi_rn, grid, 1, np.float64),
+                   _addr(phizero, grid, 1, np.float64), _addr(csi, grid, 3, np.float64),
+                   _addr(eta, grid, 3, np.float64), _addr(zet, grid, 3, np.float64), _addr(out, grid, 1, np.float64))
+        return out
+
+    def reinitialisation_test2(self, grid: Grid, p: LsmParams, phizero, csi, eta, zet):
+        """-> (phi reinitialised, pseudo-time iterations run)"""
+        self._sync_stream(phizero)
+        out = _new(phizero, grid)
+        g, cp = grid.to_c(), p.to_c()
+        it = C.c_int(0)
+        self._call("lsm_reinitialisation_test2", C.byref(g), C.byref(cp), _addr(phizero, grid, 1, np.float64),
+                   _addr(csi, grid, 3, np.float64), _addr(eta, grid, 3, np.float64),
+                   _addr(zet, grid, 3, np.float64), _addr(out, grid, 1, np.float64), C.byref(it))
+        return out, it.value
+
     # ------------------------------------------------------------ N1 - N3
     def narrowband(self, grid: Grid, p: LsmParams, phi_n):
         self._sync_stream(phi_n)

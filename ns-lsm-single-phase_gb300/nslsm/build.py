@@ -30,6 +30,7 @@ UNITS = {
     "lsm_runtime.cu": ["-Xcompiler", "-fvisibility=default"],
     "lsm_fp64.cu": ["--fmad=false"],
     "lsm_volume.cu": ["--fmad=false"],
+    "lsm_sussman.cu": ["--fmad=false"],
     "lsm_capi.cu": ["-Xcompiler", "-fvisibility=default"],
     "lsm_batch.cu": ["--fmad=true"],
     "lsm_batch_capi.cu": ["-Xcompiler", "-fvisibility=default"],

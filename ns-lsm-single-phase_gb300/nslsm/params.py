@@ -36,8 +36,10 @@ class LsmParams:
     BigPhi: float = 5.0
     epsReinitialisation: float = 1.0e-5
     M_Sphi0: int = 1
-    reinit_scheme: int = 0
+    reinit_scheme: int = 0              # 1: reinitialisation_test2, the reference's live call
     write_global_volume: bool = False
+    OrderReinitialisationBoundaries: int = 1
+    ENOBCReinitialisation: bool = False
 
     def to_c(self) -> _CParams:
         p = _CParams()
@@ -142,8 +144,8 @@ def read_ind3dmg_lsm(path_or_text: str, delti: float, nzone: int = 1, myzone: in
         r.read(nsave)  # save_LSdebug_tsteps
     p.epsReinitialisation = _real(r.read(1)[0])
     r.read(1)          # OrderLSAdvectionBoundaries
-    r.read(1)          # OrderReinitialisationBoundaries
-    r.read(1)          # ENOBCReinitialisation
+    p.OrderReinitialisationBoundaries = int(r.read(1)[0])
+    p.ENOBCReinitialisation = _logical(r.read(1)[0])
     p.BigPhi = _real(r.read(1)[0])
     p.delti_lsm = delti / float(p.numiter_lsm)
     return p

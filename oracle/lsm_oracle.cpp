@@ -924,16 +924,205 @@ int oracle_mg_metrics(const lsm_grid* gg, const double* x, const double* y, cons
     return LSM_OK;
 }
 
+/* ------------------------------------------------------------------ L0 --- */
+/* The reference's live reinitialisation: reinitialisation_test2
+   (src/reinitialisation_test2.F90:1-221) with calc_NormGrad_d
+   (src/calc_NormGrad_d.F90:1-2448) and the AdvectionMethods helpers
+   GetENO2Reconstruction (src/AdvectionMethods.F90:63-191), BiasedDerivative
+   (:248-302), GetSignPhi0 (:576-587), ENO2Boundary (:654-707) and
+   GetLambdaMassCorrection (src/global_lsm.F90:200-219). */
+} /* extern "C" */
+namespace {
+
+/* GetENO2Reconstruction, src/AdvectionMethods.F90:63-191 */
+double eno2(double f0, double fLL, double fL, double fC, double fR, double fRR, bool lo, bool hi) {
+    double a, b, Mf, dp, dm;
+    if (lo) {
+        a = fR - (2.0 * fC) + fL;
+        b = fRR - (2.0 * fR) + fC;
+        Mf = a;
+        if (std::fabs(b) < std::fabs(a)) Mf = b;
+        dp = fR - fC - 0.5 * Mf;
+        a = fR - (2.0 * fC) + fL;
+        Mf = a;
+        dm = fC - fL + 0.5 * Mf;
+    } else if (hi) {
+        a = fR - (2.0 * fC) + fL;
+        Mf = a;
+        dp = fR - fC - 0.5 * Mf;
+        a = fR - (2.0 * fC) + fL;
+        b = fC - (2.0 * fL) + fLL;
+        Mf = a;
+        if (std::fabs(b) < std::fabs(a)) Mf = b;
+        dm = fC - fL + 0.5 * Mf;
+    } else {
+        a = fR - (2.0 * fC) + fL;
+        b = fRR - (2.0 * fR) + fC;
+        Mf = a;
+        if (std::fabs(b) < std::fabs(a)) Mf = b;
+        dp = fR - fC - 0.5 * Mf;
+        a = fR - (2.0 * fC) + fL;
+        b = fC - (2.0 * fL) + fLL;
+        Mf = a;
+        if (std::fabs(b) < std::fabs(a)) Mf = b;
+        dm = fC - fL + 0.5 * Mf;
+    }
+    const double sg = std::fabs(f0) > kEpsSims ? (f0 >= 0.0 ? 1.0 : -1.0) : 0.0;
+    if (sg * (fR - fC) < 0.0 && sg * (fC - fL) < -sg * (fR - fC)) return dp;
+    if (sg * (fC - fL) > 0.0 && sg * (fR - fC) > -sg * (fC - fL)) return dm;
+    return 0.5 * (dp + dm);
+}
+
+/* ENO2Boundary, src/AdvectionMethods.F90:654-707 */
+double eno2_boundary(double f0, double f1, double f2, int bias) {
+    const double as = (double)bias;
+    const double D1 = as * (f1 - f0), D2 = as * (f2 - f1), D3 = as * (f2 - f0) / 2.0;
+    if (std::fabs(D1 - D2) < kEpsSims) return D1;
+    if (std::fabs(D1) < std::fabs(D2)) return (2.0 * D1 + D2) / 3.0;
+    if (std::fabs(D2) < std::fabs(D1)) return (D1 + 2.0 * D2) / 3.0;
+    if (std::fabs(D1) == std::fabs(D2)) return (4.0 * D1 + D2) / 5.0;
+    if (std::fabs(D1) < std::fabs(D3) && std::fabs(D2) < std::fabs(D3)) return (3.0 * D1 + 6.0 * D2 - D3) / 7.0;
+    if (std::fabs(D1) >= std::fabs(D3) && std::fabs(D2) >= std::fabs(D3)) return D3;
+    return D1;
+}
+
+/* BiasedDerivative, src/AdvectionMethods.F90:248-302 (orders 1, 2, 3) */
+double biased(double f0, double f1, double f2, double f3, int order, int bias, bool enobc) {
+    const double as = (double)bias;
+    if (order == 1) return as * (-1.0 * f0 + 1.0 * f1);
+    if (order == 2) {
+        if (enobc) return eno2_boundary(f0, f1, f2, bias);
+        return as * (-(3.0 * f0) + 4.0 * f1 - 1.0 * f2) / 2.0;
+    }
+    return as * (-(11.0 * f0) + 18.0 * f1 - 9.0 * f2 + 2.0 * f3) / 6.0;
+}
+
+/* GetSignPhi0, src/AdvectionMethods.F90:576-587 */
+inline double sign_phi0(double phi0, double eps) {
+    if (std::fabs(phi0) > eps) return phi0 >= 0.0 ? 1.0 : -1.0;
+    return phi0 / eps - 1.0 / kPi * std::sin((kPi * phi0) / eps);
+}
+
+/* GetLambdaMassCorrection, src/global_lsm.F90:200-219 */
+inline double lambda_mass(double phi, double s, double ng, double eps) {
+    const double d = deltaf(phi, eps);
+    const double num = -d * s * (1.0 - ng);
+    const double den = (d * d) * ng;
+    return std::fabs(den) < kEpsSims ? 0.0 : num / den;
+}
+
+} /* namespace */
+extern "C" {
+
+/* calc_NormGrad_d, src/calc_NormGrad_d.F90:1-2448: |grad phi_RN| by ENO2 in
+   each direction, one-sided BiasedDerivative along a direction whose face is
+   physical at the node, zero on ghost nodes.  The blocks of the reference
+   (interior, 6 faces, 12 edges, 8 corners) reduce to a per-direction choice;
+   the two i-face blocks (src/calc_NormGrad_d.F90:186-376) never assign phi0,
+   so their ENO2 stencil choice uses phizero at the last node of the
+   interior loop (iRN_end, jRN_end, kRN_end), which is kept here. */
+int oracle_calc_normgrad_d(const lsm_grid* gg, const lsm_params* p, const double* phi, const double* phizero,
+                           const double* csi, const double* eta, const double* zet, double* ng) {
+    int st = check_grid(gg); if (st) return st;
+    if (p->OrderReinitialisationBoundaries < 1 || p->OrderReinitialisationBoundaries > 3) return LSM_ERR_BAD_PARAM;
+    Grid g(gg);
+    const int order = p->OrderReinitialisationBoundaries;
+    const bool enobc = p->ENOBCReinitialisation != 0;
+    /* interior-loop range (src/calc_NormGrad_d.F90:41-56) */
+    const int is = g.ia + (g.pb ? 1 : 0), ie = g.ib - (g.pf ? 1 : 0);
+    const int js = g.ja + (g.pl ? 1 : 0), je = g.jb - (g.pr ? 1 : 0);
+    const int ks = g.ka + (g.pd ? 1 : 0), ke = g.kb - (g.pu ? 1 : 0);
+    const double stale = phizero[g.id(ie, je, ke)];
+    const long st3[3] = {1, g.ni, g.ni * g.nj};
+    const double dd[3] = {g.dc, g.de, g.dz};
+    std::fill(ng, ng + g.n, 0.0);
+#pragma omp parallel for
+    for (int k = g.ka; k <= g.kb; ++k)
+        for (int j = g.ja; j <= g.jb; ++j)
+            for (int i = g.ia; i <= g.ib; ++i) {
+                const long l = g.id(i, j, k);
+                const int c[3] = {i, j, k};
+                const int lo[3] = {g.ia, g.ja, g.ka}, hi[3] = {g.ib, g.jb, g.kb};
+                const int sta[3] = {is, js, ks}, end[3] = {ie, je, ke};
+                const bool plo[3] = {g.pb, g.pl, g.pd}, phi_[3] = {g.pf, g.pr, g.pu};
+                const bool iface = (g.pb && i == g.ia) || (g.pf && i == g.ib);
+                const bool jface = (g.pl && j == g.ja) || (g.pr && j == g.jb);
+                const bool kface = (g.pd && k == g.ka) || (g.pu && k == g.kb);
+                const double phi0 = (iface && !jface && !kface) ? stale : phizero[l];
+                double d[3];
+                for (int m = 0; m < 3; ++m) {
+                    const long s = st3[m];
+                    if (plo[m] && c[m] == lo[m]) {
+                        d[m] = dd[m] * biased(phi[l], phi[l + s], phi[l + 2 * s], phi[l + 3 * s], order, 1, enobc);
+                    } else if (phi_[m] && c[m] == hi[m]) {
+                        d[m] = dd[m] * biased(phi[l], phi[l - s], phi[l - 2 * s], phi[l - 3 * s], order, -1, enobc);
+                    } else {
+                        const bool lob = plo[m] && c[m] == sta[m], hib = phi_[m] && c[m] == end[m];
+                        const double fLL = lob ? 0.0 : phi[l - 2 * s], fRR = hib ? 0.0 : phi[l + 2 * s];
+                        d[m] = dd[m] * eno2(phi0, fLL, phi[l - s], phi[l], phi[l + s], fRR, lob, hib);
+                    }
+                }
+                const double dx = csi[3 * l + 0] * d[0] + eta[3 * l + 0] * d[1] + zet[3 * l + 0] * d[2];
+                const double dy = csi[3 * l + 1] * d[0] + eta[3 * l + 1] * d[1] + zet[3 * l + 1] * d[2];
+                const double dz = csi[3 * l + 2] * d[0] + eta[3 * l + 2] * d[1] + zet[3 * l + 2] * d[2];
+                ng[l] = std::sqrt(dx * dx + dy * dy + dz * dz);
+            }
+    return LSM_OK;
+}
+
+/* reinitialisation_test2, src/reinitialisation_test2.F90:1-221 (non-hybrid) */
+int oracle_reinitialisation_test2(const lsm_grid* gg, const lsm_params* p, const double* phizero,
+                                  const double* csi, const double* eta, const double* zet, double* out,
+                                  int* iterations) {
+    int st = check_grid(gg); if (st) return st;
+    Grid g(gg);
+    const double eps = p->epslsm, epsr = p->epsReinitialisation, dt = p->RNtimestep;
+    const double C[3][3] = {{1.0, 0.0, 1.0}, {3.0 / 4.0, 1.0 / 4.0, 1.0 / 4.0}, {1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0}};
+    std::vector<double> sg(g.n), dn(g.n), dn1(phizero, phizero + g.n), ng(g.n, 0.0), ngc(g.n, 0.0);
+    for (long l = 0; l < g.n; ++l) sg[l] = sign_phi0(phizero[l], eps);
+    st = oracle_calc_normgrad_d(gg, p, dn1.data(), phizero, csi, eta, zet, ng.data());
+    if (st) return st;
+    int done = 0;
+    for (int it = 1; it <= p->RNitermax; ++it) {
+        const double mx = *std::max_element(ng.begin(), ng.end()), mn = *std::min_element(ng.begin(), ng.end());
+        if (std::fabs(mx - 1.0) < epsr && std::fabs(mn - 1.0) < epsr) break;
+        dn = dn1;
+        oracle_calc_normgrad_d(gg, p, dn.data(), phizero, csi, eta, zet, ngc.data());
+        for (int rk = 0; rk < 3; ++rk) {
+            oracle_calc_normgrad_d(gg, p, dn1.data(), phizero, csi, eta, zet, ng.data());
+#pragma omp parallel for
+            for (int k = g.ka; k <= g.kb; ++k)
+                for (int j = g.ja; j <= g.jb; ++j)
+                    for (int i = g.ia; i <= g.ib; ++i) {
+                        const long l = g.id(i, j, k);
+                        if (ngc[l] - 1.0 > epsr) {
+                            double rhs = sg[l] * (ng[l] - 1.0);
+                            const double lam = lambda_mass(dn1[l], sg[l], ng[l], eps);
+                            const double aux = deltaf(dn1[l], eps) * ng[l];
+                            rhs = rhs - lam * aux;
+                            dn1[l] = C[rk][0] * dn[l] + C[rk][1] * dn1[l] - C[rk][2] * dt * rhs;
+                        }
+                    }
+        }
+        done = it;
+    }
+    if (iterations) *iterations = done;
+    std::memcpy(out, dn1.data(), sizeof(double) * g.n);
+    return LSM_OK;
+}
+
 /* ------------------------------------------------------------------ A0 --- */
 /* levelsetmethod, src/levelsetmethod.F90:1-372, Sussman-Fatemi branch
-   (hybrid_reinitialisation = .false.) with `reinitialization` as the
+   (hybrid_reinitialisation = .false.) with `reinitialization` (reinit_scheme
+   0) or the live `reinitialisation_test2` (reinit_scheme 1) as the
    reinitialisation routine. */
 int oracle_levelsetmethod_x(const lsm_grid* gg, const lsm_params* p, const double* q, const double* csi,
                             const double* eta, const double* zet, const double* aj, double* phi,
                             const double* phin, const double* x, const double* y, const double* z, int iter,
                             double* vols, lsm_exchange_fn fn, void* user) {
     int st = check_grid(gg); if (st) return st;
-    if (p->hybrid_reinitialisation || p->reinit_scheme != 0 || p->sussman_correction_method != 0)
+    if (p->hybrid_reinitialisation || p->reinit_scheme < 0 || p->reinit_scheme > 1 ||
+        p->sussman_correction_method != 0)
         return LSM_ERR_UNSUPPORTED;
     Grid g(gg);
     Exch ex{fn, user, gg};
@@ -954,7 +1143,8 @@ int oracle_levelsetmethod_x(const lsm_grid* gg, const lsm_params* p, const doubl
         }
     }
     if (p->call_reinitialisation && p->RNfreq > 0 && iter % p->RNfreq == 0) {
-        oracle_reinitialization_x(gg, p, phi, csi, eta, zet, pc.data(), fn, user);
+        if (p->reinit_scheme == 1) oracle_reinitialisation_test2(gg, p, phi, csi, eta, zet, pc.data(), nullptr);
+        else oracle_reinitialization_x(gg, p, phi, csi, eta, zet, pc.data(), fn, user);
         bcond(g, p, pc.data());
         std::memcpy(phi, pc.data(), sizeof(double) * g.n);
         ex(phi);

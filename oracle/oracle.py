@@ -47,7 +47,8 @@ class Params(C.Structure):
                 ("TotalVolumeComputation", C.c_int), ("GlobalMassCorrection", C.c_int),
                 ("BigPhi", C.c_double), ("epsReinitialisation", C.c_double),
                 ("M_Sphi0", C.c_int), ("reinit_scheme", C.c_int),
-                ("write_global_volume", C.c_int)]
+                ("write_global_volume", C.c_int), ("OrderReinitialisationBoundaries", C.c_int),
+                ("ENOBCReinitialisation", C.c_int)]
 
 
 def make_grid(ni, nj, nk, igp=0, jgp=0, kgp=0, physical=(1, 1, 1, 1, 1, 1), dc=1.0, de=1.0, dz=1.0):
@@ -85,6 +86,8 @@ def make_params(**kw):
     p.M_Sphi0 = 1
     p.reinit_scheme = 0
     p.write_global_volume = 0
+    p.OrderReinitialisationBoundaries = 1
+    p.ENOBCReinitialisation = 0
     for k, v in kw.items():
         if k == "btype_lsm":
             for f in range(6):
@@ -125,6 +128,8 @@ class Oracle:
             "oracle_calc_rh_rn": [_GP, _D, _D, _D, _D, _D, _D],
             "oracle_calc_lambda_rn": [_GP, _PP, _D, _D, _D, C.c_double, _D],
             "oracle_reinitialization": [_GP, _PP, _D, _D, _D, _D, _D],
+            "oracle_calc_normgrad_d": [_GP, _PP, _D, _D, _D, _D, _D, _D],
+            "oracle_reinitialisation_test2": [_GP, _PP, _D, _D, _D, _D, _D, C.POINTER(C.c_int)],
             "oracle_narrowband": [_GP, _PP, _D, _I],
             "oracle_get_gfm_list": [_GP, _PP, _D, C.POINTER(C.c_int), vp, C.c_int],
             "oracle_total_water_volume": [_GP, _D, _D, _D, _D, _D, vp],
@@ -193,6 +198,20 @@ class Oracle:
         out = np.zeros(phi0.shape, order="F")
         self._chk(self.lib.oracle_reinitialization(C.byref(g), C.byref(p), phi0, csi, eta, zet, out), "reinit")
         return out
+
+    def calc_normgrad_d(self, g, p, phi, phizero, csi, eta, zet):
+        out = np.zeros(phi.shape, order="F")
+        self._chk(self.lib.oracle_calc_normgrad_d(C.byref(g), C.byref(p), phi, phizero, csi, eta, zet, out),
+                  "normgrad_d")
+        return out
+
+    def reinitialisation_test2(self, g, p, phizero, csi, eta, zet):
+        """-> (phi reinitialised, pseudo-time iterations run)"""
+        out = np.zeros(phizero.shape, order="F")
+        it = C.c_int(0)
+        self._chk(self.lib.oracle_reinitialisation_test2(C.byref(g), C.byref(p), phizero, csi, eta, zet, out,
+                                                         C.byref(it)), "reinitialisation_test2")
+        return out, it.value
 
     def narrowband(self, g, p, phin):
         nb = np.zeros(phin.shape, dtype=np.int32, order="F")

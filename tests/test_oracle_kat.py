@@ -209,3 +209,76 @@ def test_rk3_translation_accuracy(oracle):
         cur = oracle.ad_rktvd3(g, p, cur, u, aj)
     exact = 0.1 * np.sin(2 * np.pi * (x - 10 * dt))
     assert np.abs(cur - exact)[4:-4].max() < 5e-3   # WENO3 clips the extrema slightly
+
+
+# ---------------------------------------------------------------- live Sussman reinit
+@pytest.mark.parametrize("order,enobc", [(1, 0), (2, 0), (2, 1), (3, 0)])
+def test_normgrad_d_exact_on_linear_data(oracle, order, enobc):
+    """ENO2 (interior), BiasedDerivative orders 1-3 and ENO2Boundary
+    (physical faces, edges, corners) are exact on linear data."""
+    n = 9
+    g, x, y, z, _, _ = _cart(n)
+    csi, eta, zet, aj = oracle.mg_metrics(g, x, y, z)
+    phi = cases.F(0.3 * x + 0.4 * y - 1.2 * z + 0.1)
+    p = O.make_params(epslsm=0.2, OrderReinitialisationBoundaries=order, ENOBCReinitialisation=enobc)
+    ng = oracle.calc_normgrad_d(g, p, phi, phi, csi, eta, zet)
+    assert np.allclose(ng, math.sqrt(0.3 ** 2 + 0.4 ** 2 + 1.2 ** 2), rtol=1e-12, atol=0)
+
+
+def test_normgrad_d_second_order_on_quadratic(oracle):
+    """Interior ENO2 = central difference on a quadratic (exact); second- and
+    third-order one-sided derivatives are exact on the faces too."""
+    n = 9
+    g, x, y, z, _, _ = _cart(n)
+    csi, eta, zet, aj = oracle.mg_metrics(g, x, y, z)
+    phi = cases.F(x * x + 0.5)
+    for order in (2, 3):
+        p = O.make_params(epslsm=0.2, OrderReinitialisationBoundaries=order)
+        ng = oracle.calc_normgrad_d(g, p, phi, phi, csi, eta, zet)
+        assert np.allclose(ng, 2 * x, rtol=1e-11, atol=1e-12)
+
+
+def test_reinitialisation_test2_exits_on_signed_distance(oracle):
+    """A planar signed distance has |grad phi| = 1 at every node: the first
+    convergence test exits before any pseudo-step and phi is unchanged."""
+    n = 9
+    g, x, y, z, _, _ = _cart(n)
+    csi, eta, zet, aj = oracle.mg_metrics(g, x, y, z)
+    phi = cases.F(0.6 * x + 0.8 * z - 0.5)
+    p = O.make_params(epslsm=0.2, RNitermax=10, RNtimestep=0.01, epsReinitialisation=1e-8)
+    out, iters = oracle.reinitialisation_test2(g, p, phi, csi, eta, zet)
+    assert iters == 0 and np.array_equal(out, phi)
+
+
+def test_reinitialisation_test2_masks_nodes_below_one(oracle):
+    """Only nodes whose |grad d| exceeds 1 + epsReinitialisation move
+    (src/reinitialisation_test2.F90:146): a field with |grad phi| = 0.5
+    everywhere is never updated, whatever the iteration count."""
+    n = 9
+    g, x, y, z, _, _ = _cart(n)
+    csi, eta, zet, aj = oracle.mg_metrics(g, x, y, z)
+    phi = cases.F(0.5 * (y - 0.45))
+    p = O.make_params(epslsm=0.2, RNitermax=5, RNtimestep=0.01, epsReinitialisation=1e-5)
+    out, iters = oracle.reinitialisation_test2(g, p, phi, csi, eta, zet)
+    assert iters == 5 and np.array_equal(out, phi)
+
+
+def test_normgrad_d_i_faces_use_the_last_interior_phi0(oracle):
+    """The two i-face blocks of calc_NormGrad_d never assign phi0, so their
+    ENO2 stencil choice takes phizero of the last interior node: flipping
+    phizero there (and only there) changes the i-face gradients of a field
+    whose ENO2 choices differ by sign, and nothing else."""
+    n = 9
+    g, x, y, z, _, _ = _cart(n)
+    csi, eta, zet, aj = oracle.mg_metrics(g, x, y, z)
+    d = cases.F(np.abs(y - 0.5) + 0.3 * (z - 0.5) ** 2)   # kink: ENO2 sides differ
+    p = O.make_params(epslsm=0.2)
+    pz = cases.F(np.ones_like(d))
+    a = oracle.calc_normgrad_d(g, p, d, pz, csi, eta, zet)
+    pz2 = cases.F(pz.copy())
+    pz2[n - 2, n - 2, n - 2] = -1.0          # last node of the interior loop
+    b = oracle.calc_normgrad_d(g, p, d, pz2, csi, eta, zet)
+    diff = a != b
+    iface = np.zeros_like(diff)
+    iface[[0, n - 1], 1:n - 1, 1:n - 1] = True
+    assert diff.any() and not (diff & ~iface & ~(np.indices(diff.shape) == n - 2).all(0)).any()
