@@ -24,7 +24,8 @@ step, forward only.
 
 "fp64" workload: the curvilinear solitary-wave case, 256 x 128 x 96 nodes,
 10 reinitialisation pseudo-steps per step, through `lsm_levelsetmethod` in
-the reference's FP64 arithmetic.
+the reference's FP64 arithmetic.  "sussman": the same with the
+reference's live reinitialisation (`reinitialisation_test2`, reinit_scheme 1).
 
 Metric: Gcell-steps/s = grid nodes x physical steps / second (whole job;
 for "fwdadj" each cell-step is forward + adjoint).
@@ -64,6 +65,9 @@ ALGO_WORDS = {
     "volume_kernel": 4.0,            # phi, x, y, z
     "bc_full_kernel": 2.0,
     "copy_kernel": 2.0,
+    "normgrad_d_kernel": 12.0,       # phi, phizero, metrics(9); |grad phi|
+    "sussman_rk_kernel": 6.0,        # dn, dn1 (rmw), |grad|, |grad| at the iteration start, sign
+    "minmax_partial_kernel": 1.0,
 }
 
 
@@ -171,9 +175,20 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- workload
-def make_case(ni, nj, nk, reinit_iters):
+FP64_METRIC = {
+    0: "Gcell-steps/s (plain FP64 level-set step: WENO3-RK3 advection + reinitialisation + volume)",
+    1: "Gcell-steps/s (plain FP64 level-set step with the live Sussman reinitialisation: WENO3-RK3 advection + "
+       "reinitialisation_test2 + volume)",
+}
+FP64_REINIT = {0: "reinitialization", 1: "reinitialisation_test2, ENO2 gradients, TVD-RK3 pseudo time"}
+
+
+def make_case(ni, nj, nk, reinit_iters, scheme=0):
+    """scheme 0: `reinitialization`; 1: the reference's live `reinitialisation_test2`"""
     from nslsm import configs
-    return configs.solitary_wave(ni, nj, nk, reinit_iters=reinit_iters)
+    case = configs.solitary_wave(ni, nj, nk, reinit_iters=reinit_iters)
+    case.params = case.params.replace(reinit_scheme=scheme)
+    return case
 
 
 def prepare_device(case, ls, torch):
@@ -255,7 +270,10 @@ def cpu_oracle_time(case, steps, threads):
     smax = max(float(np.abs(m[0] * u[0] + m[1] * u[1] + m[2] * u[2]).max()) for m in (csi, eta, zet))
     cp = case.params
     p = O.make_params(epslsm=cp.epslsm, delti_lsm=case.cfl / smax, RNitermax=cp.RNitermax,
-                      RNtimestep=cp.RNtimestep, isnarrow=cp.isnarrow, narrowcoef=cp.narrowcoef)
+                      RNtimestep=cp.RNtimestep, isnarrow=cp.isnarrow, narrowcoef=cp.narrowcoef,
+                      reinit_scheme=cp.reinit_scheme, epsReinitialisation=cp.epsReinitialisation,
+                      OrderReinitialisationBoundaries=cp.OrderReinitialisationBoundaries,
+                      ENOBCReinitialisation=int(cp.ENOBCReinitialisation))
     phi = case.phi0
     t0 = time.perf_counter()
     for it in range(1, steps + 1):
@@ -741,7 +759,8 @@ def run_fp64(args):
     rank, world = dist_setup(args.gpus)
     dev_index = torch.cuda.current_device()
     W = workload(args)
-    case = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"])
+    scheme = 1 if args.workload == "sussman" else 0
+    case = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"], scheme)
     case.redistance_iters = W["redistance"]
     n = case.grid.n
     ls = LevelSet(device=dev_index)
@@ -822,7 +841,7 @@ def run_fp64(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        sample = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"])
+        sample = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"], scheme)
         threads = host_threads()
         sec, used = cpu_oracle_time(sample, 1, threads)
         cpu = {"value": n / sec / 1e9, "unit": "Gcell-steps/s", "cores": used, "kind": "port",
@@ -830,13 +849,13 @@ def run_fp64(args):
                          "phi0 not redistanced)" % used}
     if rank == 0:
         line = {
-            "metric": "Gcell-steps/s (plain FP64 level-set step: WENO3-RK3 advection + reinitialisation + volume)",
+            "metric": FP64_METRIC[scheme],
             "value": value, "unit": "Gcell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (analytic solitary-wave workload; the reference ships no decks)",
             "config": {"workload": "solitary_wave curvilinear %dx%dx%d, CFL 0.4, WENO3+TVD-RK3, %d reinit "
-                                   "pseudo-steps/step, volume each step" % (W["ni"], W["nj"], W["nk"],
-                                                                            W["reinit_iters"]),
+                                   "pseudo-steps/step (%s), volume each step"
+                                   % (W["ni"], W["nj"], W["nk"], W["reinit_iters"], FP64_REINIT[scheme]),
                        "nodes": n, "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "inputs larger than L2 (working set %.2f GB > 129 MB)" % (n * 8 * 30 / 1e9)},
             "roofline": roof,
@@ -861,7 +880,8 @@ def run_reference(args):
     if args.workload == "fwdadj":
         return run_reference_fwdadj(args, world)
     W = workload(args)
-    case = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"])
+    scheme = 1 if args.workload == "sussman" else 0
+    case = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"], scheme)
     threads = host_threads()
     # warm-up (page-in, thread pool) then timed steps, each a full physical step
     cpu_oracle_time(case, max(1, min(args.warmup, 1)), threads)
@@ -870,11 +890,12 @@ def run_reference(args):
     v = case.grid.n / sec / 1e9
     line = {
         "impl": "reference",
-        "metric": "Gcell-steps/s (plain FP64 level-set step: WENO3-RK3 advection + reinitialisation + volume)",
+        "metric": FP64_METRIC[scheme],
         "value": v, "unit": "Gcell-steps/s", "n_gpus": world, "steps": steps, "warmup": 1,
         "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": {"workload": "solitary_wave curvilinear %dx%dx%d, %d reinit pseudo-steps/step"
-                                        % (W["ni"], W["nj"], W["nk"], W["reinit_iters"])},
+                                        " (%s)" % (W["ni"], W["nj"], W["nk"], W["reinit_iters"],
+                                                   FP64_REINIT[scheme])},
         "cpu_baseline": {"value": v, "unit": "Gcell-steps/s", "cores": used, "kind": "port",
                          "sample": "%d full physical steps; CPU FP64 restatement of the reference (the Fortran/MPI "
                                    "original cannot be built here: no Fortran compiler)" % steps},
@@ -983,7 +1004,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", default=None, help="NIxNJxNK instead of the workload's grid (profiling runs)")
-    ap.add_argument("--workload", choices=["fwdadj", "batched", "fp64"], default="fwdadj")
+    ap.add_argument("--workload", choices=["fwdadj", "batched", "fp64", "sussman"], default="fwdadj")
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--n-inst", type=int, default=None, help="instances of the batched workload (profiling runs)")
     args = ap.parse_args()
