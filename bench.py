@@ -674,10 +674,17 @@ def run_fwdadj(args):
     # 4-step segment, per cell-step, at the measured throughput
     seg_bytes = sum(FWDADJ_BYTES[k] * n * v[0] for k, v in prof.items() if k in FWDADJ_BYTES)
     per_cell_step = seg_bytes / (4.0 * n)
+    # the survey's accounting of the same step (each distinct array of the
+    # reference's formulation read and written once per pass): forward
+    # 53 + 14R words, adjoint 131 + 32R words, FP32
+    survey_bytes = (184 + 46 * R) * 4.0
     step_roof = {"algorithmic_bytes_per_cell_step": per_cell_step,
                  "achieved_gbs": per_cell_step * value,
                  "frac": per_cell_step * value / roof["peak"],
-                 "note": "segment of 4 steps profiled; the 20-step segment's checkpoint copy is 0.4 B/cell-step"}
+                 "survey_accounting": {"bytes_per_cell_step": survey_bytes,
+                                       "frac": survey_bytes * value / roof["peak"]},
+                 "note": "bytes: the launches of a profiled 4-step segment, each kernel's own algorithmic bytes; "
+                         "the 20-step segment's checkpoint copy adds 0.4 B/cell-step"}
 
     # ---- end to end through the C-ABI with host (pinned) arrays
     def pinned(a):

@@ -134,9 +134,12 @@ __device__ __forceinline__ void rec3_grad(T fL, T fC, T fR, T* dL, T* dC, T* dR)
 // the first / last interior node (calc_RH_AD_WENO3.F90:201-245).
 template <typename T>
 __device__ __forceinline__ T weno_diff(T m2, T m1, T c, T p1, T p2, T w, bool lo, bool hi) {
+    // the stencils are selected first so that each face costs one
+    // reconstruction (no evaluation of the branch not taken)
     const bool up = w > T(0);
-    const T fp = (up || hi) ? rec3(m1, c, p1) : rec3(p2, p1, c);
-    const T fm = (up && !lo) ? rec3(m2, m1, c) : rec3(p1, c, m1);
+    const bool P = up || hi, M = up && !lo;
+    const T fp = rec3(P ? m1 : p2, P ? c : p1, P ? p1 : c);
+    const T fm = rec3(M ? m2 : p1, M ? m1 : c, M ? c : m1);
     return fp - fm;
 }
 
