@@ -508,6 +508,8 @@ def batch_cpu_baseline(meta, R):
 def run_ours(args):
     if args.workload == "fwdadj":
         return run_fwdadj(args)
+    if args.workload == "adjcheck":
+        return run_adjcheck(args)
     if args.workload == "batched":
         return run_batched(args)
     return run_fp64(args)
@@ -886,6 +888,9 @@ def run_reference(args):
         return run_reference_batched(args, world)
     if args.workload == "fwdadj":
         return run_reference_fwdadj(args, world)
+    if args.workload == "adjcheck":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no adjoint"}))
+        return
     W = workload(args)
     scheme = 1 if args.workload == "sussman" else 0
     case = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"], scheme)
@@ -964,6 +969,148 @@ def run_reference_batched(args, world):
     print(json.dumps(line))
 
 
+def run_adjcheck(args):
+    """The adjoint configuration: 128^3 unit box, sphere r = 0.15 at (0.35,
+    0.35, 0.35), LeVeque deformation field (frozen at t = 0 over the run),
+    50 steps of WENO3-RK3 + 5 reinitialisation pseudo-steps, eps = 1.5 h;
+    loss = sum (H_eps(phi_T) - H_eps(phi_target))^2 with phi_target from a
+    run with the velocity scaled by 1.05; gradients with respect to phi0
+    and the velocity by the hand-written adjoint with a checkpoint every 10
+    steps, FP64 then FP32.  Checks: central differences of the FP64 forward
+    along 16 seeded directions (step 1e-6; a direction whose difference
+    quotient changes between steps h and h/2 crossed a branch point and is
+    not scored), the FP32 gradient against the FP64 one, and the FP64 batch
+    gradient against the FP64 torch tape on a 32^3 copy (tests/lsm_tape.py).
+    value = the largest relative error against central differences."""
+    import torch
+    from nslsm import LevelSet, configs
+    from nslsm.batch import LevelSetBatch
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import lsm_tape as TAPE
+
+    NSTEPS, CKPT, R = 50, 10, 5
+
+    def H(p, e):
+        return torch.where(p < -e, torch.zeros_like(p), torch.where(p > e, torch.ones_like(p),
+                           0.5 * (1.0 + p / e + torch.sin(np.pi * p / e) / np.pi)))
+
+    def dH(p, e):
+        return torch.where(p.abs() > e, torch.zeros_like(p), (1.0 + torch.cos(np.pi * p / e)) / (2.0 * e))
+
+    def setup(n):
+        case = configs.sphere_deformation(n, reinit_iters=R)
+        g = case.grid
+        ls = LevelSet(device=0)
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(np.asfortranarray(a).T)).cuda()  # noqa: E731
+        x, y, z = dev(case.x), dev(case.y), dev(case.z)
+        csi, eta, zet, aj = ls.mg_metrics(g, x, y, z)
+        q = dev(case.q(0.0))
+        smax = max(float((m * q[..., 1:4]).sum(-1).abs().max()) for m in (csi, eta, zet))
+        dt = case.cfl / smax
+        ls.close()
+        return dict(case=case, g=g, x=x, y=y, z=z, csi=csi, eta=eta, zet=zet, q=q, phi0=dev(case.phi0), dt=dt)
+
+    def batch(S, prec):
+        c = S["case"]
+        b = LevelSetBatch([(S["g"].ni, S["g"].nj, S["g"].nk, S["dt"], c.params.RNtimestep, c.params.epslsm)],
+                          RNitermax=R, btype=(1,) * 6, BigPhi=5.0, precision=prec, autotune=False)
+        b.set_geometry(0, S["x"], S["y"], S["z"], S["csi"], S["eta"], S["zet"])
+        return b
+
+    def forward(b, phi0, q):
+        b.set_velocity(0, q)
+        b.set_phi(0, phi0)
+        b.step(NSTEPS, volumes=False)
+        return b.get_phi(0, like=phi0)
+
+    def adjoint(b, S, phi0, q, target):
+        eps = S["case"].params.epslsm
+        b.set_velocity(0, q)
+        b.set_phi(0, phi0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.forward_record(NSTEPS, CKPT)
+        phiT = b.get_phi(0, like=phi0)
+        seed = 2.0 * (H(phiT, eps) - H(target, eps)) * dH(phiT, eps)
+        b.set_grad_phi(0, seed)
+        b.backward()
+        gphi, gq = b.get_grad_phi0(0, like=phi0), b.get_grad_velocity(0, like=phi0)
+        torch.cuda.synchronize()
+        return gphi, gq, time.perf_counter() - t0
+
+    S = setup(128)
+    eps = S["case"].params.epslsm
+    b64 = batch(S, "fp64")
+    target = forward(b64, S["phi0"], 1.05 * S["q"])
+    loss = lambda phi0, q: float(((H(forward(b64, phi0, q), eps) - H(target, eps)) ** 2).sum())  # noqa: E731
+    gphi, gq, t64 = adjoint(b64, S, S["phi0"], S["q"], target)
+    # the forward map is piecewise smooth: the band test |phi| < eps of the
+    # sign field and the upwind / Godunov selections switch along the way, so
+    # a perturbation crosses some switches with a probability that grows with
+    # the step; both the config's step and a smaller one are reported
+    fd = {}
+    for h in (1e-6, 1e-8):
+        gen = torch.Generator(device="cuda").manual_seed(7)
+        worst, scored, skipped, rows = 0.0, 0, 0, []
+        for d in range(16):
+            v = torch.randn(S["phi0"].shape if d % 2 == 0 else S["q"].shape, generator=gen, dtype=torch.float64,
+                            device="cuda")
+            if d % 2 == 0:
+                f = lambda t: loss(S["phi0"] + t * v, S["q"])  # noqa: E731
+                an = float((gphi * v).sum())
+            else:
+                v[..., 0] = 0.0
+                f = lambda t: loss(S["phi0"], S["q"] + t * v)  # noqa: E731
+                an = float((gq * v).sum())
+            fd1 = (f(h) - f(-h)) / (2 * h)
+            fd2 = (f(0.5 * h) - f(-0.5 * h)) / h
+            rows.append([d, an, fd1, fd2])
+            if abs(fd1 - fd2) > 1e-3 * max(abs(fd1), abs(fd2), 1e-300):
+                skipped += 1
+                continue
+            scored += 1
+            worst = max(worst, abs(an - fd1) / max(abs(fd1), abs(an), 1e-300))
+        fd["%g" % h] = {"directions_scored": scored, "directions_skipped": skipped,
+                        "max_rel_err": worst if scored else None, "directions": rows}
+    b64.close()
+    b32 = batch(S, "fp32")
+    g32phi, g32q, t32 = adjoint(b32, S, S["phi0"], S["q"], target)
+    b32.close()
+    rel = lambda a, r: float((a - r).norm() / r.norm())  # noqa: E731
+    fp32_vs_fp64 = {"grad_phi0": rel(g32phi, gphi), "grad_q": rel(g32q, gq)}
+
+    # FP64 torch tape on a 32^3 copy
+    T = setup(32)
+    bt = batch(T, "fp64")
+    tgt = forward(bt, T["phi0"], 1.05 * T["q"])
+    gp, gqq, _ = adjoint(bt, T, T["phi0"], T["q"], tgt)
+    bt.close()
+    M = [m[..., c].contiguous() for m in (T["csi"], T["eta"], T["zet"]) for c in range(3)]
+    p0 = T["phi0"].clone().requires_grad_(True)
+    qq = T["q"].clone().requires_grad_(True)
+    cp = T["case"].params
+    out = TAPE.run(p0, qq, M, T["dt"], cp.RNtimestep, cp.epslsm, R, NSTEPS)
+    ((H(out, cp.epslsm) - H(tgt, cp.epslsm)) ** 2).sum().backward()
+    tape = {"grad_phi0": rel(gp, p0.grad), "grad_q": rel(gqq, qq.grad)}
+    n = S["g"].n
+    line = {
+        "metric": "adjoint check: largest relative error of the FP64 adjoint against central differences "
+                  "(16 seeded directions, step 1e-6)",
+        "value": fd["1e-06"]["max_rel_err"], "unit": "relative error", "n_gpus": 1, "steps": NSTEPS, "warmup": 0, "ms_per_step": None,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (analytic sphere and deformation field)",
+        "config": {"workload": "sphere in the deformation field, 128^3, %d steps, %d reinit pseudo-steps/step, "
+                               "Heaviside loss against a 1.05x-velocity target, checkpoint every %d steps"
+                               % (NSTEPS, R, CKPT), "nodes": n},
+        "fd": dict(fd, bar=1e-4, skip_rule="difference quotients at h and h/2 differ by more than 1e-3"),
+        "fp32_vs_fp64": fp32_vs_fp64,
+        "tape_32cubed": tape,
+        "adjoint_seconds": {"fp64": t64, "fp32": t32},
+        "fwdadj_gcell_steps_per_s": {"fp64": n * NSTEPS / t64 / 1e9, "fp32": n * NSTEPS / t32 / 1e9},
+    }
+    print(json.dumps(line))
+
+
 def run_reference_fwdadj(args, world):
     """The CPU FP64 restatement of the reference (all host threads) on the
     large free-surface grid: each timed step is one physical forward step of
@@ -1011,7 +1158,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", default=None, help="NIxNJxNK instead of the workload's grid (profiling runs)")
-    ap.add_argument("--workload", choices=["fwdadj", "batched", "fp64", "sussman"], default="fwdadj")
+    ap.add_argument("--workload", choices=["fwdadj", "batched", "fp64", "sussman", "adjcheck"], default="fwdadj")
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--n-inst", type=int, default=None, help="instances of the batched workload (profiling runs)")
     args = ap.parse_args()

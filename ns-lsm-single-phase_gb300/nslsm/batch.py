@@ -27,6 +27,17 @@ from . import _lib
 from .api import _addr, _is_torch, Grid
 
 
+def _torch_sync(*arrays) -> None:
+    """The batch runs on its own stream: work torch has queued on its current
+    stream for these tensors (producing an input, zero-filling an output)
+    must finish before the library touches them."""
+    for a in arrays:
+        if a is not None and _is_torch(a) and a.is_cuda:
+            import torch
+            torch.cuda.current_stream(a.device).synchronize()
+            return
+
+
 class LevelSetBatch:
     def __init__(self, instances: Sequence[Tuple[int, int, int, float, float, float]], RNitermax: int = 5,
                  btype: Sequence[int] = (1, 1, 1, 1, 1, 1), BigPhi: float = 5.0, device: int = 0, stream=None,
@@ -73,6 +84,7 @@ class LevelSetBatch:
 
     def set_geometry(self, k, x, y, z, csi, eta, zet):
         g = self.grids[k]
+        _torch_sync(x, y, z, csi, eta, zet)
         self._chk(self.lib.lsm_batch_set_geometry(self.h, k, _addr(x, g, 1, np.float64), _addr(y, g, 1, np.float64),
                                                   _addr(z, g, 1, np.float64), _addr(csi, g, 3, np.float64),
                                                   _addr(eta, g, 3, np.float64), _addr(zet, g, 3, np.float64)),
@@ -80,10 +92,12 @@ class LevelSetBatch:
 
     def set_velocity(self, k, q):
         g = self.grids[k]
+        _torch_sync(q)
         self._chk(self.lib.lsm_batch_set_velocity(self.h, k, _addr(q, g, 4, np.float64)), "lsm_batch_set_velocity")
 
     def set_phi(self, k, phi):
         g = self.grids[k]
+        _torch_sync(phi)
         self._chk(self.lib.lsm_batch_set_phi(self.h, k, _addr(phi, g, 1, np.float64)), "lsm_batch_set_phi")
 
     def get_phi(self, k, like=None):
@@ -91,6 +105,7 @@ class LevelSetBatch:
         if like is not None and _is_torch(like):
             import torch
             out = torch.zeros((g.nk, g.nj, g.ni), dtype=torch.float64, device=like.device)
+            _torch_sync(out)
         else:
             out = np.zeros(g.shape, order="F")
         self._chk(self.lib.lsm_batch_get_phi(self.h, k, _addr(out, g, 1, np.float64)), "lsm_batch_get_phi")
@@ -109,6 +124,7 @@ class LevelSetBatch:
 
     def set_grad_phi(self, k, grad):
         g = self.grids[k]
+        _torch_sync(grad)
         self._chk(self.lib.lsm_batch_set_grad_phi(self.h, k, _addr(grad, g, 1, np.float64)), "lsm_batch_set_grad_phi")
 
     def backward(self):
@@ -119,7 +135,9 @@ class LevelSetBatch:
         if like is not None and _is_torch(like):
             import torch
             shp = (g.nk, g.nj, g.ni) + ((ncomp,) if ncomp > 1 else ())
-            return torch.zeros(shp, dtype=torch.float64, device=like.device)
+            out = torch.zeros(shp, dtype=torch.float64, device=like.device)
+            _torch_sync(out)
+            return out
         return np.zeros(((ncomp,) if ncomp > 1 else ()) + g.shape, order="F")
 
     def get_grad_phi0(self, k, like=None):

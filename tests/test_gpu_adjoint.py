@@ -186,3 +186,19 @@ def test_autograd_function_matches_direct_calls(adj_cases):
         assert np.array_equal(np.asfortranarray(phis[k].grad.cpu().numpy().T), gphi[k])
         assert np.array_equal(np.asfortranarray(qs[k].grad.cpu().numpy().T), gq[k])
     b.close()
+
+
+def test_batch_waits_for_torch_stream(adj_cases):
+    """Inputs produced by torch on its current stream are read only after
+    torch has written them (the batch runs on its own stream)."""
+    c = adj_cases[0]
+    b = _batch([c], 2)
+    base = T.to_torch(c["it"].phi0, "cuda")
+    for r in range(20):
+        x = base.clone()
+        for _ in range(50):          # a queue of kernels still running when set_phi is called
+            x = x * 1.0000001 + 1e-9
+        b.set_phi(0, x)
+        got = b.get_phi(0, like=base)
+        assert torch.equal(got, x), r
+    b.close()
