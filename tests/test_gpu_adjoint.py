@@ -202,3 +202,42 @@ def test_batch_waits_for_torch_stream(adj_cases):
         got = b.get_phi(0, like=base)
         assert torch.equal(got, x), r
     b.close()
+
+
+@pytest.mark.parametrize("btype", [(0, 2, 1, 0, 1, 0), (2, 2, 0, 0, 2, 1)])
+def test_adjoint_other_boundary_types_match_tape(oracle, adj_cases, btype):
+    """bcond_lsm types 0 (copy) and 2 (linear extrapolation on im; ignored on
+    the other faces, as in the reference) in the forward against the oracle
+    and in the adjoint against the torch tape."""
+    from nslsm.batch import LevelSetBatch
+    cases_ = adj_cases[:2]
+    R = 2
+    b = LevelSetBatch([(*c["it"].grid.shape, c["dt"], c["it"].dtau, c["it"].eps) for c in cases_], RNitermax=R,
+                      btype=btype, BigPhi=5.0, precision="fp64")
+    for k, c in enumerate(cases_):
+        it = c["it"]
+        b.set_geometry(k, it.x, it.y, it.z, c["csi"], c["eta"], c["zet"])
+        b.set_velocity(k, it.q)
+        b.set_phi(k, it.phi0)
+    b.step(NSTEPS)
+    for k, c in enumerate(cases_):
+        it = c["it"]
+        op = O.make_params(epslsm=it.eps, delti_lsm=c["dt"], RNitermax=R, RNtimestep=it.dtau, BigPhi=5.0,
+                           btype_lsm=btype)
+        phi = it.phi0
+        for s in range(1, NSTEPS + 1):
+            phi, _ = oracle.levelsetmethod(c["g"], op, it.q, c["csi"], c["eta"], c["zet"], c["aj"], phi, phi, it.x,
+                                           it.y, it.z, s)
+        assert float(np.abs(b.get_phi(k) - phi).max()) <= 1e-12
+    wts = _weights(cases_)
+    gphi, gq = _adjoint(b, cases_, wts)
+    b.close()
+    for k, c in enumerate(cases_):
+        it = c["it"]
+        M = T.metrics_torch(c["csi"], c["eta"], c["zet"], "cuda")
+        p = T.to_torch(it.phi0, "cuda").requires_grad_(True)
+        q = T.to_torch(it.q, "cuda").requires_grad_(True)
+        out = T.run(p, q, M, c["dt"], it.dtau, it.eps, R, NSTEPS, btype=btype)
+        (out * T.to_torch(wts[k], "cuda")).sum().backward()
+        assert _rel(gphi[k], np.asfortranarray(p.grad.cpu().numpy().T)) <= 1e-10
+        assert _rel(gq[k], np.asfortranarray(q.grad.cpu().numpy().T)) <= 1e-10

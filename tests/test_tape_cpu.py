@@ -91,3 +91,18 @@ def test_tape_gradient_matches_central_differences(tape_cases, R):
         n, worst = fd_check(lambda x: float(_loss(c, R, phi0, x, wts)), q, qq.grad, 16, 6, mask=qmask)
         assert n >= 12 and worst <= FD_TOL, (n, worst)
     assert float(qq.grad[..., 0].abs().max()) == 0.0
+
+
+@pytest.mark.parametrize("btype", [(0, 2, 1, 0, 1, 0), (2, 2, 0, 0, 2, 1)])
+def test_tape_forward_other_boundary_types(oracle, tape_cases, btype):
+    c = tape_cases[1]
+    it = c["it"]
+    op = O.make_params(epslsm=it.eps, delti_lsm=c["dt"], RNitermax=2, RNtimestep=it.dtau, BigPhi=5.0,
+                       btype_lsm=btype)
+    phi = it.phi0
+    for s in range(1, NSTEPS + 1):
+        phi, _ = oracle.levelsetmethod(c["g"], op, it.q, c["csi"], c["eta"], c["zet"], c["aj"], phi, phi, it.x,
+                                       it.y, it.z, s)
+    M = T.metrics_torch(c["csi"], c["eta"], c["zet"])
+    got = T.run(T.to_torch(it.phi0), T.to_torch(it.q), M, c["dt"], it.dtau, it.eps, 2, NSTEPS, btype=btype)
+    assert float((got - T.to_torch(phi)).abs().max()) <= 1e-13
