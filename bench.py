@@ -293,7 +293,7 @@ BATCH = dict(n_inst=64, lo=32, hi=96, seed=0, reinit_iters=5, cfl=0.5)
 
 # algorithmic HBM bytes per node for one launch of the batched FP32 kernels
 BATCH_ALGO_BYTES = {
-    "k_stage": 17.0 / 3.0 * 4,   # phi_prev, phi^n (stages 2-3), W(3); phi
+    "k_stage_z": 17.0 / 3.0 * 4,   # phi_prev, phi^n (stages 2-3), W(3); phi
     "k_reinit": 12.0 * 4,        # d, s, metrics(9); d
     "k_sign": 11.0 * 4,          # phi0, metrics(9); s
     "k_contra": 15.0 * 4,        # u(3), metrics(9); W(3)
@@ -522,7 +522,7 @@ FWDADJ = dict(ni=512, nj=256, nk=256, reinit_iters=10, segment=20, compare_steps
 # (each distinct array read once and written once; halos not counted)
 FWDADJ_BYTES = {
     "k_contra": 15 * 4,            # u(3), metrics(9); W(3)
-    "k_stage": 17.0 / 3.0 * 4,     # phi_prev, phi^n (stages 2-3), W(3); stage output
+    "k_stage_z": 17.0 / 3.0 * 4,     # phi_prev, phi^n (stages 2-3), W(3); stage output
     "k_sign": 11 * 4,              # phi0, metrics(9); s
     "k_reinit": 12 * 4,            # d, s, metrics(9); d
     "k_sign_reinit": 12 * 4,       # phi0, metrics(9); s, d

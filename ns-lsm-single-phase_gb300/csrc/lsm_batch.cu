@@ -11,8 +11,9 @@
 //   metrics 9; d), volume 3 (phi + 64-bit fixed-point cell volume).
 //
 // Arithmetic: the reference's formulas rearranged for the GPU (one division
-// per WENO3 reconstruction); the water volume is FP64 per cell with exact
-// 64-bit fixed-point sums.  The reinitialisation uses the closed form of the
+// per WENO3 reconstruction); the water volume sums FP64 hexahedron volumes
+// of the bulk water cells and the interface cells' shares (in the stencil
+// precision) with exact 64-bit fixed-point sums.  The reinitialisation uses the closed form of the
 // reference's method-0 lambda correction: with lambda = -(d1 - phi0) /
 // (dtau delta |grad phi0|) the correction dtau lambda delta |grad phi0|
 // returns d to phi0 wherever delta(phi0) |grad phi0| != 0, i.e.
@@ -93,6 +94,21 @@ __device__ __forceinline__ bool flat_node(const Flat& fl, long long t, Node* nd)
     nd->k = (int)(r / ((long long)I.ni * I.nj));
     nd->valid = true;
     return true;
+}
+
+// Brick `blk` of adjoint map `map`: instance and first node of its tile.
+struct ABrick {
+    int inst, i0, j0, k0;
+};
+__device__ __forceinline__ ABrick adj_brick(const Brick* __restrict__ bmap, int map, int blk) {
+    const int4 bk = __ldg(reinterpret_cast<const int4*>(bmap) + blk);
+    const AdjShape sh = adj_shape(map);
+    ABrick b;
+    b.inst = bk.x;
+    b.i0 = bk.y * sh.ox;
+    b.j0 = bk.z * sh.oy;
+    b.k0 = bk.w * sh.oz;
+    return b;
 }
 
 // ------------------------------------------------------------ WENO3
@@ -206,18 +222,99 @@ __device__ __forceinline__ T stage_rhs(const FieldsT<T>& f, const T* __restrict_
     return R;
 }
 
-template <typename T, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(TX * TY * TZ) k_stage(const Inst* __restrict__ inst,
-        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phin,
-        const T* __restrict__ phi1, T* __restrict__ out, T c1, T c2, T c3) {
-    for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
-        if (!b.valid) continue;
-        const Inst& I = inst[b.inst];
-        const long long l = I.off + b.i + (long long)I.ni * (b.j + (long long)I.nj * b.k);
-        const T pn = __ldg(phin + l), p1 = __ldg(phi1 + l);   // issued with the stencil loads
-        const T R = interior(I, b.i, b.j, b.k) ? stage_rhs(f, phi1, I, l, b.i, b.j, b.k) : T(0);
-        out[l] = c1 * pn + c2 * p1 - c3 * R;
+// RK stage on the tiles of adjoint map 2 (32 x 8 columns marching 32 planes
+// in k).  Each plane of phi1 is staged in shared memory with a two-node
+// halo in x and y (double-buffered, one barrier per plane: the x and y
+// stencils read it there); the z stencil is a five-plane register window.
+// Loads per node: phi1 once (plus the halo share), phi^n and W.  Same
+// arithmetic as stage_rhs.  Halo slots: threads 0..127 hold the y-halo rows
+// -2, -1, 8, 9 of the tile, threads 128..159 the x-halo columns -2, -1, 32,
+// 33 (the cross stencil needs no corners).
+constexpr int kStSX = 36, kStSY = 12;
+template <typename T>
+__global__ void __launch_bounds__(256) k_stage_z(const Inst* __restrict__ inst, const Brick* __restrict__ bmap,
+        int nb, FieldsT<T> f, const T* __restrict__ phin, const T* __restrict__ phi1, T* __restrict__ out, T c1, T c2,
+        T c3) {
+    __shared__ T pl[2][kStSY][kStSX];
+    const int t = threadIdx.x, tx = t & 31, ty = t >> 5;
+    int hx = 0, hy = 0;
+    if (t < 128) {
+        const int r = t >> 5;
+        hy = r < 2 ? r - 2 : r + 6;
+        hx = tx;
+    } else if (t < 160) {
+        const int u = t - 128, c = u & 3;
+        hy = u >> 2;
+        hx = c < 2 ? c - 2 : c + 30;
+    }
+    const bool has_h = t < 160;
+    unsigned ph = 0;   // buffer parity, continuous over the tiles of this CTA
+    for (int blk = blockIdx.x; blk < nb; blk += gridDim.x) {
+        const ABrick ab = adj_brick(bmap, 2, blk);
+        const Inst& I = inst[ab.inst];
+        const int ni = I.ni, nj = I.nj, nk = I.nk;
+        const long long sk = (long long)ni * nj;
+        const int i = ab.i0 + tx, j = ab.j0 + ty;
+        const int k0 = ab.k0, k1 = min(k0 + adj_shape(2).oz, nk);
+        const bool col = i < ni && j < nj;
+        const int gi = ab.i0 + hx, gj = ab.j0 + hy;
+        const bool hok = has_h && gi >= 0 && gi < ni && gj >= 0 && gj < nj;
+        const long long cb = I.off + i + (long long)ni * j;
+        const long long hb = I.off + gi + (long long)ni * gj;
+        const bool ij_int = i > 0 && i < ni - 1 && j > 0 && j < nj - 1;
+        auto own = [&](int k) { return col && k >= 0 && k < nk ? __ldg(phi1 + cb + sk * k) : T(0); };
+        T w0 = own(k0 - 2), w1 = own(k0 - 1), w2 = own(k0), w3 = own(k0 + 1), w4 = own(k0 + 2);
+        T hv = hok ? __ldg(phi1 + hb + sk * k0) : T(0);
+        T W0 = T(0), W1 = T(0), W2 = T(0), pn = T(0);
+        if (col) {
+            const long long l = cb + sk * k0;
+            W0 = __ldg(f.W[0] + l);
+            W1 = __ldg(f.W[1] + l);
+            W2 = __ldg(f.W[2] + l);
+            pn = __ldg(phin + l);
+        }
+        for (int k = k0; k < k1; ++k) {
+            // loads of plane k + 1 (window plane k + 3) go out first
+            const bool nx = k + 1 < k1;
+            const T w5 = nx ? own(k + 3) : T(0);
+            T hvn = T(0), W0n = T(0), W1n = T(0), W2n = T(0), pnn = T(0);
+            if (hok && nx) hvn = __ldg(phi1 + hb + sk * (k + 1));
+            if (col && nx) {
+                const long long l = cb + sk * (k + 1);
+                W0n = __ldg(f.W[0] + l);
+                W1n = __ldg(f.W[1] + l);
+                W2n = __ldg(f.W[2] + l);
+                pnn = __ldg(phin + l);
+            }
+            T (*P)[kStSX] = pl[ph & 1u];
+            ++ph;
+            P[ty + 2][tx + 2] = w2;
+            if (has_h) P[hy + 2][hx + 2] = hv;
+            __syncthreads();
+            if (col) {
+                T R = T(0);
+                if (ij_int && k > 0 && k < nk - 1) {
+                    const int x = tx + 2, y = ty + 2;
+                    R = W0 * weno_diff(i > 1 ? P[y][x - 2] : T(0), P[y][x - 1], w2, P[y][x + 1],
+                                       i < ni - 2 ? P[y][x + 2] : T(0), W0, i == 1, i == ni - 2);
+                    R = vfma(W1, weno_diff(j > 1 ? P[y - 2][x] : T(0), P[y - 1][x], w2, P[y + 1][x],
+                                           j < nj - 2 ? P[y + 2][x] : T(0), W1, j == 1, j == nj - 2), R);
+                    R = vfma(W2, weno_diff(k > 1 ? w0 : T(0), w1, w2, w3, k < nk - 2 ? w4 : T(0), W2, k == 1,
+                                           k == nk - 2), R);
+                }
+                out[cb + sk * k] = c1 * pn + c2 * w2 - c3 * R;
+            }
+            w0 = w1;
+            w1 = w2;
+            w2 = w3;
+            w3 = w4;
+            w4 = w5;
+            hv = hvn;
+            W0 = W0n;
+            W1 = W1n;
+            W2 = W2n;
+            pn = pnn;
+        }
     }
 }
 
@@ -475,25 +572,38 @@ __global__ void k_bc_reinit(const Inst* __restrict__ inst, int ninst, long long 
     dout[I.off + i + (long long)I.ni * (j + (long long)I.nj * k)] = bval_k<T>(bc, p0, I.ni, I.nj, I.nk, i, j, k);
 }
 
-// ------------------------------------------------------------ volume (FP64)
+// ------------------------------------------------------------ volume
 // Water volume of one tetrahedron of an interface cell: the same regions as
 // MarchingTetrahedron + GetWaterVolume (src/TetrahedronMethods.F90:26-954),
 // each sub-tetrahedron's share of the tetrahedron evaluated in barycentric
-// closed form: one FP64 determinant per tetrahedron instead of up to four
-// (equal in exact arithmetic, rounding differs).
-__device__ __forceinline__ double tet_water(const double (&V)[4][3], const double (&ph)[4]) {
-    const double TV = tetvol_fast(V[0], V[1], V[2], V[3]);
+// closed form: one determinant per tetrahedron instead of up to four
+// (equal in exact arithmetic, rounding differs).  G is the geometry type:
+// FP64 for the FP64 stencils, FP32 for the FP32 ones (vertices relative to
+// the cell's first vertex, see k_volume).
+template <typename G>
+__device__ __forceinline__ G tetvol_g(const G (&a)[3], const G (&b)[3], const G (&c)[3], const G (&d)[3]) {
+    const G u0 = b[0] - a[0], u1 = b[1] - a[1], u2 = b[2] - a[2];
+    const G v0 = c[0] - a[0], v1 = c[1] - a[1], v2 = c[2] - a[2];
+    const G w0 = d[0] - a[0], w1 = d[1] - a[1], w2 = d[2] - a[2];
+    const G t = w0 * (u1 * v2 - u2 * v1) + w1 * (u2 * v0 - u0 * v2) + w2 * (u0 * v1 - u1 * v0);
+    return fabs(t) * G(1.0 / 6.0);
+}
+
+template <typename G>
+__device__ __forceinline__ G tet_water(const G (&V)[4][3], const G (&ph)[4]) {
+    const G TV = tetvol_g(V[0], V[1], V[2], V[3]);
+    const G tiny = G(kTinyD);   // tiny(1d0); 0 in FP32, where every nonzero value exceeds it
     int s[4], nz = 0, fi = 0;
     bool allp = true, alln = true, allge = true, allle = true;
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-        s[v] = ph[v] > kTinyD ? 1 : (ph[v] < -kTinyD ? -1 : 0);
+        s[v] = ph[v] > tiny ? 1 : (ph[v] < -tiny ? -1 : 0);
         allp &= s[v] == 1; alln &= s[v] == -1; nz += s[v] == 0;
         allge &= s[v] >= 0; allle &= s[v] <= 0;
         if (s[v] == -1) fi |= 1 << v;
     }
     if (allp) return TV;
-    if (alln) return 0.0;
+    if (alln) return G(0);
     if (nz > 0 && (allge || allle)) {
         // the reference's zero-vertex cases: full or empty tetrahedron
         int water = -1;
@@ -510,18 +620,23 @@ __device__ __forceinline__ double tet_water(const double (&V)[4][3], const doubl
         } else if (nz == 3) {
             for (int v = 0; v < 4; ++v) if (s[v] != 0) { water = s[v] == 1; break; }
         }
-        return water == 0 ? 0.0 : TV;   // four zero vertices: full (FlagIndex 0)
+        return water == 0 ? G(0) : TV;   // four zero vertices: full (FlagIndex 0)
     }
     // one vertex isolated from the other three (cases 2/15, 3/14, 5/12, 9/8)
     int iso = -1;
     if (fi == 1 || fi == 14) iso = 0; else if (fi == 2 || fi == 13) iso = 1;
     else if (fi == 4 || fi == 11) iso = 2; else if (fi == 8 || fi == 7) iso = 3;
     if (iso >= 0) {
-        double fr = 1.0;
+        // prod_k p_iso / (p_iso - p_k) over one division (the differences
+        // all carry the sign of p_iso: no cancellation)
+        G num = G(1), den = G(1);
 #pragma unroll
         for (int k = 0; k < 4; ++k)
-            if (k != iso) fr *= ph[iso] / (ph[iso] - ph[k]);
-        const double AV = TV * fr;
+            if (k != iso) {
+                num *= ph[iso];
+                den *= ph[iso] - ph[k];
+            }
+        const G AV = TV * (num / den);
         return (s[iso] == -1) ? TV - AV : AV;   // isolated vertex negative: the rest is water
     }
     // two against two (cases 4/13, 6/11, 7/10): pair (A, B) as listed by the
@@ -530,58 +645,74 @@ __device__ __forceinline__ double tet_water(const double (&V)[4][3], const doubl
     if (fi == 3 || fi == 12) { A = 0; B = 1; C = 2; D = 3; }
     else if (fi == 5 || fi == 10) { A = 0; B = 2; C = 1; D = 3; }
     else { A = 1; B = 2; C = 0; D = 3; }
-    const double aC = ph[A] / (ph[A] - ph[C]), aD = ph[A] / (ph[A] - ph[D]);
-    const double bC = ph[B] / (ph[B] - ph[C]), bD = ph[B] / (ph[B] - ph[D]);
-    const double AV = TV * (aC * aD * (1.0 - bD) + aC * bD * (1.0 - bC) + bC * bD);
+    // with the edge fractions aX = pA / (pA - pX), bX = pB / (pB - pX) the
+    // share is aC aD (1 - bD) + aC bD (1 - bC) + bC bD; over the common
+    // denominator (pA - pC)(pA - pD)(pB - pC)(pB - pD), using 1 - bX =
+    // -pX / (pB - pX), it needs one division, and its three numerator terms
+    // share one sign (A, B on one side of the interface, C, D on the other)
+    const G pA = ph[A], pB = ph[B], pC = ph[C], pD = ph[D];
+    const G dAC = pA - pC, dAD = pA - pD, dBC = pB - pC, dBD = pB - pD;
+    const G num = pB * pB * dAC * dAD - pA * pA * pD * dBC - pA * pB * pC * dAD;
+    const G AV = TV * (num / (dAC * dAD * dBC * dBD));
     return (s[A] == -1) ? TV - AV : AV;
 }
 
 // CellAnalysis's split of an interface cell (src/TetrahedronMethods.F90:
-// 1823-2121): phase-change tetrahedra -> K, all-water tetrahedra -> S
-__device__ void cell_water_fast(const double (&P)[8], const double (&C)[8][3], double* K, double* S) {
-    double k = 0.0, s2 = 0.0;
+// 1823-2121): phase-change tetrahedra -> K, all-water tetrahedra -> S.
+// The classification runs in the phi type P (eps_sims = 2^-52 and +-1 are
+// exact in FP32, so its compares equal the FP64 ones on the same values),
+// the geometry in P as well, on vertex coordinates relative to the cell's
+// first vertex (C, formed in FP64 by the caller).
+template <typename P>
+__device__ void cell_water_fast(const P (&ph8)[8], const P (&C)[8][3], double* K, double* S) {
+    const P es = P(kEpsSims);
+    P k = P(0), s2 = P(0);
     bool pcc = false;
 #pragma unroll
-    for (int v = 0; v < 8; ++v) pcc |= fabs(P[v]) < kEpsSims;
+    for (int v = 0; v < 8; ++v) pcc |= fabs(ph8[v]) < es;
     if (!pcc) {
-        const double sg = copysign(1.0, P[0]);
+        const P sg = signbit(ph8[0]) ? P(-1) : P(1);   // copysign(1, phi)
         for (int v = 1; v < 8; ++v)
-            if (sg * P[v] < 0.0) { pcc = true; break; }
+            if (sg * ph8[v] < P(0)) { pcc = true; break; }
     }
     if (pcc) {
         for (int t = 0; t < 6; ++t) {
             bool pct = false, second = true;
-            const double pa = P[c_tets[t][0]];
-            if (pa <= kEpsSims) second = false;
-            if (fabs(pa) < kEpsSims) pct = true;
-            const double sg = copysign(1.0, pa);
+            const P pa = ph8[c_tets[t][0]];
+            if (pa <= es) second = false;
+            if (fabs(pa) < es) pct = true;
+            const P sg = signbit(pa) ? P(-1) : P(1);
             for (int v = 1; v < 4; ++v) {
-                const double pb = P[c_tets[t][v]];
-                if (sg * pb < 0.0 || fabs(pb) < kEpsSims) {
-                    if (pb <= kEpsSims) second = false;
+                const P pb = ph8[c_tets[t][v]];
+                if (sg * pb < P(0) || fabs(pb) < es) {
+                    if (pb <= es) second = false;
                     pct = true;
                 }
             }
             if (!pct && !second) continue;
-            double V[4][3], ph[4];
+            P V[4][3], ph[4];
             for (int v = 0; v < 4; ++v) {
                 const int cv = c_tets[t][v];
                 V[v][0] = C[cv][0]; V[v][1] = C[cv][1]; V[v][2] = C[cv][2];
-                ph[v] = P[cv];
+                ph[v] = ph8[cv];
             }
             if (pct) k += tet_water(V, ph);
-            else s2 += tetvol_fast(V[0], V[1], V[2], V[3]);
+            else s2 += tetvol_g(V[0], V[1], V[2], V[3]);
         }
     }
-    *K = k; *S = s2;
+    *K = (double)k; *S = (double)s2;
 }
 
-// Cells are classified against eps_sims = 2^-52 (exact in FP32, so the
-// comparisons equal the reference's FP64 ones on the same values).  Bulk
-// water cells add their precomputed fixed-point hexahedron volume; the block
-// then packs its interface cells into the first lanes (ballot + prefix, in
-// cell order) so the FP64 geometry runs on dense warps.  Sums are 64-bit
-// integers (exact, order-independent).
+// Cells are classified against eps_sims = 2^-52 in the phi type.  Bulk
+// water cells add their precomputed FP64 fixed-point hexahedron volume;
+// each warp packs its interface cells into its first lanes (ballot + rank,
+// in cell order) so their geometry runs on dense lanes, in the stencil
+// precision T (FP32: each interface cell's share carries a relative
+// rounding error of about 1e-7 of that cell's volume).  Every thread keeps
+// 64-bit integer sums over the bricks of one instance; the CTA reduces
+// them and adds them to the instance's accumulators with integer atomics
+// when the instance changes and at the end (exact and order-independent:
+// the result does not depend on the schedule).
 __device__ __forceinline__ long long warp_sum_ll(long long v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -591,18 +722,41 @@ __device__ __forceinline__ long long warp_sum_ll(long long v) {
 template <typename T, int TX, int TY, int TZ>
 __global__ void __launch_bounds__(TX * TY * TZ) k_volume(const Inst* __restrict__ inst,
         const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phi,
-        long long* __restrict__ partials) {
+        unsigned long long* __restrict__ acc) {
     constexpr int NT = TX * TY * TZ, NW = NT / 32;
-    const T eps = T(2.220446049250313e-16);
-    __shared__ long long sh[3][NW];
-    __shared__ long long mixed[NT];
-    __shared__ int wcount[NW];
+    const T eps = T(kEpsSims);
+    __shared__ long long red[3][NW];
+    __shared__ long long slot[NW][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    long long Kq = 0, Sq = 0, Bq = 0;
+    int cur = -1;
+    // block-uniform: every thread of the CTA walks the same bricks
+    auto flush = [&]() {
+        Kq = warp_sum_ll(Kq);
+        Sq = warp_sum_ll(Sq);
+        Bq = warp_sum_ll(Bq);
+        if (lane == 0) {
+            red[0][w] = Kq;
+            red[1][w] = Sq;
+            red[2][w] = Bq;
+        }
+        __syncthreads();
+        if (threadIdx.x < 3) {
+            long long a = 0;
+            for (int q = 0; q < NW; ++q) a += red[threadIdx.x][q];
+            if (a != 0) atomicAdd(acc + 3 * (long long)cur + threadIdx.x, (unsigned long long)a);
+        }
+        __syncthreads();
+        Kq = Sq = Bq = 0;
+    };
     for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
         const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
+        if (b.inst != cur) {
+            if (cur >= 0) flush();
+            cur = b.inst;
+        }
         const Inst& I = inst[b.inst];
         const long long sj = I.ni, sk = (long long)I.ni * I.nj;
-        long long Kq = 0, Sq = 0, Bq = 0;
         bool mix = false;
         long long l = 0;
         if (b.i < I.ni - 1 && b.j < I.nj - 1 && b.k < I.nk - 1) {
@@ -614,71 +768,55 @@ __global__ void __launch_bounds__(TX * TY * TZ) k_volume(const Inst* __restrict_
                 const T p = __ldg(phi + o[v]);
                 allw &= p > eps; alla &= p < -eps;
             }
-            if (allw) Bq = __ldg(f.cellfix + l);
+            if (allw) Bq += __ldg(f.cellfix + l);
             mix = !allw && !alla;
         }
         const unsigned m = __ballot_sync(0xffffffffu, mix);
-        if (lane == 0) wcount[w] = __popc(m);
-        __syncthreads();
-        int base = 0, total = 0;
-        for (int q = 0; q < NW; ++q) { base += q < w ? wcount[q] : 0; total += wcount[q]; }
-        if (mix) mixed[base + __popc(m & ((1u << lane) - 1u))] = l;
-        __syncthreads();
-        if (threadIdx.x < total) {
-            const long long c = mixed[threadIdx.x];
-            const long long o[8] = {c, c + 1, c + 1 + sj, c + sj, c + sk, c + 1 + sk, c + 1 + sj + sk, c + sj + sk};
-            double P[8], C[8][3];
+        if (m) {
+            if (mix) slot[w][__popc(m & ((1u << lane) - 1u))] = l;
+            __syncwarp();
+            if (lane < __popc(m)) {
+                const long long c = slot[w][lane];
+                const long long o[8] = {c, c + 1, c + 1 + sj, c + sj, c + sk, c + 1 + sk, c + 1 + sj + sk,
+                                        c + sj + sk};
+                // vertex coordinates relative to vertex 0 (differences in FP64,
+                // then rounded to T: the FP32 geometry keeps the cell's own
+                // size as its scale, not the domain's)
+                T P8[8], C[8][3];
+                double X0[3];
 #pragma unroll
-            for (int v = 0; v < 8; ++v) {
-                P[v] = (double)__ldg(phi + o[v]);
-                C[v][0] = __ldg(f.xyz[0] + o[v]); C[v][1] = __ldg(f.xyz[1] + o[v]); C[v][2] = __ldg(f.xyz[2] + o[v]);
+                for (int a = 0; a < 3; ++a) X0[a] = __ldg(f.xyz[a] + c);
+#pragma unroll
+                for (int v = 0; v < 8; ++v) {
+                    P8[v] = __ldg(phi + o[v]);
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) C[v][a] = (T)(__ldg(f.xyz[a] + o[v]) - X0[a]);
+                }
+                double K = 0.0, S = 0.0;
+                cell_water_fast(P8, C, &K, &S);
+                Kq += __double2ll_rn(K * kVolScale);
+                Sq += __double2ll_rn(S * kVolScale);
             }
-            double K = 0.0, S = 0.0;
-            cell_water_fast(P, C, &K, &S);
-            Kq = __double2ll_rn(K * kVolScale);
-            Sq = __double2ll_rn(S * kVolScale);
+            __syncwarp();
         }
-        Kq = warp_sum_ll(Kq); Sq = warp_sum_ll(Sq); Bq = warp_sum_ll(Bq);
-        if (lane == 0) { sh[0][w] = Kq; sh[1][w] = Sq; sh[2][w] = Bq; }
-        __syncthreads();
-        if (threadIdx.x < 3) {
-            long long acc = 0;
-            for (int q = 0; q < NW; ++q) acc += sh[threadIdx.x][q];
-            partials[3 * (long long)blk + threadIdx.x] = acc;
-        }
-        __syncthreads();
     }
+    if (cur >= 0) flush();
 }
 
-// one block per instance sums its bricks' partials (exact integer sums)
-__global__ void __launch_bounds__(256) k_volume_final(const Inst* __restrict__ inst, int ninst, int nbricks,
-                                                      const long long* __restrict__ partials, double* __restrict__ vols) {
-    const int b = blockIdx.x;
-    if (b >= ninst) return;
-    const int first = inst[b].brick0;
-    const int last = b + 1 < ninst ? inst[b + 1].brick0 : nbricks;
-    __shared__ long long sh[3][8];
-    long long acc[3] = {0, 0, 0};
-    for (int q = first + threadIdx.x; q < last; q += 256)
-        for (int c = 0; c < 3; ++c) acc[c] += partials[3 * (long long)q + c];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+// converts each instance's accumulators (K, S, bulk) to volumes and clears
+// them for the next launch of k_volume
+__global__ void k_volume_final(int ninst, unsigned long long* __restrict__ acc, double* __restrict__ vols) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= ninst) return;
+    long long v[3];
     for (int c = 0; c < 3; ++c) {
-        const long long v = warp_sum_ll(acc[c]);
-        if (lane == 0) sh[c][w] = v;
+        v[c] = (long long)acc[3 * q + c];
+        acc[3 * q + c] = 0ull;
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        long long v[3];
-        for (int c = 0; c < 3; ++c) {
-            long long a = 0;
-            for (int q = 0; q < 8; ++q) a += sh[c][q];
-            v[c] = a;
-        }
-        vols[4 * b] = (double)v[0] * kVolUnit;
-        vols[4 * b + 1] = (double)v[1] * kVolUnit;
-        vols[4 * b + 2] = (double)v[2] * kVolUnit;
-        vols[4 * b + 3] = (double)(v[0] + v[1] + v[2]) * kVolUnit;
-    }
+    vols[4 * q] = (double)v[0] * kVolUnit;
+    vols[4 * q + 1] = (double)v[1] * kVolUnit;
+    vols[4 * q + 2] = (double)v[2] * kVolUnit;
+    vols[4 * q + 3] = (double)(v[0] + v[1] + v[2]) * kVolUnit;
 }
 
 // fixed-point Davies-Salmond volume of every cell of one instance
@@ -789,21 +927,6 @@ __device__ __forceinline__ T stage_node_grad(const T (&s)[5], T w, T lp, bool lo
     G[3] = k * ((P ? c : b) - (M ? T(0) : a2));
     G[4] = k * (P ? T(0) : a);
     return vp - vm;
-}
-
-// Adjoint brick of block `blk` in adjoint map `map`: instance and origin.
-struct ABrick {
-    int inst, i0, j0, k0;
-};
-__device__ __forceinline__ ABrick adj_brick(const Brick* __restrict__ bmap, int map, int blk) {
-    const int4 bk = __ldg(reinterpret_cast<const int4*>(bmap) + blk);
-    const AdjShape sh = adj_shape(map);
-    ABrick b;
-    b.inst = bk.x;
-    b.i0 = bk.y * sh.ox;
-    b.j0 = bk.z * sh.oy;
-    b.k0 = bk.w * sh.oz;
-    return b;
 }
 
 // Stage adjoint, x part (adjoint map 0: bricks of 8 whole rows of one
@@ -1160,10 +1283,6 @@ void dispatch(int shape, A... a) {
 LSM_BATCH_RUNNER(RunContra, k_contra,
                  (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, cudaStream_t s),
                  (inst, bi, nb, f))
-LSM_BATCH_RUNNER(RunStage, k_stage,
-                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* pn, const T* p1, T* out,
-                  double c1, double c2, double c3, cudaStream_t s),
-                 (inst, bi, nb, f, pn, p1, out, T(c1), T(c2), T(c3)))
 LSM_BATCH_RUNNER(RunBcFull, k_bc_full,
                  (int grid, const Inst* inst, const Brick* bi, int nb, BC bc, const T* src, T* dst, unsigned* err,
                   cudaStream_t s),
@@ -1180,8 +1299,8 @@ LSM_BATCH_RUNNER(RunSignReinit, k_sign_reinit,
                   unsigned* err, cudaStream_t s),
                  (inst, bi, nb, f, p0, dout, err))
 LSM_BATCH_RUNNER(RunVolume, k_volume,
-                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi, long long* part,
-                  cudaStream_t s),
+                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi,
+                  unsigned long long* part, cudaStream_t s),
                  (inst, bi, nb, f, phi, part))
 
 template <typename T, int TX, int TY, int TZ>
@@ -1189,7 +1308,7 @@ struct Occupancy {
     static void run(int kernel, int* out) {
         const int nt = TX * TY * TZ;
         switch (kernel) {
-        case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_stage<T, TX, TY, TZ>, nt, 0); break;
+        case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_contra<T, TX, TY, TZ>, nt, 0); break;
         case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_reinit<T, TX, TY, TZ>, nt, 0); break;
         default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_volume<T, TX, TY, TZ>, nt, 0); break;
         }
@@ -1206,9 +1325,16 @@ void contra(int shape, int grid, const Inst* inst, const Brick* bi, int nb, Fiel
     dispatch<RunContra, T>(shape, grid, inst, bi, nb, f, s);
 }
 template <typename T>
-void stage(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phin, const T* phi1,
-           T* out, double c1, double c2, double c3, cudaStream_t s) {
-    dispatch<RunStage, T>(shape, grid, inst, bi, nb, f, phin, phi1, out, c1, c2, c3, s);
+void stage(int grid, const Inst* inst, const Brick* bmap2, int nb, FieldsT<T> f, const T* phin, const T* phi1, T* out,
+           double c1, double c2, double c3, cudaStream_t s) {
+    ProfScope ps_("k_stage_z", s);
+    k_stage_z<T><<<grid, 256, 0, s>>>(inst, bmap2, nb, f, phin, phi1, out, T(c1), T(c2), T(c3));
+}
+template <typename T>
+int stage_blocks_per_sm() {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_stage_z<T>, 256, 0);
+    return n;
 }
 template <typename T>
 void bc_stage(const Inst* inst, int ninst, long long nface, BC bc, const T* phin, const T* phi1, T* out, double c1,
@@ -1243,14 +1369,12 @@ void bc_reinit(const Inst* inst, int ninst, long long nface, FieldsT<T> f, BC bc
 }
 template <typename T>
 void volume(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi,
-            long long* partials, cudaStream_t s) {
-    dispatch<RunVolume, T>(shape, grid, inst, bi, nb, f, phi, partials, s);
+            unsigned long long* acc, cudaStream_t s) {
+    dispatch<RunVolume, T>(shape, grid, inst, bi, nb, f, phi, acc, s);
 }
-void volume_final(const Inst* inst, int ninst, const Brick* bi, int nb, const long long* partials, double* vols,
-                  cudaStream_t s) {
-    (void)bi;
+void volume_final(int ninst, unsigned long long* acc, double* vols, cudaStream_t s) {
     ProfScope ps_("k_volume_final", s);
-    k_volume_final<<<ninst, 256, 0, s>>>(inst, ninst, nb, partials, vols);
+    k_volume_final<<<(ninst + 127) / 128, 128, 0, s>>>(ninst, acc, vols);
 }
 void cell_hex(long long off, int ni, int nj, int nk, const double* x, const double* y, const double* z,
               long long* cellfix, cudaStream_t s) {
@@ -1313,7 +1437,8 @@ void adj_contra(const Flat& fl, FieldsT<T> f, const T* w0, const T* w1, const T*
 
 #define LSM_BATCH_INSTANTIATE(T)                                                                                      \
     template void contra<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, cudaStream_t);                       \
-    template void stage<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, const T*, T*, double,       \
+    template int stage_blocks_per_sm<T>();                                                                      \
+    template void stage<T>(int, const Inst*, const Brick*, int, FieldsT<T>, const T*, const T*, T*, double,            \
                            double, double, cudaStream_t);                                                                     \
     template void bc_stage<T>(const Inst*, int, long long, BC, const T*, const T*, T*, double, double, cudaStream_t);   \
     template void bc_full<T>(int, int, const Inst*, const Brick*, int, BC, const T*, T*, unsigned*, cudaStream_t);      \
@@ -1323,7 +1448,8 @@ void adj_contra(const Flat& fl, FieldsT<T> f, const T* w0, const T* w1, const T*
     template void bc_reinit<T>(const Inst*, int, long long, FieldsT<T>, BC, const T*, T*, cudaStream_t);              \
     template void sign_reinit<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, unsigned*,      \
                                  cudaStream_t);                                                                   \
-    template void volume<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, long long*, cudaStream_t);  \
+    template void volume<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, unsigned long long*,   \
+                             cudaStream_t);                                                                          \
     template void adj_face<T>(const Flat&, int, long long, BC, int, const T*, const T*, const T*, double, double, T*, \
                               cudaStream_t);                                                                          \
     template void adj_stage<T>(const int*, const Inst*, const Brick* const*, const int*, FieldsT<T>, const T*,      \

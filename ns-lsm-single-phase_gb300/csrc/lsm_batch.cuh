@@ -72,9 +72,14 @@ constexpr Shape kShapes[kNumShapes] = {{32, 4, 2}, {32, 8, 1}, {64, 4, 1}, {32, 
 template <typename T>
 void contra(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f,
             cudaStream_t s);
+// RK stage out = c1 phin + c2 phi1 - c3 dt aj RH(phi1) on the tiles of
+// adjoint map 2 (z march, shared-memory planes); grid from
+// stage_blocks_per_sm
 template <typename T>
-void stage(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f, const T* phin,
-           const T* phi1, T* out, double c1, double c2, double c3, cudaStream_t s);
+void stage(int grid, const Inst* inst, const Brick* bmap2, int nb, FieldsT<T> f, const T* phin, const T* phi1,
+           T* out, double c1, double c2, double c3, cudaStream_t s);
+template <typename T>
+int stage_blocks_per_sm();
 template <typename T>
 void bc_stage(const Inst* inst, int ninst, long long nface, BC bc, const T* phin, const T* phi1, T* out, double c1,
               double c2, cudaStream_t s);
@@ -96,11 +101,13 @@ void sign_reinit(int shape, int grid, const Inst* inst, const Brick* bricks, int
 template <typename T>
 void bc_reinit(const Inst* inst, int ninst, long long nface, FieldsT<T> f, BC bc, const T* din, T* dout,
                cudaStream_t s);
+// water volume of every instance: k_volume adds 64-bit fixed-point sums
+// (K, S, bulk) to acc[3 * inst + c] (zero on entry); volume_final writes
+// vols[4 * inst + 0..3] = (K, S, bulk, total) and clears acc
 template <typename T>
 void volume(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f, const T* phi,
-            long long* partials, cudaStream_t s);
-void volume_final(const Inst* inst, int ninst, const Brick* bricks, int nbricks, const long long* partials,
-                  double* vols, cudaStream_t s);
+            unsigned long long* acc, cudaStream_t s);
+void volume_final(int ninst, unsigned long long* acc, double* vols, cudaStream_t s);
 // fixed-point hexahedron volume of every cell of one instance (static
 // geometry); x, y, z and cellfix are the packed base arrays, `off` the
 // instance's first node

@@ -53,8 +53,8 @@ struct lsm_batch {
     int nbricks = 0;
     lsm::batch::Brick* d_amap[4] = {};  // brick tables of the adjoint stencil kernels (lsm::batch::adj_shape)
     int namap[4] = {0, 0, 0, 0}, agrid[4] = {1, 1, 1, 1};
-    long long* d_part = nullptr;
-    size_t part_cap = 0;
+    int sgrid = 1;                      // CTAs of the RK stage (on adjoint map 2)
+    unsigned long long* d_vacc = nullptr;   // volume accumulators, 3 per instance (k_volume)
     double* d_vols = nullptr;
     double* h_vols = nullptr;    // pinned
     unsigned* d_err = nullptr;
@@ -223,15 +223,9 @@ int build_bricks(lsm_batch* b, int shape) {
     BCU(b, cudaMalloc(&b->d_brick, sizeof(Brick) * brick.size()));
     BCU(b, cudaMemcpyAsync(b->d_brick, brick.data(), sizeof(Brick) * brick.size(), cudaMemcpyHostToDevice, b->stream));
     BCU(b, cudaMemcpyAsync(b->d_inst, hi.data(), sizeof(Inst) * hi.size(), cudaMemcpyHostToDevice, b->stream));
-    const size_t need = 3 * (size_t)b->nbricks;
-    if (need > b->part_cap) {
-        if (b->d_part) {
-            cudaStreamSynchronize(b->stream);
-            cudaFree(b->d_part);
-            b->d_part = nullptr;
-        }
-        BCU(b, cudaMalloc(&b->d_part, sizeof(long long) * need));
-        b->part_cap = need;
+    if (!b->d_vacc) {
+        BCU(b, cudaMalloc(&b->d_vacc, sizeof(unsigned long long) * 3 * (size_t)b->ninst));
+        BCU(b, cudaMemsetAsync(b->d_vacc, 0, sizeof(unsigned long long) * 3 * (size_t)b->ninst, b->stream));
     }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
@@ -242,6 +236,9 @@ int build_bricks(lsm_batch* b, int shape) {
                                            : lsm::batch::adj_blocks_per_sm<float>(m));
         b->agrid[m] = std::max(1, std::min(b->namap[m], sms * pa));
     }
+    const int ps = std::max(1, b->prec ? lsm::batch::stage_blocks_per_sm<double>()
+                                       : lsm::batch::stage_blocks_per_sm<float>());
+    b->sgrid = std::max(1, std::min(b->namap[2], sms * ps));
     b->shape = shape;
     BCU(b, cudaStreamSynchronize(b->stream));
     return LSM_OK;
@@ -293,14 +290,15 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
     FieldsT<T> f = fields<T>(b);
     if (rec) f.sgn = rec->sgn;
     if (vol) {
-        B::volume<T>(sh, gr, b->d_inst, b->d_brick, nb, f, phin, b->d_part, b->stream);
-        B::volume_final(b->d_inst, b->ninst, b->d_brick, nb, b->d_part, b->d_vols, b->stream);
+        B::volume<T>(sh, gr, b->d_inst, b->d_brick, nb, f, phin, b->d_vacc, b->stream);
+        B::volume_final(b->ninst, b->d_vacc, b->d_vols, b->stream);
     }
     B::contra<T>(sh, gr, b->d_inst, b->d_brick, nb, f, b->stream);
     T* S[3] = {rec ? rec->A[0] : f.stage[0], rec ? rec->A[1] : f.stage[1], rec ? rec->A[2] : f.stage[0]};
     const T* in[3] = {phin, S[0], S[1]};
     for (int s = 0; s < 3; ++s) {
-        B::stage<T>(sh, gr, b->d_inst, b->d_brick, nb, f, phin, in[s], S[s], kC[s][0], kC[s][1], kC[s][2], b->stream);
+        B::stage<T>(b->sgrid, b->d_inst, b->d_amap[2], b->namap[2], f, phin, in[s], S[s], kC[s][0], kC[s][1], kC[s][2],
+                    b->stream);
         B::bc_stage<T>(b->d_inst, b->ninst, b->nface, bc, phin, in[s], S[s], kC[s][0], kC[s][1], b->stream);
     }
     const int R = b->cfg.RNitermax;
@@ -344,8 +342,7 @@ int autotune(lsm_batch* b) {
         BTRY(build_bricks(b, s));
         B::sign<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, f.phi, b->stream);
         auto pass = [&]() {
-            B::stage<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, f.phi, f.phi, f.stage[0], 1.0, 0.0, 1.0,
-                            b->stream);
+            B::contra<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, b->stream);
             B::reinit<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, f.phi, f.d[0], nullptr, b->stream);
         };
         pass();
@@ -663,7 +660,7 @@ int lsm_batch_destroy(lsm_batch_handle b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     for (void* p : {b->field_arena, (void*)b->xyz, (void*)b->staging, (void*)b->d_inst, (void*)b->d_offs,
                     (void*)b->d_brick, (void*)b->d_amap[0], (void*)b->d_amap[1], (void*)b->d_amap[2],
-                    (void*)b->d_amap[3], (void*)b->d_part, (void*)b->d_vols, (void*)b->d_err, b->adj})
+                    (void*)b->d_amap[3], (void*)b->d_vacc, (void*)b->d_vols, (void*)b->d_err, b->adj})
         if (p) cudaFree(p);
     if (b->h_vols) cudaFreeHost(b->h_vols);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
