@@ -190,44 +190,15 @@ __global__ void __launch_bounds__(TX * TY * TZ) k_contra(const Inst* __restrict_
 }
 
 // ------------------------------------------------------------ RK stage
-__device__ __forceinline__ bool interior(const Inst& I, int i, int j, int k) {
-    return i > 0 && i < I.ni - 1 && j > 0 && j < I.nj - 1 && k > 0 && k < I.nk - 1;
-}
-
-// sum_m W_m (Phi+ - Phi-)_m at an interior node (calc_RH_AD_WENO3 x aj dt)
-template <typename T>
-__device__ __forceinline__ T stage_rhs(const FieldsT<T>& f, const T* __restrict__ phi1, const Inst& I, long long l,
-                                       int i, int j, int k) {
-    const long long sj = I.ni, sk = (long long)I.ni * I.nj;
-    const T p = __ldg(phi1 + l);
-    T R;
-    {
-        const T w = __ldg(f.W[0] + l);
-        const T m2 = i > 1 ? __ldg(phi1 + l - 2) : T(0);
-        const T p2 = i < I.ni - 2 ? __ldg(phi1 + l + 2) : T(0);
-        R = w * weno_diff(m2, __ldg(phi1 + l - 1), p, __ldg(phi1 + l + 1), p2, w, i == 1, i == I.ni - 2);
-    }
-    {
-        const T w = __ldg(f.W[1] + l);
-        const T m2 = j > 1 ? __ldg(phi1 + l - 2 * sj) : T(0);
-        const T p2 = j < I.nj - 2 ? __ldg(phi1 + l + 2 * sj) : T(0);
-        R = vfma(w, weno_diff(m2, __ldg(phi1 + l - sj), p, __ldg(phi1 + l + sj), p2, w, j == 1, j == I.nj - 2), R);
-    }
-    {
-        const T w = __ldg(f.W[2] + l);
-        const T m2 = k > 1 ? __ldg(phi1 + l - 2 * sk) : T(0);
-        const T p2 = k < I.nk - 2 ? __ldg(phi1 + l + 2 * sk) : T(0);
-        R = vfma(w, weno_diff(m2, __ldg(phi1 + l - sk), p, __ldg(phi1 + l + sk), p2, w, k == 1, k == I.nk - 2), R);
-    }
-    return R;
-}
 
 // RK stage on the tiles of adjoint map 2 (32 x 8 columns marching 32 planes
 // in k).  Each plane of phi1 is staged in shared memory with a two-node
 // halo in x and y (double-buffered, one barrier per plane: the x and y
 // stencils read it there); the z stencil is a five-plane register window.
-// Loads per node: phi1 once (plus the halo share), phi^n and W.  Same
-// arithmetic as stage_rhs.  Halo slots: threads 0..127 hold the y-halo rows
+// Loads per node: phi1 once (plus the halo share), phi^n and W.  Interior
+// nodes: out = c1 phi^n + c2 phi1 - c3 sum_m W_m (Phi+ - Phi-)_m
+// (calc_RH_AD_WENO3 x aj dt, the x term first); other nodes get R = 0 and
+// their faces from bcond_lsm afterwards.  Halo slots: threads 0..127 hold the y-halo rows
 // -2, -1, 8, 9 of the tile, threads 128..159 the x-halo columns -2, -1, 32,
 // 33 (the cross stencil needs no corners).
 constexpr int kStSX = 36, kStSY = 12;
@@ -592,7 +563,7 @@ __device__ __forceinline__ G tetvol_g(const G (&a)[3], const G (&b)[3], const G 
 template <typename G>
 __device__ __forceinline__ G tet_water(const G (&V)[4][3], const G (&ph)[4]) {
     const G TV = tetvol_g(V[0], V[1], V[2], V[3]);
-    const G tiny = G(kTinyD);   // tiny(1d0); 0 in FP32, where every nonzero value exceeds it
+    const G tiny = G(sizeof(G) == 8 ? kTinyD : 0.0);   // tiny(1d0); in FP32 every nonzero value exceeds it
     int s[4], nz = 0, fi = 0;
     bool allp = true, alln = true, allge = true, allle = true;
 #pragma unroll
@@ -1098,79 +1069,49 @@ __global__ void __launch_bounds__(256) k_adj_stage_m(const Inst* __restrict__ in
     }
 }
 
-// Reinitialisation adjoint coefficients of node (i, j, k) from its inputs:
+// Reinitialisation adjoint coefficients of one node from its inputs:
 // with w = dtau s lam / (2 G) and the Godunov selections of the forward
 // pass, A_m = w dG^2/dmen_m, B_m = w dG^2/dmas_m (a physical face's single
-// difference goes to B on the low face, to A on the high face).
+// difference goes to B on the low face, to A on the high face; lo / hi flag
+// the node's faces).  Branch-free: with sigma = sign(s) both Godunov
+// branches are one, P = sigma max(sigma bb, 0), Q = sigma min(sigma ff, 0),
+// and w dG^2/dmen_m = dtau |s| lam / G sum_x M[m][x] (P chosen ? sigma P : 0).
 template <typename T>
 struct CoefIn {
-    T d[7];     // d at the node, -x, +x, -y, +y, -z, +z (one-sided on faces)
+    T d[7];     // d at the node, -x, +x, -y, +y, -z, +z (any finite value where outside)
     T s, lam;
     T M[9];
 };
 
 template <typename T>
-__device__ __forceinline__ void coef_load(const FieldsT<T>& f, const T* __restrict__ d, const T* __restrict__ lam,
-                                          const Inst& I, int i, int j, int k, bool ok, CoefIn<T>& c) {
-    if (!ok) {
-        c.s = T(0);
-        c.lam = T(0);
-        return;
-    }
-    const long long sj = I.ni, sk = (long long)I.ni * I.nj;
-    const long long l = I.off + i + sj * j + sk * k;
-    c.s = __ldg(f.sgn + l);
-    c.lam = __ldg(lam + l);
-    c.d[0] = __ldg(d + l);
-    c.d[1] = i > 0 ? __ldg(d + l - 1) : c.d[0];
-    c.d[2] = i < I.ni - 1 ? __ldg(d + l + 1) : c.d[0];
-    c.d[3] = j > 0 ? __ldg(d + l - sj) : c.d[0];
-    c.d[4] = j < I.nj - 1 ? __ldg(d + l + sj) : c.d[0];
-    c.d[5] = k > 0 ? __ldg(d + l - sk) : c.d[0];
-    c.d[6] = k < I.nk - 1 ? __ldg(d + l + sk) : c.d[0];
-#pragma unroll
-    for (int q = 0; q < 9; ++q) c.M[q] = __ldg(f.m[q] + l);
-}
-
-template <typename T>
-__device__ __forceinline__ void coef_eval(const CoefIn<T>& c, T dtau, int i, int j, int k, int ni, int nj, int nk,
+__device__ __forceinline__ void coef_eval(const CoefIn<T>& c, T dtau, const bool (&lo)[3], const bool (&hi)[3],
                                           T (&A)[3], T (&B)[3]) {
-#pragma unroll
-    for (int m = 0; m < 3; ++m) A[m] = B[m] = T(0);
-    if (c.s == T(0)) return;
-    const int c3d[3] = {i, j, k};
-    const int n3[3] = {ni, nj, nk};
+    const T sg = c.s > T(0) ? T(1) : T(-1);
     T mas[3], men[3];
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
         const T fwd = c.d[2 + 2 * m] - c.d[0], bwd = c.d[0] - c.d[1 + 2 * m];
-        mas[m] = c3d[m] < n3[m] - 1 ? fwd : bwd;
-        men[m] = c3d[m] > 0 ? bwd : fwd;
+        mas[m] = sg * (hi[m] ? bwd : fwd);
+        men[m] = sg * (lo[m] ? fwd : bwd);
     }
-    T db[3], df[3], acc = T(0);
+    T e[3], g[3], acc = T(0);
 #pragma unroll
     for (int x = 0; x < 3; ++x) {
-        const T bb = c.M[x] * men[0] + c.M[3 + x] * men[1] + c.M[6 + x] * men[2];
-        const T ff = c.M[x] * mas[0] + c.M[3 + x] * mas[1] + c.M[6 + x] * mas[2];
-        const T P = c.s > T(0) ? vmax(bb, T(0)) : vmin(bb, T(0));
-        const T Q = c.s > T(0) ? vmin(ff, T(0)) : vmax(ff, T(0));
-        const bool takeP = P * P >= Q * Q;
-        acc += takeP ? P * P : Q * Q;
-        db[x] = takeP ? T(2) * P : T(0);
-        df[x] = takeP ? T(0) : T(2) * Q;
+        const T bb = c.M[x] * men[0] + c.M[3 + x] * men[1] + c.M[6 + x] * men[2];   // sigma bb
+        const T ff = c.M[x] * mas[0] + c.M[3 + x] * mas[1] + c.M[6 + x] * mas[2];   // sigma ff
+        const T p = vmax(bb, T(0)), q = vmin(ff, T(0));
+        const bool takeP = p * p >= q * q;
+        acc += takeP ? p * p : q * q;
+        e[x] = takeP ? p : T(0);
+        g[x] = takeP ? T(0) : q;
     }
-    if (!(acc > T(0))) return;
-    const T wgt = T(0.5) * dtau * c.s * c.lam * vrsqrt(acc);   // dtau s lam / (2 G)
+    const T wgt = (c.s != T(0) && acc > T(0)) ? dtau * fabs(c.s) * c.lam * vrsqrt(acc) : T(0);
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
-        const T gmen = c.M[3 * m] * db[0] + c.M[3 * m + 1] * db[1] + c.M[3 * m + 2] * db[2];
-        const T gmas = c.M[3 * m] * df[0] + c.M[3 * m + 1] * df[1] + c.M[3 * m + 2] * df[2];
-        if (c3d[m] == 0) B[m] = wgt * (gmen + gmas);
-        else if (c3d[m] == n3[m] - 1) A[m] = wgt * (gmen + gmas);
-        else {
-            A[m] = wgt * gmen;
-            B[m] = wgt * gmas;
-        }
+        const T gmen = c.M[3 * m] * e[0] + c.M[3 * m + 1] * e[1] + c.M[3 * m + 2] * e[2];
+        const T gmas = c.M[3 * m] * g[0] + c.M[3 * m + 1] * g[1] + c.M[3 * m + 2] * g[2];
+        A[m] = lo[m] ? T(0) : wgt * (hi[m] ? gmen + gmas : gmen);
+        B[m] = hi[m] ? T(0) : wgt * (lo[m] ? gmen + gmas : gmas);
     }
 }
 
@@ -1178,45 +1119,97 @@ __device__ __forceinline__ void coef_eval(const CoefIn<T>& c, T dtau, int i, int
 //   lam_out(j) = lam(j) - sum_m [A_m(j) - B_m(j) - A_m(j+e_m) + B_m(j-e_m)]
 // (adjoint map 3).  A block of 32 x kReinRY threads covers nodes i0-1 ..
 // i0+30, j0-1 .. j0+kReinRY-2 and writes the inner 30 x (kReinRY-2); it
-// marches in k: iteration k loads the inputs of plane k+1 (prefetch),
-// evaluates the coefficients of plane k and writes plane k-1.  x neighbours
-// come by warp shuffles, y neighbours through shared memory (three plane
-// buffers, one barrier per plane), z neighbours stay in registers.
+// marches in k.  Iteration k evaluates the coefficients of plane k and
+// writes plane k-1.  Each node loads its own d, s, lam and metrics only:
+// the x neighbours of d come by warp shuffles (the tile's edge lanes load
+// the one outside), the y neighbours from the plane in shared memory (the
+// edge rows load the one outside), the z neighbours from a register window
+// (d is fetched two planes ahead, the rest one plane ahead).  The
+// coefficients travel the same way: A_x / B_x by shuffles, A_y / B_y
+// through shared memory, A_z / B_z in registers.  One barrier per plane,
+// shared planes double-buffered (a buffer is rewritten two iterations
+// later, after every thread has passed the barrier between).
 template <typename T>
-__global__ void __launch_bounds__(32 * kReinRY) k_adj_reinit(const Inst* __restrict__ inst,
+__global__ void __launch_bounds__(32 * kReinRY, sizeof(T) == 4 ? 2 : 1) k_adj_reinit(const Inst* __restrict__ inst,
         const Brick* __restrict__ bmap, int nb, FieldsT<T> f, const T* __restrict__ d, const T* __restrict__ lam,
         T* __restrict__ lam_out) {
     constexpr int RY = kReinRY;
-    __shared__ T sA1[3][RY][32], sB1[3][RY][32];
+    __shared__ T sD[2][RY + 2][32];   // row ty + 1 holds row ty (rows 0, RY + 1: padding)
+    __shared__ T sA1[2][RY][32], sB1[2][RY][32];
+    const unsigned FM = 0xffffffffu;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     for (int blk = blockIdx.x; blk < nb; blk += gridDim.x) {
         const ABrick ab = adj_brick(bmap, 3, blk);
         const Inst& I = inst[ab.inst];
         const int ni = I.ni, nj = I.nj, nk = I.nk;
+        const long long sj = ni, sk = (long long)ni * nj;
         const int i = ab.i0 - 1 + tx, j = ab.j0 - 1 + ty;
         const int k0 = ab.k0, k1 = min(k0 + adj_shape(3).oz, nk);
         const bool node = i >= 0 && i < ni && j >= 0 && j < nj;
         const bool out = node && tx >= 1 && tx <= 30 && ty >= 1 && ty <= RY - 2;
         const T dtau = ipar<T>(I.dtau, I.dtau64);
-        CoefIn<T> nxt;
-        coef_load(f, d, lam, I, i, j, k0 - 1, node && k0 >= 1, nxt);
+        const long long cb = I.off + i + sj * j;   // this column at k = 0
+        // the neighbour outside the tile that edge lanes / rows load
+        const int ox = tx == 0 ? -1 : (tx == 31 ? 1 : 0), oy = ty == 0 ? -1 : (ty == RY - 1 ? 1 : 0);
+        const bool ldx = node && ox != 0 && i + ox >= 0 && i + ox < ni;
+        const bool ldy = node && oy != 0 && j + oy >= 0 && j + oy < nj;
+        auto ldd = [&](int k) { return node && k >= 0 && k < nk ? __ldg(d + cb + sk * k) : T(0); };
+        // plane-k inputs other than d (plane k evaluated iff 0 <= k < nk, k <= k1)
+        struct PlaneIn {
+            T s, lam, ex, ey, M[9];
+        };
+        auto ldp = [&](int k, PlaneIn& q) {
+            q.s = q.lam = q.ex = q.ey = T(0);
+            if (node && k >= 0 && k < nk && k <= k1) {
+                const long long l = cb + sk * k;
+                q.s = __ldg(f.sgn + l);
+                q.lam = __ldg(lam + l);
+                if (ldx) q.ex = __ldg(d + l + ox);
+                if (ldy) q.ey = __ldg(d + l + oy * sj);
+#pragma unroll
+                for (int c = 0; c < 9; ++c) q.M[c] = __ldg(f.m[c] + l);
+            }
+        };
+        __syncthreads();   // the previous tile's readers of sD / sA1 / sB1 are done
+        T dm = ldd(k0 - 2), dc = ldd(k0 - 1), dp = ldd(k0);   // d at k-1, k, k+1 for k = k0-1
+        PlaneIn cur, nxt;
+        ldp(k0 - 1, nxt);
         T Ap[3] = {T(0), T(0), T(0)}, Bp[3] = {T(0), T(0), T(0)}, Bz2 = T(0), lamp = T(0);
+        int it = 0;
 #pragma unroll 2
-        for (int k = k0 - 1; k <= k1; ++k) {
-            const CoefIn<T> cur = nxt;
-            coef_load(f, d, lam, I, i, j, k + 1, node && k + 1 >= 0 && k + 1 < nk && k + 1 <= k1, nxt);
-            T A[3], B[3];
-            coef_eval(cur, dtau, i, j, k, ni, nj, nk, A, B);
-            const int b = (k + 3) % 3;
-            sA1[b][ty][tx] = A[1];
-            sB1[b][ty][tx] = B[1];
-            // x neighbours of plane k-1
-            const T ax = __shfl_down_sync(0xffffffffu, Ap[0], 1);
-            const T bx = __shfl_up_sync(0xffffffffu, Bp[0], 1);
+        for (int k = k0 - 1; k <= k1; ++k, ++it) {
+            cur = nxt;
+            const T dnn = ldd(k + 2);   // two planes ahead
+            ldp(k + 1, nxt);
+            sD[it & 1][ty + 1][tx] = dc;
+            if (it > 0) {
+                sA1[(it - 1) & 1][ty][tx] = Ap[1];
+                sB1[(it - 1) & 1][ty][tx] = Bp[1];
+            }
             __syncthreads();
+            // neighbours of d at plane k (one-sided copies on physical faces)
+            CoefIn<T> c;
+            c.s = cur.s;
+            c.lam = cur.lam;
+#pragma unroll
+            for (int q = 0; q < 9; ++q) c.M[q] = cur.M[q];
+            c.d[0] = dc;
+            const T xl = __shfl_up_sync(FM, dc, 1), xr = __shfl_down_sync(FM, dc, 1);
+            c.d[1] = tx == 0 ? cur.ex : xl;
+            c.d[2] = tx == 31 ? cur.ex : xr;
+            c.d[3] = ty == 0 ? cur.ey : sD[it & 1][ty][tx];
+            c.d[4] = ty == RY - 1 ? cur.ey : sD[it & 1][ty + 2][tx];
+            c.d[5] = dm;
+            c.d[6] = dp;
+            const bool lo[3] = {i == 0, j == 0, k == 0}, hi[3] = {i == ni - 1, j == nj - 1, k == nk - 1};
+            T A[3], B[3];
+            coef_eval(c, dtau, lo, hi, A, B);
+            // plane k-1: x neighbours by shuffles, y from shared memory
+            const T ax = __shfl_down_sync(FM, Ap[0], 1);
+            const T bx = __shfl_up_sync(FM, Bp[0], 1);
             const int ko = k - 1;
             if (out && ko >= k0 && ko < k1) {
-                const int q = (ko + 3) % 3;
+                const int q = (it - 1) & 1;
                 T t0 = Ap[0] - Bp[0];
                 if (i < ni - 1) t0 -= ax;
                 if (i > 0) t0 += bx;
@@ -1226,8 +1219,7 @@ __global__ void __launch_bounds__(32 * kReinRY) k_adj_reinit(const Inst* __restr
                 T t2 = Ap[2] - Bp[2];
                 if (ko < nk - 1) t2 -= A[2];
                 if (ko > 0) t2 += Bz2;
-                const long long l = I.off + i + (long long)ni * (j + (long long)nj * ko);
-                lam_out[l] = lamp - t0 - t1 - t2;
+                lam_out[cb + sk * ko] = lamp - t0 - t1 - t2;
             }
             Bz2 = Bp[2];
 #pragma unroll
@@ -1236,6 +1228,9 @@ __global__ void __launch_bounds__(32 * kReinRY) k_adj_reinit(const Inst* __restr
                 Bp[m] = B[m];
             }
             lamp = cur.lam;
+            dm = dc;
+            dc = dp;
+            dp = dnn;
         }
     }
 }
