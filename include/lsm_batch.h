@@ -13,15 +13,18 @@
  * and a final bcond_lsm.
  *
  * Precision: the stencils run in FP32 (precision 0, throughput) or FP64
- * (precision 1, gradient checks); the water volume is FP64 per cell (the
- * reference's marching tetrahedra on FP64 coordinates), rounded to a
- * multiple of 2^-48 and summed as 64-bit integers, so each instance's sum is
- * exact and independent of the summation order (valid below 2^15 units^3).
+ * (precision 1, gradient checks); the water volume sums FP64 hexahedron
+ * volumes of the bulk water cells and the interface cells' shares (the
+ * reference's marching tetrahedra, in the stencil precision on coordinates
+ * relative to each cell's first vertex), each rounded to a multiple of
+ * 2^-48 and summed as 64-bit integers, so each instance's sum is exact and
+ * independent of the summation order (valid below 2^15 units^3).
  *
  * Adjoint: lsm_batch_forward_record runs `nsteps` steps keeping the state
- * every `checkpoint_every` steps; after seeding dL/dphi^{nsteps} per
- * instance, lsm_batch_backward recomputes each segment from its checkpoint
- * and runs the hand-written reverse kernels (WENO3 nonlinear weights
+ * every `checkpoint_every` steps (the last segment with all its internals);
+ * after seeding dL/dphi^{nsteps} per instance, lsm_batch_backward recomputes
+ * every other segment from its checkpoint and runs the hand-written reverse
+ * kernels (WENO3 nonlinear weights
  * differentiated, upwind side frozen; Godunov selections and the sign field
  * frozen), giving dL/dphi^0 and dL/dq(2:4) (the velocity is held fixed over
  * the recorded steps).
@@ -78,10 +81,12 @@ int lsm_batch_get_phi(lsm_batch_handle h, int inst, double* phi);
 int lsm_batch_step(lsm_batch_handle h, int nsteps, double* volumes);
 
 /* Adjoint.  Run `nsteps` steps from the current phi (which becomes phi^0),
-   keeping a checkpoint every `checkpoint_every` steps.  lsm_batch_backward
-   recomputes each segment once from its checkpoint, keeping every step's
-   internals, and reverses it.  Device memory: N (ceil(nsteps / k) +
-   k (5 + RNitermax) + 9) elements of the batch precision, k =
+   keeping a checkpoint every `checkpoint_every` steps; the last segment
+   runs with every step's internals kept.  lsm_batch_backward reverses the
+   last segment from those and each earlier one after recomputing it once
+   from its checkpoint (keeping its internals); with nsteps <=
+   checkpoint_every nothing is recomputed.  Device memory: N (ceil(nsteps /
+   k) + k (5 + RNitermax) + 9) elements of the batch precision, k =
    checkpoint_every. */
 int lsm_batch_forward_record(lsm_batch_handle h, int nsteps, int checkpoint_every);
 /* Seed dL/dphi at the end of the recorded steps for one instance (FP64, host

@@ -63,6 +63,7 @@ struct lsm_batch {
     cudaGraphExec_t exec = nullptr;
     // adjoint state: one allocation, carved by adj_view
     int rec_steps = 0, rec_ck = 0;
+    bool rec_live = false;   // the slots hold the last recorded segment's internals
     void* adj = nullptr;
     size_t adj_bytes = 0;
     std::string err;
@@ -281,9 +282,10 @@ T* rec_d(const lsm_batch* b, const Rec<T>& r, int k) {
 // One physical step phin -> phi_out (phi_out may alias phin; nullptr skips
 // the final bcond_lsm).  With `rec` the stage outputs, the pseudo-step
 // outputs (before the final bcond_lsm) and the sign field are kept; `vol`
-// adds the pre-advection water volume.
+// adds the pre-advection water volume; a recorded step checks phi_out for
+// non-finite values when `check` (plain steps always do).
 template <typename T>
-void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec, bool vol) {
+void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec, bool vol, bool check = false) {
     namespace B = lsm::batch;
     const int sh = b->shape, gr = b->grid, nb = b->nbricks;
     const B::BC bc = make_bc(b);
@@ -319,9 +321,11 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
             cur = o;
         }
         // recorded steps keep the raw last pseudo-step and write phi^{n+1} apart
-        if (rec && phi_out) B::bc_full<T>(sh, gr, b->d_inst, b->d_brick, nb, bc, cur, phi_out, nullptr, b->stream);
+        if (rec && phi_out)
+            B::bc_full<T>(sh, gr, b->d_inst, b->d_brick, nb, bc, cur, phi_out, check ? b->d_err : nullptr, b->stream);
     } else if (phi_out) {
-        B::bc_full<T>(sh, gr, b->d_inst, b->d_brick, nb, bc, S[2], phi_out, rec ? nullptr : b->d_err, b->stream);
+        B::bc_full<T>(sh, gr, b->d_inst, b->d_brick, nb, bc, S[2], phi_out, rec && !check ? nullptr : b->d_err,
+                      b->stream);
     }
 }
 
@@ -474,20 +478,37 @@ int forward_record_t(lsm_batch* b, int nsteps, int ck) {
     }
     b->rec_steps = nsteps;
     b->rec_ck = ck;
+    b->rec_live = false;
     AdjView<T> v = adj_view<T>(b);
     FieldsT<T>& f = fields<T>(b);
+    const long long LD = (long long)b->ld;
     BCU(b, cudaMemsetAsync(v.lam, 0, sizeof(T) * b->N, b->stream));
-    for (int n = 0; n < nsteps; ++n) {
+    // every segment but the last: plain steps (graph) from a checkpoint
+    const int nseg = n_ckpt(nsteps, ck), c_last = (nseg - 1) * ck;
+    for (int n = 0; n < c_last; ++n) {
         if (n % ck == 0)
-            BCU(b, cudaMemcpyAsync(v.ckpt + (long long)(n / ck) * (long long)b->ld, f.phi, sizeof(T) * b->N,
+            BCU(b, cudaMemcpyAsync(v.ckpt + (long long)(n / ck) * LD, f.phi, sizeof(T) * b->N,
                                    cudaMemcpyDeviceToDevice, b->stream));
         BTRY(run_steps(b, 1));
+    }
+    // the last segment keeps its internals in the slots, so that the reverse
+    // sweep starts there without recomputing it (the same steps, volumes and
+    // non-finite check as plain steps)
+    BCU(b, cudaMemcpyAsync(v.ckpt + (long long)(nseg - 1) * LD, f.phi, sizeof(T) * b->N, cudaMemcpyDeviceToDevice,
+                           b->stream));
+    BCU(b, cudaMemcpyAsync(v.seg, f.phi, sizeof(T) * b->N, cudaMemcpyDeviceToDevice, b->stream));
+    const int L = nsteps - c_last;
+    for (int q = 0; q < L; ++q) {
+        const Rec<T> r = slot<T>(b, v, q);
+        enqueue_step_io<T>(b, v.seg + (long long)q * LD, q + 1 < L ? v.seg + (long long)(q + 1) * LD : f.phi, &r,
+                           true, true);
     }
     BCU(b, cudaGetLastError());
     unsigned flags = 0;
     BCU(b, cudaMemcpyAsync(&flags, b->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream));
     BCU(b, cudaStreamSynchronize(b->stream));
     if (flags & lsm::kErrNonFinite) return fail(b, LSM_ERR_NONFINITE, "non-finite phi in the batch");
+    b->rec_live = true;
     return LSM_OK;
 }
 
@@ -540,12 +561,16 @@ int backward_t(lsm_batch* b) {
     for (int sg = nseg - 1; sg >= 0; --sg) {
         const int c0 = sg * ck, L = std::min(c0 + ck, nsteps) - c0;
         // recompute the segment once from its checkpoint, keeping every
-        // step's internals, then reverse it step by step
-        BCU(b, cudaMemcpyAsync(v.seg, v.ckpt + (long long)sg * LD, sizeof(T) * N, cudaMemcpyDeviceToDevice, b->stream));
-        for (int q = 0; q < L; ++q) {
-            const Rec<T> r = slot<T>(b, v, q);
-            enqueue_step_io<T>(b, v.seg + (long long)q * LD, q + 1 < L ? v.seg + (long long)(q + 1) * LD : nullptr, &r,
-                               false);
+        // step's internals (the last segment's are still in the slots after
+        // lsm_batch_forward_record), then reverse it step by step
+        if (!(sg == nseg - 1 && b->rec_live)) {
+            BCU(b, cudaMemcpyAsync(v.seg, v.ckpt + (long long)sg * LD, sizeof(T) * N, cudaMemcpyDeviceToDevice,
+                                   b->stream));
+            for (int q = 0; q < L; ++q) {
+                const Rec<T> r = slot<T>(b, v, q);
+                enqueue_step_io<T>(b, v.seg + (long long)q * LD, q + 1 < L ? v.seg + (long long)(q + 1) * LD : nullptr,
+                                   &r, false);
+            }
         }
         for (int q = L - 1; q >= 0; --q) adj_step<T>(b, v, slot<T>(b, v, q), v.seg + (long long)q * LD);
     }
@@ -554,6 +579,8 @@ int backward_t(lsm_batch* b) {
                               b->stream);
     if (v.lam != canon.lam)
         BCU(b, cudaMemcpyAsync(canon.lam, v.lam, sizeof(T) * N, cudaMemcpyDeviceToDevice, b->stream));
+    // earlier segments were recomputed into the slots
+    b->rec_live = nseg == 1;
     BCU(b, cudaGetLastError());
     BCU(b, cudaStreamSynchronize(b->stream));
     return LSM_OK;

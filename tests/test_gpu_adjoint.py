@@ -241,3 +241,21 @@ def test_adjoint_other_boundary_types_match_tape(oracle, adj_cases, btype):
         (out * T.to_torch(wts[k], "cuda")).sum().backward()
         assert _rel(gphi[k], np.asfortranarray(p.grad.cpu().numpy().T)) <= 1e-10
         assert _rel(gq[k], np.asfortranarray(q.grad.cpu().numpy().T)) <= 1e-10
+
+
+@pytest.mark.parametrize("ck", [CKPT, NSTEPS])
+def test_second_backward_repeats_the_gradient(adj_cases, ck):
+    """The forward keeps the last segment's internals; a second reverse
+    sweep (after earlier segments were recomputed into the same slots, or
+    with one segment only) gives the same gradient bit for bit."""
+    cases_ = adj_cases[:2]
+    b = _batch(cases_, 3)
+    wts = _weights(cases_)
+    g1, q1 = _adjoint(b, cases_, wts, ck=ck)
+    for k, w in enumerate(wts):
+        b.set_grad_phi(k, w)
+    b.backward()
+    for k in range(len(cases_)):
+        assert np.array_equal(b.get_grad_phi0(k), g1[k])
+        assert np.array_equal(b.get_grad_velocity(k), q1[k])
+    b.close()
