@@ -526,6 +526,9 @@ FWDADJ_BYTES = {
     "k_sign": 11 * 4,              # phi0, metrics(9); s
     "k_reinit": 12 * 4,            # d, s, metrics(9); d
     "k_sign_reinit": 12 * 4,       # phi0, metrics(9); s, d
+    "k_reinit_rec": 18 * 4,        # d, s, metrics(9); d, adjoint coefficients(6)
+    "k_sign_reinit_rec": 18 * 4,   # phi0, metrics(9); s, d, adjoint coefficients(6)
+    "k_adj_reinit_c": 8 * 4,       # lam, coefficients(6); lam_out
     "k_volume": 4 + 8,             # phi (FP32) + fixed-point cell volume (interface-cell coordinates not counted)
     "k_bc_full": 2 * 4,            # phi in, phi out
     "k_adj_stage_x": 8 * 4,        # in, W_x, lamP0, lamPhin (rmw), lamW_x (rmw); lam_in
@@ -603,10 +606,17 @@ def run_fwdadj(args):
     torch.cuda.synchronize()
     v64 = n * (nc - 1) / (e0.elapsed_time(e1) / 1e3) / 1e9
     ls.set_stream(None)
+    ls.close()
+    del phin64
+    torch.cuda.empty_cache()
 
-    # ---- the FP32 batch (one instance of the whole grid)
+    # ---- the FP32 batch (one instance of the whole grid); the recorded
+    # segment keeps the pseudo-steps' adjoint coefficients when they fit in
+    # device memory (else the reverse sweep recomputes them)
+    need = LevelSetBatch.adjoint_bytes(n, R, S, S, "fp32", "store")
+    mode = "store" if need + (8 << 30) < torch.cuda.mem_get_info()[0] else "recompute"
     b = LevelSetBatch([(g.ni, g.nj, g.nk, dt, dtau, eps)], RNitermax=R, btype=(1,) * 6, BigPhi=5.0,
-                      stream=stream.cuda_stream)
+                      stream=stream.cuda_stream, adjoint_mode=mode)
     b.set_geometry(0, x, y, z, csi, eta, zet)
     b.set_velocity(0, q)
     b.set_phi(0, phi0)
@@ -652,10 +662,44 @@ def run_fwdadj(args):
     value = world * n * S * args.steps / (ms_max / 1e3) / 1e9
     shape = b.shape
 
+    # ---- end to end through the C-ABI with host (pinned) arrays
+    def pinned(a):
+        a = np.asfortranarray(a)
+        t = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
+        v = t.numpy().reshape(a.shape, order="F")
+        v[...] = a
+        return v, t
+
+    h_phi, t1 = pinned(case.phi0)
+    h_q, t2 = pinned(case.q(0.0))
+    h_w, t3 = pinned(wts.cpu().numpy().T)
+    h_phiT, t4 = pinned(np.zeros(g.shape))
+    h_gphi, t5 = pinned(np.zeros(g.shape))
+    h_gq, t6 = pinned(np.zeros((4,) + g.shape))
+    keep = (t1, t2, t3, t4, t5, t6)
+    e2e_steps = 2
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        b.set_phi(0, h_phi)
+        b.set_velocity(0, h_q)
+        b.forward_record(S, S)
+        b._chk(b.lib.lsm_batch_get_phi(b.h, 0, h_phiT.ctypes.data), "get_phi")
+        b.set_grad_phi(0, h_w)
+        b.backward()
+        b._chk(b.lib.lsm_batch_get_grad_phi0(b.h, 0, h_gphi.ctypes.data), "get_grad_phi0")
+        b._chk(b.lib.lsm_batch_get_grad_velocity(b.h, 0, h_gq.ctypes.data), "get_grad_velocity")
+    torch.cuda.synchronize()
+    e2e_s = dist_max(time.perf_counter() - t0, world)
+    e2e_value = world * n * S * e2e_steps / e2e_s / 1e9
+    del keep
+
+    b.close()
+
     # ---- per-kernel attribution: a batch without the graph, one shorter
     # segment (4 steps) forward + adjoint under the library's event timer
     b2 = LevelSetBatch([(g.ni, g.nj, g.nk, dt, dtau, eps)], RNitermax=R, btype=(1,) * 6, BigPhi=5.0,
-                       stream=stream.cuda_stream, use_graph=False, autotune=False, shape=shape[0])
+                       stream=stream.cuda_stream, use_graph=False, autotune=False, shape=shape[0], adjoint_mode=mode)
     b2.set_geometry(0, x, y, z, csi, eta, zet)
     b2.set_velocity(0, q)
     b2.set_phi(0, phi0)
@@ -690,38 +734,6 @@ def run_fwdadj(args):
                  "note": "bytes: the launches of a profiled 4-step segment, each kernel's own algorithmic bytes; "
                          "the 20-step segment's checkpoint and segment-state copies add 0.8 B/cell-step"}
 
-    # ---- end to end through the C-ABI with host (pinned) arrays
-    def pinned(a):
-        a = np.asfortranarray(a)
-        t = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
-        v = t.numpy().reshape(a.shape, order="F")
-        v[...] = a
-        return v, t
-
-    h_phi, t1 = pinned(case.phi0)
-    h_q, t2 = pinned(case.q(0.0))
-    h_w, t3 = pinned(wts.cpu().numpy().T)
-    h_phiT, t4 = pinned(np.zeros(g.shape))
-    h_gphi, t5 = pinned(np.zeros(g.shape))
-    h_gq, t6 = pinned(np.zeros((4,) + g.shape))
-    keep = (t1, t2, t3, t4, t5, t6)
-    e2e_steps = 2
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        b.set_phi(0, h_phi)
-        b.set_velocity(0, h_q)
-        b.forward_record(S, S)
-        b._chk(b.lib.lsm_batch_get_phi(b.h, 0, h_phiT.ctypes.data), "get_phi")
-        b.set_grad_phi(0, h_w)
-        b.backward()
-        b._chk(b.lib.lsm_batch_get_grad_phi0(b.h, 0, h_gphi.ctypes.data), "get_grad_phi0")
-        b._chk(b.lib.lsm_batch_get_grad_velocity(b.h, 0, h_gq.ctypes.data), "get_grad_velocity")
-    torch.cuda.synchronize()
-    e2e_s = dist_max(time.perf_counter() - t0, world)
-    e2e_value = world * n * S * e2e_steps / e2e_s / 1e9
-    del keep
-
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sec, used = cpu_oracle_time(case, 1, host_threads())
@@ -740,6 +752,8 @@ def run_fwdadj(args):
                                    "volume each step; one step = %d-step segment forward keeping its internals + "
                                    "adjoint (checkpoint every %d steps: no recompute)" % (g.ni, g.nj, g.nk, R, S, S),
                        "nodes": n, "physical_steps_per_step": S, "tile_shape": shape[1],
+                       "adjoint_mode": mode, "adjoint_state_gb": round(LevelSetBatch.adjoint_bytes(
+                           n, R, S, S, "fp32", mode) / 1e9, 1),
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "loss": "linear, seeded N(0,1) weights on phi_T",
                        "l2": "inputs larger than L2 (phi alone %.2f GB > 129 MB)" % (n * 4 / 1e9)},
@@ -758,8 +772,6 @@ def run_fwdadj(args):
             "kernel_times_ms": {k: {"launches": v[0], "total_ms": round(v[1], 4)} for k, v in prof.items()},
         }
         print(json.dumps(line))
-    b.close()
-    ls.close()
 
 
 def run_fp64(args):

@@ -56,6 +56,9 @@ typedef struct lsm_batch_config {
     int autotune;       /* 1: time every tile shape on this batch and keep the fastest */
     int shape;          /* tile shape index when autotune == 0 (0..4) */
     int precision;      /* 0: FP32 stencils, 1: FP64 stencils (tile shape 0, no autotune) */
+    int adjoint_mode;   /* 0: recorded pseudo-steps store their adjoint coefficients (6 arrays
+                           each; the reverse sweep is a stencil), 1: the reverse sweep
+                           recomputes them from the stored pseudo-step inputs (1 array each) */
 } lsm_batch_config;
 
 typedef struct lsm_batch* lsm_batch_handle;
@@ -86,8 +89,8 @@ int lsm_batch_step(lsm_batch_handle h, int nsteps, double* volumes);
    last segment from those and each earlier one after recomputing it once
    from its checkpoint (keeping its internals); with nsteps <=
    checkpoint_every nothing is recomputed.  Device memory: N (ceil(nsteps /
-   k) + k (5 + RNitermax) + 9) elements of the batch precision, k =
-   checkpoint_every. */
+   k) + k (5 + c RNitermax) + 9) elements of the batch precision, k =
+   checkpoint_every, c = 6 (adjoint_mode 0) or 1 (adjoint_mode 1). */
 int lsm_batch_forward_record(lsm_batch_handle h, int nsteps, int checkpoint_every);
 /* Seed dL/dphi at the end of the recorded steps for one instance (FP64, host
    or device; instances not seeded get zero). */

@@ -517,6 +517,133 @@ __global__ void __launch_bounds__(TX * TY * TZ) k_sign_reinit(const Inst* __rest
     }
 }
 
+// Recorded pseudo-steps also write the adjoint's coefficients, so that the
+// reverse sweep is a 7-point stencil on lam.  With the Godunov selections
+// of the step (branch sign sel: P = sel max(sel bb, 0), Q = sel min(sel ff,
+// 0), the larger square taken), G^2 = acc, and w = dtau |s| / G:
+//   A'_m = w sum_x M[m][x] (P taken ? sel P : 0),  B'_m = the same with Q,
+// moved to B' on a low face and to A' on a high face (their one difference
+// serves both sides), and the pseudo-step's adjoint is
+//   lam_out(j) = lam(j) - sum_m [lam(j) (A'_m - B'_m)(j)
+//                - lam(j+e_m) A'_m(j+e_m) + lam(j-e_m) B'_m(j-e_m)].
+// acc is accumulated exactly as in godunov() (bit-identical pseudo-step).
+template <typename T>
+__device__ __forceinline__ T godunov_sel(const FieldsT<T>& f, const T* __restrict__ d, const Inst& I, long long l,
+                                         int i, int j, int k, T sel, T (&M)[9], T (&e)[3], T (&g)[3]) {
+    T mas[3], men[3];
+    godunov_diffs(d, I, l, i, j, k, mas, men);
+    const T sg = sel > T(0) ? T(1) : T(-1);
+    T acc = T(0);
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+        M[x] = __ldg(f.m[x] + l);
+        M[3 + x] = __ldg(f.m[3 + x] + l);
+        M[6 + x] = __ldg(f.m[6 + x] + l);
+        const T bb = sg * (M[x] * men[0] + M[3 + x] * men[1] + M[6 + x] * men[2]);
+        const T ff = sg * (M[x] * mas[0] + M[3 + x] * mas[1] + M[6 + x] * mas[2]);
+        const T p = vmax(bb, T(0)), q = vmin(ff, T(0));
+        const bool takeP = p * p >= q * q;
+        acc += takeP ? p * p : q * q;
+        e[x] = takeP ? p : T(0);
+        g[x] = takeP ? T(0) : q;
+    }
+    return acc;
+}
+
+template <typename T>
+__device__ __forceinline__ void coef_store(const T (&M)[9], const T (&e)[3], const T (&g)[3], T w, const Inst& I,
+                                           int i, int j, int k, T* __restrict__ cf, long long ld, long long l) {
+    const int c3d[3] = {i, j, k}, n3[3] = {I.ni, I.nj, I.nk};
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        const bool lo = c3d[m] == 0, hi = c3d[m] == n3[m] - 1;
+        const T gmen = M[3 * m] * e[0] + M[3 * m + 1] * e[1] + M[3 * m + 2] * e[2];
+        const T gmas = M[3 * m] * g[0] + M[3 * m + 1] * g[1] + M[3 * m + 2] * g[2];
+        cf[m * ld + l] = lo ? T(0) : w * (hi ? gmen + gmas : gmen);
+        cf[(3 + m) * ld + l] = hi ? T(0) : w * (lo ? gmen + gmas : gmas);
+    }
+}
+
+template <typename T, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(TX * TY * TZ) k_reinit_rec(const Inst* __restrict__ inst,
+        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ din, T* __restrict__ dout,
+        T* __restrict__ cf, long long ld, unsigned* err) {
+    for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
+        const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
+        if (!b.valid) continue;
+        const Inst& I = inst[b.inst];
+        const long long l = I.off + b.i + (long long)I.ni * (b.j + (long long)I.nj * b.k);
+        const T s = __ldg(f.sgn + l);
+        const T d = __ldg(din + l);
+        const T dtau = ipar<T>(I.dtau, I.dtau64);
+        T M[9], e[3], g[3];
+        const T acc = godunov_sel(f, din, I, l, b.i, b.j, b.k, s, M, e, g);
+        const T r = s == T(0) ? d : d - dtau * s * (vsqrt(acc) - T(1));
+        dout[l] = r;
+        coef_store(M, e, g, s != T(0) && acc > T(0) ? dtau * fabs(s) * vrsqrt(acc) : T(0), I, b.i, b.j, b.k, cf, ld,
+                   l);
+        if (err && !vfinite(r)) atomicOr(err, (unsigned)kErrNonFinite);
+    }
+}
+
+// k_sign_reinit with the coefficients of the first pseudo-step (the branch
+// sign is sign(phi0), which a node with s != 0 shares)
+template <typename T, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(TX * TY * TZ) k_sign_reinit_rec(const Inst* __restrict__ inst,
+        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phi0, T* __restrict__ dout,
+        T* __restrict__ cf, long long ld, unsigned* err) {
+    for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
+        const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
+        if (!b.valid) continue;
+        const Inst& I = inst[b.inst];
+        const long long l = I.off + b.i + (long long)I.ni * (b.j + (long long)I.nj * b.k);
+        const T p = __ldg(phi0 + l);
+        const T dtau = ipar<T>(I.dtau, I.dtau64);
+        T M[9], e[3], g[3];
+        const T acc = godunov_sel(f, phi0, I, l, b.i, b.j, b.k, p > T(0) ? T(1) : T(-1), M, e, g);
+        const T gn = vsqrt(acc);
+        const T s = sign_of(p, gn, ipar<T>(I.eps, I.eps64));
+        f.sgn[l] = s;
+        const T r = s == T(0) ? p : p - dtau * s * (gn - T(1));
+        dout[l] = r;
+        coef_store(M, e, g, s != T(0) && acc > T(0) ? dtau * fabs(s) * vrsqrt(acc) : T(0), I, b.i, b.j, b.k, cf, ld,
+                   l);
+        if (err && !vfinite(r)) atomicOr(err, (unsigned)kErrNonFinite);
+    }
+}
+
+// Reverse of one recorded pseudo-step from its stored coefficients (cf:
+// A'_0..2, B'_0..2, ld apart); every load is issued before the arithmetic
+template <typename T, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(TX * TY * TZ) k_adj_reinit_c(const Inst* __restrict__ inst,
+        const Brick* __restrict__ bricks, int nbricks, const T* __restrict__ cf, long long ld,
+        const T* __restrict__ lam, T* __restrict__ lam_out) {
+    for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
+        const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
+        if (!b.valid) continue;
+        const Inst& I = inst[b.inst];
+        const long long st[3] = {1, (long long)I.ni, (long long)I.ni * I.nj};
+        const long long l = I.off + b.i + st[1] * b.j + st[2] * b.k;
+        const int c3d[3] = {b.i, b.j, b.k}, n3[3] = {I.ni, I.nj, I.nk};
+        const T L = __ldg(lam + l);
+        T A[3], B[3], Lp[3], Ap[3], Lm[3], Bm[3];
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            A[m] = __ldg(cf + m * ld + l);
+            B[m] = __ldg(cf + (3 + m) * ld + l);
+            const bool up = c3d[m] < n3[m] - 1, dn = c3d[m] > 0;
+            Lp[m] = up ? __ldg(lam + l + st[m]) : T(0);
+            Ap[m] = up ? __ldg(cf + m * ld + l + st[m]) : T(0);
+            Lm[m] = dn ? __ldg(lam + l - st[m]) : T(0);
+            Bm[m] = dn ? __ldg(cf + (3 + m) * ld + l - st[m]) : T(0);
+        }
+        T t[3];
+#pragma unroll
+        for (int m = 0; m < 3; ++m) t[m] = L * A[m] - L * B[m] - Lp[m] * Ap[m] + Lm[m] * Bm[m];
+        lam_out[l] = L - t[0] - t[1] - t[2];
+    }
+}
+
 // P0 after the last pseudo-step: interior from its output, boundary nodes
 // recomputed from its input (their output slots are being overwritten).
 template <typename T>
@@ -1293,6 +1420,18 @@ LSM_BATCH_RUNNER(RunSignReinit, k_sign_reinit,
                  (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* p0, T* dout,
                   unsigned* err, cudaStream_t s),
                  (inst, bi, nb, f, p0, dout, err))
+LSM_BATCH_RUNNER(RunReinitRec, k_reinit_rec,
+                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* din, T* dout, T* cf,
+                  long long ld, unsigned* err, cudaStream_t s),
+                 (inst, bi, nb, f, din, dout, cf, ld, err))
+LSM_BATCH_RUNNER(RunSignReinitRec, k_sign_reinit_rec,
+                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* p0, T* dout, T* cf,
+                  long long ld, unsigned* err, cudaStream_t s),
+                 (inst, bi, nb, f, p0, dout, cf, ld, err))
+LSM_BATCH_RUNNER(RunAdjReinitC, k_adj_reinit_c,
+                 (int grid, const Inst* inst, const Brick* bi, int nb, const T* cf, long long ld, const T* lam,
+                  T* lam_out, cudaStream_t s),
+                 (inst, bi, nb, cf, ld, lam, lam_out))
 LSM_BATCH_RUNNER(RunVolume, k_volume,
                  (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi,
                   unsigned long long* part, cudaStream_t s),
@@ -1355,6 +1494,21 @@ template <typename T>
 void sign_reinit(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi0,
                  T* dout, unsigned* err, cudaStream_t s) {
     dispatch<RunSignReinit, T>(shape, grid, inst, bi, nb, f, phi0, dout, err, s);
+}
+template <typename T>
+void reinit_rec(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* din, T* dout,
+                T* cf, long long ld, unsigned* err, cudaStream_t s) {
+    dispatch<RunReinitRec, T>(shape, grid, inst, bi, nb, f, din, dout, cf, ld, err, s);
+}
+template <typename T>
+void sign_reinit_rec(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi0,
+                     T* dout, T* cf, long long ld, unsigned* err, cudaStream_t s) {
+    dispatch<RunSignReinitRec, T>(shape, grid, inst, bi, nb, f, phi0, dout, cf, ld, err, s);
+}
+template <typename T>
+void adj_reinit_c(int shape, int grid, const Inst* inst, const Brick* bi, int nb, const T* cf, long long ld,
+                  const T* lam, T* lam_out, cudaStream_t s) {
+    dispatch<RunAdjReinitC, T>(shape, grid, inst, bi, nb, cf, ld, lam, lam_out, s);
 }
 template <typename T>
 void bc_reinit(const Inst* inst, int ninst, long long nface, FieldsT<T> f, BC bc, const T* din, T* dout,
@@ -1443,6 +1597,12 @@ void adj_contra(const Flat& fl, FieldsT<T> f, const T* w0, const T* w1, const T*
     template void bc_reinit<T>(const Inst*, int, long long, FieldsT<T>, BC, const T*, T*, cudaStream_t);              \
     template void sign_reinit<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, unsigned*,      \
                                  cudaStream_t);                                                                   \
+    template void reinit_rec<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, T*, long long,  \
+                                unsigned*, cudaStream_t);                                                       \
+    template void sign_reinit_rec<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, T*,        \
+                                     long long, unsigned*, cudaStream_t);                                       \
+    template void adj_reinit_c<T>(int, int, const Inst*, const Brick*, int, const T*, long long, const T*, T*,      \
+                                  cudaStream_t);                                                                \
     template void volume<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, unsigned long long*,   \
                              cudaStream_t);                                                                          \
     template void adj_face<T>(const Flat&, int, long long, BC, int, const T*, const T*, const T*, double, double, T*, \

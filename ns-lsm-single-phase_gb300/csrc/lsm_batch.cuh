@@ -101,6 +101,14 @@ void sign_reinit(int shape, int grid, const Inst* inst, const Brick* bricks, int
 template <typename T>
 void bc_reinit(const Inst* inst, int ninst, long long nface, FieldsT<T> f, BC bc, const T* din, T* dout,
                cudaStream_t s);
+// reinit / sign_reinit of a recorded step that also write the pseudo-step's
+// adjoint coefficients A'_0..2, B'_0..2 (cf, arrays ld apart)
+template <typename T>
+void reinit_rec(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f, const T* din,
+                T* dout, T* cf, long long ld, unsigned* err, cudaStream_t s);
+template <typename T>
+void sign_reinit_rec(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f,
+                     const T* phi0, T* dout, T* cf, long long ld, unsigned* err, cudaStream_t s);
 // water volume of every instance: k_volume adds 64-bit fixed-point sums
 // (K, S, bulk) to acc[3 * inst + c] (zero on entry); volume_final writes
 // vols[4 * inst + 0..3] = (K, S, bulk, total) and clears acc
@@ -157,6 +165,11 @@ void adj_stage(const int* grid, const Inst* inst, const Brick* const* bmap, cons
 template <typename T>
 void adj_reinit(int grid, const Inst* inst, const Brick* bmap, int nb, FieldsT<T> f, const T* d, const T* lam,
                 T* lam_out, cudaStream_t s);
+// Reverse of one recorded pseudo-step from the coefficients reinit_rec
+// stored: a 7-point stencil on lam (forward brick table)
+template <typename T>
+void adj_reinit_c(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, const T* cf, long long ld,
+                  const T* lam, T* lam_out, cudaStream_t s);
 // resident blocks per SM of the kernel of adjoint map `map`
 template <typename T>
 int adj_blocks_per_sm(int map);

@@ -264,19 +264,24 @@ FieldsT<float>& fields<float>(lsm_batch* b) { return b->f32; }
 template <>
 FieldsT<double>& fields<double>(lsm_batch* b) { return b->f64; }
 
-// Recorded internals of one step (adjoint): the three stage outputs, the
-// RNitermax raw pseudo-step outputs (D + k ld) and the sign field.
+// Recorded internals of one step (adjoint): the three stage outputs and
+//   adjoint_mode 0: the raw last pseudo-step output (D) and each
+//                   pseudo-step's adjoint coefficients (C + 6 k ld);
+//   adjoint_mode 1: the RNitermax raw pseudo-step outputs (D + k ld) and
+//                   the sign field.
 template <typename T>
 struct Rec {
     T* A[3];
     T* D;
-    T* sgn;
+    T* sgn;   // mode 1 only
+    T* C;     // mode 0 only
 };
 
-// the pseudo-step outputs of a recorded step are b->ld elements apart
+// raw output of pseudo-step k of a recorded step (mode 1: every k; mode 0:
+// the last one only)
 template <typename T>
 T* rec_d(const lsm_batch* b, const Rec<T>& r, int k) {
-    return r.D + (long long)k * (long long)b->ld;
+    return b->cfg.adjoint_mode == 0 ? r.D : r.D + (long long)k * (long long)b->ld;
 }
 
 // One physical step phin -> phi_out (phi_out may alias phin; nullptr skips
@@ -290,7 +295,8 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
     const int sh = b->shape, gr = b->grid, nb = b->nbricks;
     const B::BC bc = make_bc(b);
     FieldsT<T> f = fields<T>(b);
-    if (rec) f.sgn = rec->sgn;
+    const bool coef = rec && b->cfg.adjoint_mode == 0;   // recorded step storing adjoint coefficients
+    if (rec && !coef) f.sgn = rec->sgn;
     if (vol) {
         B::volume<T>(sh, gr, b->d_inst, b->d_brick, nb, f, phin, b->d_vacc, b->stream);
         B::volume_final(b->ninst, b->d_vacc, b->d_vols, b->stream);
@@ -313,10 +319,20 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
         const T* cur = S[2];
         for (int it = 0; it < R; ++it) {
             const bool last = it == R - 1;
-            T* o = rec ? rec_d(b, *rec, it) : (last ? phi_out : f.d[it & 1]);
+            T* o = coef ? (last ? rec->D : f.d[it & 1]) : rec ? rec_d(b, *rec, it) : (last ? phi_out : f.d[it & 1]);
             unsigned* err = (last && !rec) ? b->d_err : nullptr;
-            if (it == 0) B::sign_reinit<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, err, b->stream);
-            else B::reinit<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, err, b->stream);
+            if (coef) {
+                T* cf = rec->C + 6LL * it * (long long)b->ld;
+                if (it == 0)
+                    B::sign_reinit_rec<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, cf, (long long)b->ld, err,
+                                          b->stream);
+                else
+                    B::reinit_rec<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, cf, (long long)b->ld, err, b->stream);
+            } else if (it == 0) {
+                B::sign_reinit<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, err, b->stream);
+            } else {
+                B::reinit<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, err, b->stream);
+            }
             if (last && !rec) B::bc_reinit<T>(b->d_inst, b->ninst, b->nface, f, bc, cur, phi_out, b->stream);
             cur = o;
         }
@@ -409,8 +425,8 @@ int check_inst(lsm_batch* b, int q) {
 
 // ------------------------------------------------------------ adjoint state
 // Checkpoints (nck arrays), segment states (ck), the recorded internals of
-// every step of a segment (ck (4 + R): A1..A3, D1..DR, sign), adjoint
-// fields lam, lam2, lamPhin (3), lamW (3), lam_u (3); arrays b->ld apart.
+// every step of a segment (ck slots, Rec), adjoint fields lam, lam2,
+// lamPhin (3), lamW (3), lam_u (3); arrays b->ld apart.
 template <typename T>
 struct AdjView {
     T *ckpt, *seg, *slots, *lam, *lam2, *lamPhin, *lamW[3], *lamU[3];
@@ -418,7 +434,10 @@ struct AdjView {
 
 int n_ckpt(int nsteps, int ck) { return (nsteps + ck - 1) / ck; }
 // arrays of one recorded step, each b->ld elements apart
-long long slot_elems(const lsm_batch* b) { return (long long)(4 + b->cfg.RNitermax) * (long long)b->ld; }
+long long slot_elems(const lsm_batch* b) {
+    const long long R = b->cfg.RNitermax;
+    return (b->cfg.adjoint_mode == 0 ? 4 + 6 * R : 4 + R) * (long long)b->ld;
+}
 
 size_t adj_elems(const lsm_batch* b, int nsteps, int ck) {
     return b->ld * (size_t)(n_ckpt(nsteps, ck) + ck + 3 + 3 + 3) + (size_t)ck * (size_t)slot_elems(b);
@@ -431,7 +450,13 @@ Rec<T> slot(lsm_batch* b, const AdjView<T>& v, int q) {
     Rec<T> r;
     for (int s = 0; s < 3; ++s) r.A[s] = p + s * L;
     r.D = p + 3 * L;
-    r.sgn = p + (3 + b->cfg.RNitermax) * L;
+    if (b->cfg.adjoint_mode == 0) {
+        r.C = p + 4 * L;
+        r.sgn = nullptr;
+    } else {
+        r.C = nullptr;
+        r.sgn = p + (3 + b->cfg.RNitermax) * L;
+    }
     return r;
 }
 
@@ -519,7 +544,7 @@ template <typename T>
 void adj_step(lsm_batch* b, AdjView<T>& v, const Rec<T>& r, const T* phin) {
     namespace B = lsm::batch;
     FieldsT<T> f = fields<T>(b);
-    f.sgn = r.sgn;
+    if (r.sgn) f.sgn = r.sgn;
     const B::BC bc = make_bc(b);
     const long long N = b->N;
     const Flat fl{b->d_inst, b->d_offs, b->ninst, N};
@@ -531,8 +556,13 @@ void adj_step(lsm_batch* b, AdjView<T>& v, const Rec<T>& r, const T* phin) {
     if (R > 0) {
         faces(1, nullptr, nullptr, rec_d(b, r, R - 1), 0.0, 0.0);
         for (int k = R - 1; k >= 0; --k) {
-            const T* dk = k == 0 ? r.A[2] : rec_d(b, r, k - 1);
-            B::adj_reinit<T>(b->agrid[3], b->d_inst, b->d_amap[3], b->namap[3], f, dk, v.lam, v.lam2, b->stream);
+            if (r.C) {
+                B::adj_reinit_c<T>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, r.C + 6LL * k * (long long)b->ld,
+                                   (long long)b->ld, v.lam, v.lam2, b->stream);
+            } else {
+                const T* dk = k == 0 ? r.A[2] : rec_d(b, r, k - 1);
+                B::adj_reinit<T>(b->agrid[3], b->d_inst, b->d_amap[3], b->namap[3], f, dk, v.lam, v.lam2, b->stream);
+            }
             std::swap(v.lam, v.lam2);
         }
     } else {
@@ -606,7 +636,9 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
         if (inst[q].ni < 4 || inst[q].nj < 4 || inst[q].nk < 4) return LSM_ERR_BAD_SHAPE;
     for (int f = 0; f < 6; ++f)
         if (cfg->btype_lsm[f] < 0 || cfg->btype_lsm[f] > 2) return LSM_ERR_BAD_PARAM;
-    if (cfg->RNitermax < 0 || (cfg->precision != 0 && cfg->precision != 1)) return LSM_ERR_BAD_PARAM;
+    if (cfg->RNitermax < 0 || (cfg->precision != 0 && cfg->precision != 1) ||
+        (cfg->adjoint_mode != 0 && cfg->adjoint_mode != 1))
+        return LSM_ERR_BAD_PARAM;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
         cudaGetLastError();

@@ -50,7 +50,7 @@ module lsm_iso_c
    type, bind(C) :: lsm_batch_config
       integer(c_int) :: RNitermax, btype_lsm(6)
       real(c_double) :: BigPhi
-      integer(c_int) :: use_graph, autotune, shape, precision
+      integer(c_int) :: use_graph, autotune, shape, precision, adjoint_mode
    end type lsm_batch_config
 
    interface

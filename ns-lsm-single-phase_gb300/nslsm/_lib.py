@@ -56,7 +56,7 @@ class LsmBatchConfig(C.Structure):
     """struct lsm_batch_config"""
     _fields_ = [("RNitermax", C.c_int), ("btype_lsm", C.c_int * 6), ("BigPhi", C.c_double),
                 ("use_graph", C.c_int), ("autotune", C.c_int), ("shape", C.c_int),
-                ("precision", C.c_int)]
+                ("precision", C.c_int), ("adjoint_mode", C.c_int)]
 
 
 EXCHANGE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.POINTER(LsmGrid))

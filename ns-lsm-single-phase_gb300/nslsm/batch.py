@@ -41,10 +41,15 @@ def _torch_sync(*arrays) -> None:
 class LevelSetBatch:
     def __init__(self, instances: Sequence[Tuple[int, int, int, float, float, float]], RNitermax: int = 5,
                  btype: Sequence[int] = (1, 1, 1, 1, 1, 1), BigPhi: float = 5.0, device: int = 0, stream=None,
-                 use_graph: bool = True, autotune: bool = True, shape: int = 0, precision: str = "fp32"):
-        """instances: (ni, nj, nk, dt, dtau, eps) per instance; precision "fp32" or "fp64"."""
+                 use_graph: bool = True, autotune: bool = True, shape: int = 0, precision: str = "fp32",
+                 adjoint_mode: str = "store"):
+        """instances: (ni, nj, nk, dt, dtau, eps) per instance; precision "fp32" or "fp64";
+        adjoint_mode "store" (recorded pseudo-steps keep their adjoint coefficients: 6 arrays each)
+        or "recompute" (the reverse sweep re-derives them: 1 array each)."""
         if precision not in ("fp32", "fp64"):
             raise ValueError("precision must be 'fp32' or 'fp64'")
+        if adjoint_mode not in ("store", "recompute"):
+            raise ValueError("adjoint_mode must be 'store' or 'recompute'")
         self.lib = _lib.load()
         n = len(instances)
         arr = (_lib.LsmBatchInstance * n)()
@@ -58,7 +63,9 @@ class LevelSetBatch:
         cfg.BigPhi = float(BigPhi)
         cfg.use_graph, cfg.autotune, cfg.shape = int(use_graph), int(autotune), int(shape)
         cfg.precision = 1 if precision == "fp64" else 0
+        cfg.adjoint_mode = 0 if adjoint_mode == "store" else 1
         self.precision = precision
+        self.adjoint_mode = adjoint_mode
         h = C.c_void_p()
         st = self.lib.lsm_batch_create(C.byref(h), int(device), stream, n, arr, C.byref(cfg))
         if st != 0:
@@ -118,6 +125,16 @@ class LevelSetBatch:
         return v
 
     # ------------------------------------------------------------ adjoint
+    @staticmethod
+    def adjoint_bytes(nodes: int, RNitermax: int, nsteps: int, checkpoint_every: int, precision: str = "fp32",
+                      adjoint_mode: str = "store") -> int:
+        """Device bytes forward_record allocates for the adjoint state (padding ignored):
+        N (ceil(nsteps / k) + k (5 + c R) + 9) elements, c = 6 (store) or 1 (recompute)."""
+        c = 6 if adjoint_mode == "store" else 1
+        k = int(checkpoint_every)
+        arrays = -(-int(nsteps) // k) + k * (5 + c * int(RNitermax)) + 9
+        return int(nodes) * arrays * (8 if precision == "fp64" else 4)
+
     def forward_record(self, nsteps: int, checkpoint_every: int = 4):
         self._chk(self.lib.lsm_batch_forward_record(self.h, int(nsteps), int(checkpoint_every)),
                   "lsm_batch_forward_record")

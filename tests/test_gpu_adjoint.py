@@ -88,9 +88,10 @@ def test_fp64_batch_forward_matches_oracle(oracle, adj_cases, R):
     b.close()
 
 
+@pytest.mark.parametrize("mode", ["store", "recompute"])
 @pytest.mark.parametrize("R", [0, 3])
-def test_fp64_adjoint_matches_torch_tape(adj_cases, R):
-    b = _batch(adj_cases, R)
+def test_fp64_adjoint_matches_torch_tape(adj_cases, R, mode):
+    b = _batch(adj_cases, R, adjoint_mode=mode)
     wts = _weights(adj_cases)
     gphi, gq = _adjoint(b, adj_cases, wts)
     b.close()
@@ -149,11 +150,12 @@ def test_fp64_adjoint_matches_central_differences(adj_cases):
     assert scored >= 16 and worst <= 1e-4, (scored, worst)
 
 
-def test_checkpoint_interval_does_not_change_gradient(adj_cases):
+@pytest.mark.parametrize("mode", ["store", "recompute"])
+def test_checkpoint_interval_does_not_change_gradient(adj_cases, mode):
     wts = _weights(adj_cases)
     outs = []
     for ck in (1, 2, 5):
-        b = _batch(adj_cases, 2)
+        b = _batch(adj_cases, 2, adjoint_mode=mode)
         outs.append(_adjoint(b, adj_cases, wts, nsteps=5, ck=ck))
         b.close()
     for o in outs[1:]:
@@ -259,3 +261,19 @@ def test_second_backward_repeats_the_gradient(adj_cases, ck):
         assert np.array_equal(b.get_grad_phi0(k), g1[k])
         assert np.array_equal(b.get_grad_velocity(k), q1[k])
     b.close()
+
+
+def test_adjoint_modes_agree(adj_cases):
+    """Stored coefficients (the forward's own Godunov selections) and the
+    reverse sweep's recomputation give the same FP64 gradient to rounding,
+    and the same FP32 gradient to FP32 rounding."""
+    wts = _weights(adj_cases)
+    for prec, tol in (("fp64", 1e-13), ("fp32", 1e-5)):
+        res = {}
+        for mode in ("store", "recompute"):
+            b = _batch(adj_cases, 3, precision=prec, adjoint_mode=mode, autotune=False)
+            res[mode] = _adjoint(b, adj_cases, wts)
+            b.close()
+        for k in range(len(adj_cases)):
+            assert _rel(res["store"][0][k], res["recompute"][0][k]) <= tol
+            assert _rel(res["store"][1][k], res["recompute"][1][k]) <= tol
