@@ -585,7 +585,10 @@ int backward_t(lsm_batch* b) {
     const AdjView<T> canon = v;
     const long long N = b->N;
     T* const zero_fields[7] = {v.lamPhin, v.lamW[0], v.lamW[1], v.lamW[2], v.lamU[0], v.lamU[1], v.lamU[2]};
-    for (T* p : zero_fields) k_zero<T><<<cblocks(N), 256, 0, b->stream>>>(N, p);
+    for (T* p : zero_fields) {
+        lsm::ProfScope ps("k_zero", b->stream);
+        k_zero<T><<<cblocks(N), 256, 0, b->stream>>>(N, p);
+    }
     const int ck = b->rec_ck, nsteps = b->rec_steps, nseg = n_ckpt(nsteps, ck);
     const long long LD = (long long)b->ld;
     for (int sg = nseg - 1; sg >= 0; --sg) {
