@@ -807,10 +807,10 @@ __device__ void cell_water_fast(const P (&ph8)[8], const P (&C)[8][3], double* K
 // in cell order) so their geometry runs on dense lanes, in the stencil
 // precision T (FP32: each interface cell's share carries a relative
 // rounding error of about 1e-7 of that cell's volume).  Every thread keeps
-// 64-bit integer sums over the bricks of one instance; the CTA reduces
-// them and adds them to the instance's accumulators with integer atomics
-// when the instance changes and at the end (exact and order-independent:
-// the result does not depend on the schedule).
+// 64-bit integer sums over the bricks of one instance; each warp adds them
+// to the instance's accumulators with integer atomics when its CTA moves to
+// another instance and at the end (exact and order-independent: the result
+// does not depend on the schedule; no block-wide barrier).
 __device__ __forceinline__ long long warp_sum_ll(long long v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -821,30 +821,18 @@ template <typename T, int TX, int TY, int TZ>
 __global__ void __launch_bounds__(TX * TY * TZ) k_volume(const Inst* __restrict__ inst,
         const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phi,
         unsigned long long* __restrict__ acc) {
-    constexpr int NT = TX * TY * TZ, NW = NT / 32;
+    constexpr int NW = TX * TY * TZ / 32;
     const T eps = T(kEpsSims);
-    __shared__ long long red[3][NW];
     __shared__ long long slot[NW][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     long long Kq = 0, Sq = 0, Bq = 0;
     int cur = -1;
-    // block-uniform: every thread of the CTA walks the same bricks
+    // warp-uniform (every thread of the CTA walks the same bricks)
     auto flush = [&]() {
-        Kq = warp_sum_ll(Kq);
-        Sq = warp_sum_ll(Sq);
-        Bq = warp_sum_ll(Bq);
-        if (lane == 0) {
-            red[0][w] = Kq;
-            red[1][w] = Sq;
-            red[2][w] = Bq;
-        }
-        __syncthreads();
-        if (threadIdx.x < 3) {
-            long long a = 0;
-            for (int q = 0; q < NW; ++q) a += red[threadIdx.x][q];
-            if (a != 0) atomicAdd(acc + 3 * (long long)cur + threadIdx.x, (unsigned long long)a);
-        }
-        __syncthreads();
+        const long long v[3] = {warp_sum_ll(Kq), warp_sum_ll(Sq), warp_sum_ll(Bq)};
+        if (lane == 0)
+            for (int c = 0; c < 3; ++c)
+                if (v[c] != 0) atomicAdd(acc + 3 * (long long)cur + c, (unsigned long long)v[c]);
         Kq = Sq = Bq = 0;
     };
     for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
@@ -860,13 +848,16 @@ __global__ void __launch_bounds__(TX * TY * TZ) k_volume(const Inst* __restrict_
         if (b.i < I.ni - 1 && b.j < I.nj - 1 && b.k < I.nk - 1) {
             l = I.off + b.i + sj * b.j + sk * b.k;
             const long long o[8] = {l, l + 1, l + 1 + sj, l + sj, l + sk, l + 1 + sk, l + 1 + sj + sk, l + sj + sk};
+            // the cell volume is fetched with the corners (one memory round
+            // trip per brick; it is used for water cells only)
+            const long long cv = __ldg(f.cellfix + l);
             bool allw = true, alla = true;
 #pragma unroll
             for (int v = 0; v < 8; ++v) {
                 const T p = __ldg(phi + o[v]);
                 allw &= p > eps; alla &= p < -eps;
             }
-            if (allw) Bq += __ldg(f.cellfix + l);
+            if (allw) Bq += cv;
             mix = !allw && !alla;
         }
         const unsigned m = __ballot_sync(0xffffffffu, mix);

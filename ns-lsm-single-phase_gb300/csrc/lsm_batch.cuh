@@ -121,6 +121,8 @@ void volume_final(int ninst, unsigned long long* acc, double* vols, cudaStream_t
 // instance's first node
 void cell_hex(long long off, int ni, int nj, int nk, const double* x, const double* y, const double* z,
               long long* cellfix, cudaStream_t s);
+// resident CTAs per SM of a brick kernel of tile shape `shape` (FP32):
+// kernel 0 k_contra, 1 k_reinit, other k_volume
 int max_blocks_per_sm(int shape, int kernel);
 
 // ------------------------------------------------------------ adjoint
