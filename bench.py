@@ -681,18 +681,27 @@ def run_fwdadj(args):
     h_gphi, t5 = pinned(np.zeros(g.shape))
     h_gq, t6 = pinned(np.zeros((4,) + g.shape))
     keep = (t1, t2, t3, t4, t5, t6)
-    e2e_steps = 2
+    e2e_steps = 3
+    parts = {}
+
+    def part(name, fn):
+        t = time.perf_counter()
+        fn()
+        parts[name] = parts.get(name, 0.0) + (time.perf_counter() - t) * 1e3 / e2e_steps
+
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        b.set_phi(0, h_phi)
-        b.set_velocity(0, h_q)
-        b.forward_record(S, S)
-        b._chk(b.lib.lsm_batch_get_phi(b.h, 0, h_phiT.ctypes.data), "get_phi")
-        b.set_grad_phi(0, h_w)
-        b.backward()
-        b._chk(b.lib.lsm_batch_get_grad_phi0(b.h, 0, h_gphi.ctypes.data), "get_grad_phi0")
-        b._chk(b.lib.lsm_batch_get_grad_velocity(b.h, 0, h_gq.ctypes.data), "get_grad_velocity")
+        part("set_phi", lambda: b.set_phi(0, h_phi))
+        part("set_velocity", lambda: b.set_velocity(0, h_q))
+        part("forward_record", lambda: b.forward_record(S, S))
+        part("get_phi", lambda: b._chk(b.lib.lsm_batch_get_phi(b.h, 0, h_phiT.ctypes.data), "get_phi"))
+        part("set_grad_phi", lambda: b.set_grad_phi(0, h_w))
+        part("backward", lambda: b.backward())
+        part("get_grad_phi0", lambda: b._chk(b.lib.lsm_batch_get_grad_phi0(b.h, 0, h_gphi.ctypes.data),
+                                             "get_grad_phi0"))
+        part("get_grad_velocity", lambda: b._chk(b.lib.lsm_batch_get_grad_velocity(b.h, 0, h_gq.ctypes.data),
+                                                 "get_grad_velocity"))
     torch.cuda.synchronize()
     e2e_s = dist_max(time.perf_counter() - t0, world)
     e2e_value = world * n * S * e2e_steps / e2e_s / 1e9
@@ -771,7 +780,8 @@ def run_fwdadj(args):
             "accuracy_vs_fp64": {"steps": nc, "band_linf_phi_err": band_err, "band": "|phi64| < 4 epslsm (6 cells)",
                                  "volume_rel_diff": vol_err},
             "e2e": {"value": e2e_value, "unit": "Gcell-steps/s", "h2d_bytes_per_step": 8 * n * (1 + 4 + 1),
-                    "d2h_bytes_per_step": 8 * n * (1 + 1 + 4), "steps": e2e_steps},
+                    "d2h_bytes_per_step": 8 * n * (1 + 1 + 4), "steps": e2e_steps,
+                    "ms_per_call": {k: round(v, 1) for k, v in parts.items()}},
             "clocks": clocks.summary(),
             "gpu_launches": launches,
             "kernel_times_ms": {k: {"launches": v[0], "total_ms": round(v[1], 4)} for k, v in prof.items()},
