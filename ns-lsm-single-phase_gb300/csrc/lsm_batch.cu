@@ -613,34 +613,83 @@ __global__ void __launch_bounds__(TX * TY * TZ) k_sign_reinit_rec(const Inst* __
 }
 
 // Reverse of one recorded pseudo-step from its stored coefficients (cf:
-// A'_0..2, B'_0..2, ld apart); every load is issued before the arithmetic
-template <typename T, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(TX * TY * TZ) k_adj_reinit_c(const Inst* __restrict__ inst,
-        const Brick* __restrict__ bricks, int nbricks, const T* __restrict__ cf, long long ld,
-        const T* __restrict__ lam, T* __restrict__ lam_out) {
-    for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
-        if (!b.valid) continue;
-        const Inst& I = inst[b.inst];
-        const long long st[3] = {1, (long long)I.ni, (long long)I.ni * I.nj};
-        const long long l = I.off + b.i + st[1] * b.j + st[2] * b.k;
-        const int c3d[3] = {b.i, b.j, b.k}, n3[3] = {I.ni, I.nj, I.nk};
-        const T L = __ldg(lam + l);
-        T A[3], B[3], Lp[3], Ap[3], Lm[3], Bm[3];
+// A'_0..2, B'_0..2, ld apart), on the tiles of adjoint map 2 (32 x 8
+// columns marching 32 planes in k).  Each node loads its own lam and six
+// coefficients once (one plane ahead); the z neighbours (lam, A'_2 above,
+// B'_2 below) stay in registers, the x neighbours come by warp shuffles
+// (the tile's edge lanes load the one outside), the y neighbours are
+// loaded (L1/L2).
+template <typename T>
+__global__ void __launch_bounds__(256) k_adj_reinit_c(const Inst* __restrict__ inst, const Brick* __restrict__ bmap,
+        int nb, const T* __restrict__ cf, long long ld, const T* __restrict__ lam, T* __restrict__ lam_out) {
+    const unsigned FM = 0xffffffffu;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int blk = blockIdx.x; blk < nb; blk += gridDim.x) {
+        const ABrick ab = adj_brick(bmap, 2, blk);
+        const Inst& I = inst[ab.inst];
+        const int ni = I.ni, nj = I.nj, nk = I.nk;
+        const long long sj = ni, sk = (long long)ni * nj;
+        const int i = ab.i0 + tx, j = ab.j0 + ty;
+        const int k0 = ab.k0, k1 = min(k0 + adj_shape(2).oz, nk);
+        const bool col = i < ni && j < nj;
+        const long long cb = I.off + i + sj * j;
+        const bool xm = i > 0, xp = i < ni - 1, ym = j > 0, yp = j < nj - 1;
+        const bool exm = col && xm && tx == 0, exp_ = col && xp && tx == 31;
+        // own values of a plane: lam, A'_0..2, B'_0..2; the x-edge lanes' outside
+        // neighbour (lam, and A'_0 above / B'_0 below); the y neighbours
+        struct Plane {
+            T L, A[3], B[3], Le, Ce, Lym, Bym, Lyp, Ayp;
+        };
+        auto ld_plane = [&](int k, Plane& p) {
+            p.L = p.Le = p.Ce = p.Lym = p.Bym = p.Lyp = p.Ayp = T(0);
 #pragma unroll
-        for (int m = 0; m < 3; ++m) {
-            A[m] = __ldg(cf + m * ld + l);
-            B[m] = __ldg(cf + (3 + m) * ld + l);
-            const bool up = c3d[m] < n3[m] - 1, dn = c3d[m] > 0;
-            Lp[m] = up ? __ldg(lam + l + st[m]) : T(0);
-            Ap[m] = up ? __ldg(cf + m * ld + l + st[m]) : T(0);
-            Lm[m] = dn ? __ldg(lam + l - st[m]) : T(0);
-            Bm[m] = dn ? __ldg(cf + (3 + m) * ld + l - st[m]) : T(0);
+            for (int m = 0; m < 3; ++m) p.A[m] = p.B[m] = T(0);
+            if (!col || k < 0 || k >= nk) return;
+            const long long l = cb + sk * k;
+            p.L = __ldg(lam + l);
+#pragma unroll
+            for (int m = 0; m < 3; ++m) {
+                p.A[m] = __ldg(cf + m * ld + l);
+                p.B[m] = __ldg(cf + (3 + m) * ld + l);
+            }
+            if (exm) {
+                p.Le = __ldg(lam + l - 1);
+                p.Ce = __ldg(cf + 3 * ld + l - 1);
+            }
+            if (exp_) {
+                p.Le = __ldg(lam + l + 1);
+                p.Ce = __ldg(cf + l + 1);
+            }
+            if (ym) {
+                p.Lym = __ldg(lam + l - sj);
+                p.Bym = __ldg(cf + 4 * ld + l - sj);
+            }
+            if (yp) {
+                p.Lyp = __ldg(lam + l + sj);
+                p.Ayp = __ldg(cf + ld + l + sj);
+            }
+        };
+        Plane pm, pc, pn;          // planes k-1, k, k+1
+        ld_plane(k0 - 1, pm);
+        ld_plane(k0, pc);
+        for (int k = k0; k < k1; ++k) {
+            ld_plane(k + 1, pn);
+            // x neighbours: lam and A'_0 of i+1, lam and B'_0 of i-1
+            const T Lxp = __shfl_down_sync(FM, pc.L, 1), Axp = __shfl_down_sync(FM, pc.A[0], 1);
+            const T Lxm = __shfl_up_sync(FM, pc.L, 1), Bxm = __shfl_up_sync(FM, pc.B[0], 1);
+            if (col) {
+                const T L = pc.L;
+                const T lxp = xp ? (tx == 31 ? pc.Le : Lxp) : T(0), axp = xp ? (tx == 31 ? pc.Ce : Axp) : T(0);
+                const T lxm = xm ? (tx == 0 ? pc.Le : Lxm) : T(0), bxm = xm ? (tx == 0 ? pc.Ce : Bxm) : T(0);
+                const bool zm = k > 0, zp = k < nk - 1;
+                const T t0 = L * pc.A[0] - L * pc.B[0] - lxp * axp + lxm * bxm;
+                const T t1 = L * pc.A[1] - L * pc.B[1] - pc.Lyp * pc.Ayp + pc.Lym * pc.Bym;
+                const T t2 = L * pc.A[2] - L * pc.B[2] - (zp ? pn.L * pn.A[2] : T(0)) + (zm ? pm.L * pm.B[2] : T(0));
+                lam_out[cb + sk * k] = L - t0 - t1 - t2;
+            }
+            pm = pc;
+            pc = pn;
         }
-        T t[3];
-#pragma unroll
-        for (int m = 0; m < 3; ++m) t[m] = L * A[m] - L * B[m] - Lp[m] * Ap[m] + Lm[m] * Bm[m];
-        lam_out[l] = L - t[0] - t[1] - t[2];
     }
 }
 
@@ -1419,10 +1468,6 @@ LSM_BATCH_RUNNER(RunSignReinitRec, k_sign_reinit_rec,
                  (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* p0, T* dout, T* cf,
                   long long ld, unsigned* err, cudaStream_t s),
                  (inst, bi, nb, f, p0, dout, cf, ld, err))
-LSM_BATCH_RUNNER(RunAdjReinitC, k_adj_reinit_c,
-                 (int grid, const Inst* inst, const Brick* bi, int nb, const T* cf, long long ld, const T* lam,
-                  T* lam_out, cudaStream_t s),
-                 (inst, bi, nb, cf, ld, lam, lam_out))
 LSM_BATCH_RUNNER(RunVolume, k_volume,
                  (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi,
                   unsigned long long* part, cudaStream_t s),
@@ -1497,9 +1542,16 @@ void sign_reinit_rec(int shape, int grid, const Inst* inst, const Brick* bi, int
     dispatch<RunSignReinitRec, T>(shape, grid, inst, bi, nb, f, phi0, dout, cf, ld, err, s);
 }
 template <typename T>
-void adj_reinit_c(int shape, int grid, const Inst* inst, const Brick* bi, int nb, const T* cf, long long ld,
-                  const T* lam, T* lam_out, cudaStream_t s) {
-    dispatch<RunAdjReinitC, T>(shape, grid, inst, bi, nb, cf, ld, lam, lam_out, s);
+void adj_reinit_c(int grid, const Inst* inst, const Brick* bmap2, int nb, const T* cf, long long ld, const T* lam,
+                  T* lam_out, cudaStream_t s) {
+    ProfScope ps_("k_adj_reinit_c", s);
+    k_adj_reinit_c<T><<<grid, 256, 0, s>>>(inst, bmap2, nb, cf, ld, lam, lam_out);
+}
+template <typename T>
+int adj_reinit_c_blocks_per_sm() {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adj_reinit_c<T>, 256, 0);
+    return n;
 }
 template <typename T>
 void bc_reinit(const Inst* inst, int ninst, long long nface, FieldsT<T> f, BC bc, const T* din, T* dout,
@@ -1592,8 +1644,9 @@ void adj_contra(const Flat& fl, FieldsT<T> f, const T* w0, const T* w1, const T*
                                 unsigned*, cudaStream_t);                                                       \
     template void sign_reinit_rec<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, T*,        \
                                      long long, unsigned*, cudaStream_t);                                       \
-    template void adj_reinit_c<T>(int, int, const Inst*, const Brick*, int, const T*, long long, const T*, T*,      \
+    template void adj_reinit_c<T>(int, const Inst*, const Brick*, int, const T*, long long, const T*, T*,           \
                                   cudaStream_t);                                                                \
+    template int adj_reinit_c_blocks_per_sm<T>();                                                               \
     template void volume<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, unsigned long long*,   \
                              cudaStream_t);                                                                          \
     template void adj_face<T>(const Flat&, int, long long, BC, int, const T*, const T*, const T*, double, double, T*, \

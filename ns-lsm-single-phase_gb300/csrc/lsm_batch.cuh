@@ -168,10 +168,13 @@ template <typename T>
 void adj_reinit(int grid, const Inst* inst, const Brick* bmap, int nb, FieldsT<T> f, const T* d, const T* lam,
                 T* lam_out, cudaStream_t s);
 // Reverse of one recorded pseudo-step from the coefficients reinit_rec
-// stored: a 7-point stencil on lam (forward brick table)
+// stored: a 7-point stencil on lam, on the tiles of adjoint map 2 (grid
+// from adj_reinit_c_blocks_per_sm)
 template <typename T>
-void adj_reinit_c(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, const T* cf, long long ld,
-                  const T* lam, T* lam_out, cudaStream_t s);
+void adj_reinit_c(int grid, const Inst* inst, const Brick* bmap2, int nb, const T* cf, long long ld, const T* lam,
+                  T* lam_out, cudaStream_t s);
+template <typename T>
+int adj_reinit_c_blocks_per_sm();
 // resident blocks per SM of the kernel of adjoint map `map`
 template <typename T>
 int adj_blocks_per_sm(int map);

@@ -53,7 +53,7 @@ struct lsm_batch {
     int nbricks = 0;
     lsm::batch::Brick* d_amap[4] = {};  // brick tables of the adjoint stencil kernels (lsm::batch::adj_shape)
     int namap[4] = {0, 0, 0, 0}, agrid[4] = {1, 1, 1, 1};
-    int sgrid = 1;                      // CTAs of the RK stage (on adjoint map 2)
+    int sgrid = 1, acgrid = 1;          // CTAs of the RK stage and of k_adj_reinit_c (on adjoint map 2)
     unsigned long long* d_vacc = nullptr;   // volume accumulators, 3 per instance (k_volume)
     double* d_vols = nullptr;
     double* h_vols = nullptr;    // pinned
@@ -240,6 +240,9 @@ int build_bricks(lsm_batch* b, int shape) {
     const int ps = std::max(1, b->prec ? lsm::batch::stage_blocks_per_sm<double>()
                                        : lsm::batch::stage_blocks_per_sm<float>());
     b->sgrid = std::max(1, std::min(b->namap[2], sms * ps));
+    const int pac = std::max(1, b->prec ? lsm::batch::adj_reinit_c_blocks_per_sm<double>()
+                                        : lsm::batch::adj_reinit_c_blocks_per_sm<float>());
+    b->acgrid = std::max(1, std::min(b->namap[2], sms * pac));
     b->shape = shape;
     BCU(b, cudaStreamSynchronize(b->stream));
     return LSM_OK;
@@ -557,7 +560,7 @@ void adj_step(lsm_batch* b, AdjView<T>& v, const Rec<T>& r, const T* phin) {
         faces(1, nullptr, nullptr, rec_d(b, r, R - 1), 0.0, 0.0);
         for (int k = R - 1; k >= 0; --k) {
             if (r.C) {
-                B::adj_reinit_c<T>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, r.C + 6LL * k * (long long)b->ld,
+                B::adj_reinit_c<T>(b->acgrid, b->d_inst, b->d_amap[2], b->namap[2], r.C + 6LL * k * (long long)b->ld,
                                    (long long)b->ld, v.lam, v.lam2, b->stream);
             } else {
                 const T* dk = k == 0 ? r.A[2] : rec_d(b, r, k - 1);
