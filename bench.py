@@ -526,7 +526,7 @@ FWDADJ_BYTES = {
     "k_sign": 11 * 4,              # phi0, metrics(9); s
     "k_reinit": 12 * 4,            # d, s, metrics(9); d
     "k_sign_reinit": 12 * 4,       # phi0, metrics(9); s, d
-    "k_reinit_rec": 18 * 4,        # d, s, metrics(9); d, adjoint coefficients(6)
+    "k_reinit_rec_z": 18 * 4,      # d, s, metrics(9); d, adjoint coefficients(6)
     "k_sign_reinit_rec": 18 * 4,   # phi0, metrics(9); s, d, adjoint coefficients(6)
     "k_adj_reinit_c": 8 * 4,       # lam, coefficients(6); lam_out
     "k_volume": 4 + 8,             # phi (FP32) + fixed-point cell volume (interface-cell coordinates not counted)

@@ -528,6 +528,24 @@ __global__ void __launch_bounds__(TX * TY * TZ) k_sign_reinit(const Inst* __rest
 //                - lam(j+e_m) A'_m(j+e_m) + lam(j-e_m) B'_m(j-e_m)].
 // acc is accumulated exactly as in godunov() (bit-identical pseudo-step).
 template <typename T>
+__device__ __forceinline__ T godunov_sel_v(const T (&mas)[3], const T (&men)[3], const T (&M)[9], T sel, T (&e)[3],
+                                           T (&g)[3]) {
+    const T sg = sel > T(0) ? T(1) : T(-1);
+    T acc = T(0);
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+        const T bb = sg * (M[x] * men[0] + M[3 + x] * men[1] + M[6 + x] * men[2]);
+        const T ff = sg * (M[x] * mas[0] + M[3 + x] * mas[1] + M[6 + x] * mas[2]);
+        const T p = vmax(bb, T(0)), q = vmin(ff, T(0));
+        const bool takeP = p * p >= q * q;
+        acc += takeP ? p * p : q * q;
+        e[x] = takeP ? p : T(0);
+        g[x] = takeP ? T(0) : q;
+    }
+    return acc;
+}
+
+template <typename T>
 __device__ __forceinline__ T godunov_sel(const FieldsT<T>& f, const T* __restrict__ d, const Inst& I, long long l,
                                          int i, int j, int k, T sel, T (&M)[9], T (&e)[3], T (&g)[3]) {
     T mas[3], men[3];
@@ -564,25 +582,89 @@ __device__ __forceinline__ void coef_store(const T (&M)[9], const T (&e)[3], con
     }
 }
 
-template <typename T, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(TX * TY * TZ) k_reinit_rec(const Inst* __restrict__ inst,
-        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ din, T* __restrict__ dout,
-        T* __restrict__ cf, long long ld, unsigned* err) {
-    for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
-        if (!b.valid) continue;
-        const Inst& I = inst[b.inst];
-        const long long l = I.off + b.i + (long long)I.ni * (b.j + (long long)I.nj * b.k);
-        const T s = __ldg(f.sgn + l);
-        const T d = __ldg(din + l);
+// A recorded pseudo-step (d' and its adjoint coefficients) on the tiles of
+// adjoint map 2 (32 x 8 columns marching 32 planes in k): each node loads
+// d, s and its metrics once, a plane ahead; the z neighbours of d stay in a
+// register window, the x neighbours come by warp shuffles (the tile's edge
+// lanes load the one outside) and the y neighbours are loaded (L1/L2).  d'
+// is bit-identical to k_reinit's.
+template <typename T>
+__global__ void __launch_bounds__(256) k_reinit_rec_z(const Inst* __restrict__ inst, const Brick* __restrict__ bmap,
+        int nb, FieldsT<T> f, const T* __restrict__ din, T* __restrict__ dout, T* __restrict__ cf, long long ld,
+        unsigned* err) {
+    const unsigned FM = 0xffffffffu;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int blk = blockIdx.x; blk < nb; blk += gridDim.x) {
+        const ABrick ab = adj_brick(bmap, 2, blk);
+        const Inst& I = inst[ab.inst];
+        const int ni = I.ni, nj = I.nj, nk = I.nk;
+        const long long sj = ni, sk = (long long)ni * nj;
+        const int i = ab.i0 + tx, j = ab.j0 + ty;
+        const int k0 = ab.k0, k1 = min(k0 + adj_shape(2).oz, nk);
+        const bool col = i < ni && j < nj;
+        const long long cb = I.off + i + sj * j;
+        const bool xm = i > 0, xp = i < ni - 1, ym = j > 0, yp = j < nj - 1;
+        const bool ex = col && ((tx == 0 && xm) || (tx == 31 && xp));
+        const int eo = tx == 0 ? -1 : 1;
         const T dtau = ipar<T>(I.dtau, I.dtau64);
-        T M[9], e[3], g[3];
-        const T acc = godunov_sel(f, din, I, l, b.i, b.j, b.k, s, M, e, g);
-        const T r = s == T(0) ? d : d - dtau * s * (vsqrt(acc) - T(1));
-        dout[l] = r;
-        coef_store(M, e, g, s != T(0) && acc > T(0) ? dtau * fabs(s) * vrsqrt(acc) : T(0), I, b.i, b.j, b.k, cf, ld,
-                   l);
-        if (err && !vfinite(r)) atomicOr(err, (unsigned)kErrNonFinite);
+        struct Plane {
+            T s, M[9], dxe, dym, dyp;
+        };
+        auto ld_plane = [&](int k, Plane& p) {
+            p.s = p.dxe = p.dym = p.dyp = T(0);
+#pragma unroll
+            for (int c = 0; c < 9; ++c) p.M[c] = T(0);
+            if (!col || k < 0 || k >= nk) return;
+            const long long l = cb + sk * k;
+            p.s = __ldg(f.sgn + l);
+#pragma unroll
+            for (int c = 0; c < 9; ++c) p.M[c] = __ldg(f.m[c] + l);
+            if (ex) p.dxe = __ldg(din + l + eo);
+            if (ym) p.dym = __ldg(din + l - sj);
+            if (yp) p.dyp = __ldg(din + l + sj);
+        };
+        auto ldd = [&](int k) { return col && k >= 0 && k < nk ? __ldg(din + cb + sk * k) : T(0); };
+        T dm = ldd(k0 - 1), dc = ldd(k0), dp = ldd(k0 + 1);
+        Plane pc, pn;
+        ld_plane(k0, pc);
+        for (int k = k0; k < k1; ++k) {
+            const T dn = ldd(k + 2);
+            if (k + 1 < k1) ld_plane(k + 1, pn);
+            const T xl = __shfl_up_sync(FM, dc, 1), xr = __shfl_down_sync(FM, dc, 1);
+            if (col) {
+                // one-sided differences (calc_RH_RN.F90:36-170), as one_sided()
+                const T dxm = tx == 0 ? pc.dxe : xl, dxp = tx == 31 ? pc.dxe : xr;
+                const T nbm[3] = {dxm, pc.dym, dm}, nbp[3] = {dxp, pc.dyp, dp};
+                const bool lo[3] = {!xm, !ym, k == 0}, hi[3] = {!xp, !yp, k == nk - 1};
+                T mas[3], men[3];
+#pragma unroll
+                for (int m = 0; m < 3; ++m) {
+                    const T a = hi[m] ? T(0) : nbp[m] - dc;
+                    const T b = lo[m] ? T(0) : dc - nbm[m];
+                    mas[m] = hi[m] ? b : a;
+                    men[m] = lo[m] ? a : b;
+                }
+                T e[3], g[3];
+                const T acc = godunov_sel_v(mas, men, pc.M, pc.s, e, g);
+                const T s = pc.s;
+                const T r = s == T(0) ? dc : dc - dtau * s * (vsqrt(acc) - T(1));
+                const long long l = cb + sk * k;
+                dout[l] = r;
+                const T w = s != T(0) && acc > T(0) ? dtau * fabs(s) * vrsqrt(acc) : T(0);
+#pragma unroll
+                for (int m = 0; m < 3; ++m) {
+                    const T gmen = pc.M[3 * m] * e[0] + pc.M[3 * m + 1] * e[1] + pc.M[3 * m + 2] * e[2];
+                    const T gmas = pc.M[3 * m] * g[0] + pc.M[3 * m + 1] * g[1] + pc.M[3 * m + 2] * g[2];
+                    cf[m * ld + l] = lo[m] ? T(0) : w * (hi[m] ? gmen + gmas : gmen);
+                    cf[(3 + m) * ld + l] = hi[m] ? T(0) : w * (lo[m] ? gmen + gmas : gmas);
+                }
+                if (err && !vfinite(r)) atomicOr(err, (unsigned)kErrNonFinite);
+            }
+            dm = dc;
+            dc = dp;
+            dp = dn;
+            pc = pn;
+        }
     }
 }
 
@@ -1460,10 +1542,6 @@ LSM_BATCH_RUNNER(RunSignReinit, k_sign_reinit,
                  (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* p0, T* dout,
                   unsigned* err, cudaStream_t s),
                  (inst, bi, nb, f, p0, dout, err))
-LSM_BATCH_RUNNER(RunReinitRec, k_reinit_rec,
-                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* din, T* dout, T* cf,
-                  long long ld, unsigned* err, cudaStream_t s),
-                 (inst, bi, nb, f, din, dout, cf, ld, err))
 LSM_BATCH_RUNNER(RunSignReinitRec, k_sign_reinit_rec,
                  (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* p0, T* dout, T* cf,
                   long long ld, unsigned* err, cudaStream_t s),
@@ -1532,9 +1610,16 @@ void sign_reinit(int shape, int grid, const Inst* inst, const Brick* bi, int nb,
     dispatch<RunSignReinit, T>(shape, grid, inst, bi, nb, f, phi0, dout, err, s);
 }
 template <typename T>
-void reinit_rec(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* din, T* dout,
-                T* cf, long long ld, unsigned* err, cudaStream_t s) {
-    dispatch<RunReinitRec, T>(shape, grid, inst, bi, nb, f, din, dout, cf, ld, err, s);
+void reinit_rec_z(int grid, const Inst* inst, const Brick* bmap2, int nb, FieldsT<T> f, const T* din, T* dout, T* cf,
+                  long long ld, unsigned* err, cudaStream_t s) {
+    ProfScope ps_("k_reinit_rec_z", s);
+    k_reinit_rec_z<T><<<grid, 256, 0, s>>>(inst, bmap2, nb, f, din, dout, cf, ld, err);
+}
+template <typename T>
+int reinit_rec_z_blocks_per_sm() {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_reinit_rec_z<T>, 256, 0);
+    return n;
 }
 template <typename T>
 void sign_reinit_rec(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi0,
@@ -1640,8 +1725,9 @@ void adj_contra(const Flat& fl, FieldsT<T> f, const T* w0, const T* w1, const T*
     template void bc_reinit<T>(const Inst*, int, long long, FieldsT<T>, BC, const T*, T*, cudaStream_t);              \
     template void sign_reinit<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, unsigned*,      \
                                  cudaStream_t);                                                                   \
-    template void reinit_rec<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, T*, long long,  \
-                                unsigned*, cudaStream_t);                                                       \
+    template void reinit_rec_z<T>(int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, T*, long long,     \
+                                  unsigned*, cudaStream_t);                                                     \
+    template int reinit_rec_z_blocks_per_sm<T>();                                                               \
     template void sign_reinit_rec<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, T*,        \
                                      long long, unsigned*, cudaStream_t);                                       \
     template void adj_reinit_c<T>(int, const Inst*, const Brick*, int, const T*, long long, const T*, T*,           \

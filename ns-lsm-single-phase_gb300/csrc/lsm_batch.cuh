@@ -101,14 +101,18 @@ void sign_reinit(int shape, int grid, const Inst* inst, const Brick* bricks, int
 template <typename T>
 void bc_reinit(const Inst* inst, int ninst, long long nface, FieldsT<T> f, BC bc, const T* din, T* dout,
                cudaStream_t s);
-// reinit / sign_reinit of a recorded step that also write the pseudo-step's
-// adjoint coefficients A'_0..2, B'_0..2 (cf, arrays ld apart)
-template <typename T>
-void reinit_rec(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f, const T* din,
-                T* dout, T* cf, long long ld, unsigned* err, cudaStream_t s);
+// sign_reinit / reinit of a recorded step that also write the
+// pseudo-step's adjoint coefficients A'_0..2, B'_0..2 (cf, arrays ld apart)
 template <typename T>
 void sign_reinit_rec(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f,
                      const T* phi0, T* dout, T* cf, long long ld, unsigned* err, cudaStream_t s);
+// reinit_rec on the tiles of adjoint map 2 (z march; grid from
+// reinit_rec_z_blocks_per_sm)
+template <typename T>
+void reinit_rec_z(int grid, const Inst* inst, const Brick* bmap2, int nb, FieldsT<T> f, const T* din, T* dout, T* cf,
+                  long long ld, unsigned* err, cudaStream_t s);
+template <typename T>
+int reinit_rec_z_blocks_per_sm();
 // water volume of every instance: k_volume adds 64-bit fixed-point sums
 // (K, S, bulk) to acc[3 * inst + c] (zero on entry); volume_final writes
 // vols[4 * inst + 0..3] = (K, S, bulk, total) and clears acc

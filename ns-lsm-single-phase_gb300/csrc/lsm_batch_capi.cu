@@ -53,7 +53,7 @@ struct lsm_batch {
     int nbricks = 0;
     lsm::batch::Brick* d_amap[4] = {};  // brick tables of the adjoint stencil kernels (lsm::batch::adj_shape)
     int namap[4] = {0, 0, 0, 0}, agrid[4] = {1, 1, 1, 1};
-    int sgrid = 1, acgrid = 1;          // CTAs of the RK stage and of k_adj_reinit_c (on adjoint map 2)
+    int sgrid = 1, acgrid = 1, rzgrid = 1;   // CTAs of the map-2 kernels: stage, k_adj_reinit_c, k_reinit_rec_z
     unsigned long long* d_vacc = nullptr;   // volume accumulators, 3 per instance (k_volume)
     double* d_vols = nullptr;
     double* h_vols = nullptr;    // pinned
@@ -243,6 +243,9 @@ int build_bricks(lsm_batch* b, int shape) {
     const int pac = std::max(1, b->prec ? lsm::batch::adj_reinit_c_blocks_per_sm<double>()
                                         : lsm::batch::adj_reinit_c_blocks_per_sm<float>());
     b->acgrid = std::max(1, std::min(b->namap[2], sms * pac));
+    const int prz = std::max(1, b->prec ? lsm::batch::reinit_rec_z_blocks_per_sm<double>()
+                                        : lsm::batch::reinit_rec_z_blocks_per_sm<float>());
+    b->rzgrid = std::max(1, std::min(b->namap[2], sms * prz));
     b->shape = shape;
     BCU(b, cudaStreamSynchronize(b->stream));
     return LSM_OK;
@@ -330,7 +333,8 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
                     B::sign_reinit_rec<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, cf, (long long)b->ld, err,
                                           b->stream);
                 else
-                    B::reinit_rec<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, cf, (long long)b->ld, err, b->stream);
+                    B::reinit_rec_z<T>(b->rzgrid, b->d_inst, b->d_amap[2], b->namap[2], f, cur, o, cf, (long long)b->ld,
+                                       err, b->stream);
             } else if (it == 0) {
                 B::sign_reinit<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, err, b->stream);
             } else {
