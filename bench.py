@@ -294,8 +294,8 @@ BATCH = dict(n_inst=64, lo=32, hi=96, seed=0, reinit_iters=5, cfl=0.5)
 # algorithmic HBM bytes per node for one launch of the batched FP32 kernels
 BATCH_ALGO_BYTES = {
     "k_stage_z": 17.0 / 3.0 * 4,   # phi_prev, phi^n (stages 2-3), W(3); phi
-    "k_reinit": 12.0 * 4,        # d, s, metrics(9); d
-    "k_sign": 11.0 * 4,          # phi0, metrics(9); s
+    "k_reinit_z": 12.0 * 4,      # d, s, metrics(9); d
+    "k_sign_reinit_z": 12.0 * 4, # phi0, metrics(9); s, d
     "k_contra": 15.0 * 4,        # u(3), metrics(9); W(3)
     "k_volume": 4.0 + 8.0,       # phi (FP32) + FP64 cell volume (+ coordinates of interface cells only)
     "k_bc_full": 8.0,
@@ -523,11 +523,10 @@ FWDADJ = dict(ni=512, nj=256, nk=256, reinit_iters=10, segment=20, compare_steps
 FWDADJ_BYTES = {
     "k_contra": 15 * 4,            # u(3), metrics(9); W(3)
     "k_stage_z": 17.0 / 3.0 * 4,     # phi_prev, phi^n (stages 2-3), W(3); stage output
-    "k_sign": 11 * 4,              # phi0, metrics(9); s
-    "k_reinit": 12 * 4,            # d, s, metrics(9); d
-    "k_sign_reinit": 12 * 4,       # phi0, metrics(9); s, d
+    "k_reinit_z": 12 * 4,          # d, s, metrics(9); d
+    "k_sign_reinit_z": 12 * 4,     # phi0, metrics(9); s, d
     "k_reinit_rec_z": 18 * 4,      # d, s, metrics(9); d, adjoint coefficients(6)
-    "k_sign_reinit_rec": 18 * 4,   # phi0, metrics(9); s, d, adjoint coefficients(6)
+    "k_sign_reinit_rec_z": 18 * 4, # phi0, metrics(9); s, d, adjoint coefficients(6)
     "k_adj_reinit_c": 8 * 4,       # lam, coefficients(6); lam_out
     "k_volume": 4 + 8,             # phi (FP32) + fixed-point cell volume (interface-cell coordinates not counted)
     "k_bc_full": 2 * 4,            # phi in, phi out
@@ -734,17 +733,17 @@ def run_fwdadj(args):
     # 4-step segment, per cell-step, at the measured throughput
     seg_bytes = sum(FWDADJ_BYTES[k] * n * v[0] for k, v in prof.items() if k in FWDADJ_BYTES)
     per_cell_step = seg_bytes / (float(SA) * n)
-    # the survey's accounting of the same step (each distinct array of the
-    # reference's formulation read and written once per pass): forward
+    # the same step counted by the passes of the reference's formulation
+    # (each distinct array read and written once per pass): forward
     # 53 + 14R words, adjoint 131 + 32R words of which 53 + 14R are the
     # forward recompute, which this schedule (one segment, internals kept
     # by the forward) does not run; FP32
-    survey_bytes = (131 + 32 * R) * 4.0
+    pass_bytes = (131 + 32 * R) * 4.0
     step_roof = {"algorithmic_bytes_per_cell_step": per_cell_step,
                  "achieved_gbs": per_cell_step * value,
                  "frac": per_cell_step * value / roof["peak"],
-                 "survey_accounting": {"bytes_per_cell_step": survey_bytes,
-                                       "frac": survey_bytes * value / roof["peak"]},
+                 "per_pass_accounting": {"bytes_per_cell_step": pass_bytes,
+                                         "frac": pass_bytes * value / roof["peak"]},
                  "note": "bytes: the launches of a profiled 4-step segment, each kernel's own algorithmic bytes; "
                          "the 20-step segment's checkpoint and segment-state copies add 0.8 B/cell-step"}
 

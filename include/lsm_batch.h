@@ -53,8 +53,9 @@ typedef struct lsm_batch_config {
     int btype_lsm[6];   /* bcond_lsm face types (0 absorb, 1 extrapolate, 2 advect) */
     double BigPhi;      /* first-order extrapolation cut-off */
     int use_graph;      /* 1: capture the per-step launches in a CUDA graph */
-    int autotune;       /* 1: time every tile shape on this batch and keep the fastest */
-    int shape;          /* tile shape index when autotune == 0 (0..4) */
+    int autotune;       /* 1: time the candidates on this batch and keep the fastest */
+    int shape;          /* when autotune == 0: 0..4 tile shape (pseudo-steps on the brick
+                           table), 5 tile shape 0 with the pseudo-steps marching in k */
     int precision;      /* 0: FP32 stencils, 1: FP64 stencils (tile shape 0, no autotune) */
     int adjoint_mode;   /* 0: recorded pseudo-steps store their adjoint coefficients (6 arrays
                            each; the reverse sweep is a stencil), 1: the reverse sweep
@@ -102,7 +103,8 @@ int lsm_batch_get_grad_phi0(lsm_batch_handle h, int inst, double* grad);
 /* dL/dq of one instance in the layout of q (4, ni, nj, nk); q(1) gets zero. */
 int lsm_batch_get_grad_velocity(lsm_batch_handle h, int inst, double* grad_q);
 
-/* Tile shape in use (index, and its TX, TY, TZ). */
+/* Tile shape in use (index 0..5 as lsm_batch_config.shape, and the brick
+   table's TX, TY, TZ). */
 int lsm_batch_shape(lsm_batch_handle h, int* index, int* tx, int* ty, int* tz);
 /* Total nodes of the batch and kernels launched per physical step. */
 long long lsm_batch_nodes(lsm_batch_handle h);

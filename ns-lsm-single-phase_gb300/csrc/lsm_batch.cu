@@ -453,20 +453,6 @@ __device__ __forceinline__ T sign_of(T p, T g, T eps) {
     return p / eps - T(1.0 / kPi) * vsin(T(kPi) * p / eps);
 }
 
-template <typename T, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(TX * TY * TZ) k_sign(const Inst* __restrict__ inst,
-        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phi0) {
-    for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
-        if (!b.valid) continue;
-        const Inst& I = inst[b.inst];
-        const long long l = I.off + b.i + (long long)I.ni * (b.j + (long long)I.nj * b.k);
-        const T p = __ldg(phi0 + l);
-        const T g = godunov(f, phi0, I, l, b.i, b.j, b.k, p > T(0) ? T(1) : T(-1));
-        f.sgn[l] = sign_of(p, g, ipar<T>(I.eps, I.eps64));
-    }
-}
-
 // one reinitialisation pseudo-step at a node: d - dtau s (|grad d|_G - 1)
 template <typename T>
 __device__ __forceinline__ T reinit_node(const FieldsT<T>& f, const T* __restrict__ din, const Inst& I, long long l,
@@ -545,51 +531,18 @@ __device__ __forceinline__ T godunov_sel_v(const T (&mas)[3], const T (&men)[3],
     return acc;
 }
 
-template <typename T>
-__device__ __forceinline__ T godunov_sel(const FieldsT<T>& f, const T* __restrict__ d, const Inst& I, long long l,
-                                         int i, int j, int k, T sel, T (&M)[9], T (&e)[3], T (&g)[3]) {
-    T mas[3], men[3];
-    godunov_diffs(d, I, l, i, j, k, mas, men);
-    const T sg = sel > T(0) ? T(1) : T(-1);
-    T acc = T(0);
-#pragma unroll
-    for (int x = 0; x < 3; ++x) {
-        M[x] = __ldg(f.m[x] + l);
-        M[3 + x] = __ldg(f.m[3 + x] + l);
-        M[6 + x] = __ldg(f.m[6 + x] + l);
-        const T bb = sg * (M[x] * men[0] + M[3 + x] * men[1] + M[6 + x] * men[2]);
-        const T ff = sg * (M[x] * mas[0] + M[3 + x] * mas[1] + M[6 + x] * mas[2]);
-        const T p = vmax(bb, T(0)), q = vmin(ff, T(0));
-        const bool takeP = p * p >= q * q;
-        acc += takeP ? p * p : q * q;
-        e[x] = takeP ? p : T(0);
-        g[x] = takeP ? T(0) : q;
-    }
-    return acc;
-}
-
-template <typename T>
-__device__ __forceinline__ void coef_store(const T (&M)[9], const T (&e)[3], const T (&g)[3], T w, const Inst& I,
-                                           int i, int j, int k, T* __restrict__ cf, long long ld, long long l) {
-    const int c3d[3] = {i, j, k}, n3[3] = {I.ni, I.nj, I.nk};
-#pragma unroll
-    for (int m = 0; m < 3; ++m) {
-        const bool lo = c3d[m] == 0, hi = c3d[m] == n3[m] - 1;
-        const T gmen = M[3 * m] * e[0] + M[3 * m + 1] * e[1] + M[3 * m + 2] * e[2];
-        const T gmas = M[3 * m] * g[0] + M[3 * m + 1] * g[1] + M[3 * m + 2] * g[2];
-        cf[m * ld + l] = lo ? T(0) : w * (hi ? gmen + gmas : gmen);
-        cf[(3 + m) * ld + l] = hi ? T(0) : w * (lo ? gmen + gmas : gmas);
-    }
-}
-
-// A recorded pseudo-step (d' and its adjoint coefficients) on the tiles of
-// adjoint map 2 (32 x 8 columns marching 32 planes in k): each node loads
-// d, s and its metrics once, a plane ahead; the z neighbours of d stay in a
-// register window, the x neighbours come by warp shuffles (the tile's edge
-// lanes load the one outside) and the y neighbours are loaded (L1/L2).  d'
-// is bit-identical to k_reinit's.
-template <typename T>
-__global__ void __launch_bounds__(256) k_reinit_rec_z(const Inst* __restrict__ inst, const Brick* __restrict__ bmap,
+// One reinitialisation pseudo-step on the tiles of adjoint map 2 (32 x 8
+// columns marching 32 planes in k): each node loads d (and s) and its
+// metrics once, a plane ahead; the z neighbours of d stay in a register
+// window, the x neighbours come by warp shuffles (the tile's edge lanes load
+// the one outside) and the y neighbours are loaded (L1/L2).
+//   SIGN: the first pseudo-step fused with calc_sign_ini: din is phi0, the
+//         Godunov branch is chosen by sign(phi0) (a node whose s is not 0
+//         has the sign of phi0), s is computed and stored;
+//   REC:  the pseudo-step's adjoint coefficients are stored as well.
+// d' equals reinit_node's arithmetic (one_sided, godunov) bit for bit.
+template <typename T, bool SIGN, bool REC>
+__global__ void __launch_bounds__(256) k_reinit_z(const Inst* __restrict__ inst, const Brick* __restrict__ bmap,
         int nb, FieldsT<T> f, const T* __restrict__ din, T* __restrict__ dout, T* __restrict__ cf, long long ld,
         unsigned* err) {
     const unsigned FM = 0xffffffffu;
@@ -606,7 +559,7 @@ __global__ void __launch_bounds__(256) k_reinit_rec_z(const Inst* __restrict__ i
         const bool xm = i > 0, xp = i < ni - 1, ym = j > 0, yp = j < nj - 1;
         const bool ex = col && ((tx == 0 && xm) || (tx == 31 && xp));
         const int eo = tx == 0 ? -1 : 1;
-        const T dtau = ipar<T>(I.dtau, I.dtau64);
+        const T dtau = ipar<T>(I.dtau, I.dtau64), eps = ipar<T>(I.eps, I.eps64);
         struct Plane {
             T s, M[9], dxe, dym, dyp;
         };
@@ -616,7 +569,7 @@ __global__ void __launch_bounds__(256) k_reinit_rec_z(const Inst* __restrict__ i
             for (int c = 0; c < 9; ++c) p.M[c] = T(0);
             if (!col || k < 0 || k >= nk) return;
             const long long l = cb + sk * k;
-            p.s = __ldg(f.sgn + l);
+            if (!SIGN) p.s = __ldg(f.sgn + l);
 #pragma unroll
             for (int c = 0; c < 9; ++c) p.M[c] = __ldg(f.m[c] + l);
             if (ex) p.dxe = __ldg(din + l + eo);
@@ -645,18 +598,24 @@ __global__ void __launch_bounds__(256) k_reinit_rec_z(const Inst* __restrict__ i
                     men[m] = lo[m] ? a : b;
                 }
                 T e[3], g[3];
-                const T acc = godunov_sel_v(mas, men, pc.M, pc.s, e, g);
-                const T s = pc.s;
-                const T r = s == T(0) ? dc : dc - dtau * s * (vsqrt(acc) - T(1));
                 const long long l = cb + sk * k;
+                const T acc = godunov_sel_v(mas, men, pc.M, SIGN ? (dc > T(0) ? T(1) : T(-1)) : pc.s, e, g);
+                T s = pc.s;
+                if (SIGN) {
+                    s = sign_of(dc, vsqrt(acc), eps);
+                    f.sgn[l] = s;
+                }
+                const T r = s == T(0) ? dc : dc - dtau * s * (vsqrt(acc) - T(1));
                 dout[l] = r;
-                const T w = s != T(0) && acc > T(0) ? dtau * fabs(s) * vrsqrt(acc) : T(0);
+                if (REC) {
+                    const T w = s != T(0) && acc > T(0) ? dtau * fabs(s) * vrsqrt(acc) : T(0);
 #pragma unroll
-                for (int m = 0; m < 3; ++m) {
-                    const T gmen = pc.M[3 * m] * e[0] + pc.M[3 * m + 1] * e[1] + pc.M[3 * m + 2] * e[2];
-                    const T gmas = pc.M[3 * m] * g[0] + pc.M[3 * m + 1] * g[1] + pc.M[3 * m + 2] * g[2];
-                    cf[m * ld + l] = lo[m] ? T(0) : w * (hi[m] ? gmen + gmas : gmen);
-                    cf[(3 + m) * ld + l] = hi[m] ? T(0) : w * (lo[m] ? gmen + gmas : gmas);
+                    for (int m = 0; m < 3; ++m) {
+                        const T gmen = pc.M[3 * m] * e[0] + pc.M[3 * m + 1] * e[1] + pc.M[3 * m + 2] * e[2];
+                        const T gmas = pc.M[3 * m] * g[0] + pc.M[3 * m + 1] * g[1] + pc.M[3 * m + 2] * g[2];
+                        cf[m * ld + l] = lo[m] ? T(0) : w * (hi[m] ? gmen + gmas : gmen);
+                        cf[(3 + m) * ld + l] = hi[m] ? T(0) : w * (lo[m] ? gmen + gmas : gmas);
+                    }
                 }
                 if (err && !vfinite(r)) atomicOr(err, (unsigned)kErrNonFinite);
             }
@@ -665,32 +624,6 @@ __global__ void __launch_bounds__(256) k_reinit_rec_z(const Inst* __restrict__ i
             dp = dn;
             pc = pn;
         }
-    }
-}
-
-// k_sign_reinit with the coefficients of the first pseudo-step (the branch
-// sign is sign(phi0), which a node with s != 0 shares)
-template <typename T, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(TX * TY * TZ) k_sign_reinit_rec(const Inst* __restrict__ inst,
-        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phi0, T* __restrict__ dout,
-        T* __restrict__ cf, long long ld, unsigned* err) {
-    for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
-        if (!b.valid) continue;
-        const Inst& I = inst[b.inst];
-        const long long l = I.off + b.i + (long long)I.ni * (b.j + (long long)I.nj * b.k);
-        const T p = __ldg(phi0 + l);
-        const T dtau = ipar<T>(I.dtau, I.dtau64);
-        T M[9], e[3], g[3];
-        const T acc = godunov_sel(f, phi0, I, l, b.i, b.j, b.k, p > T(0) ? T(1) : T(-1), M, e, g);
-        const T gn = vsqrt(acc);
-        const T s = sign_of(p, gn, ipar<T>(I.eps, I.eps64));
-        f.sgn[l] = s;
-        const T r = s == T(0) ? p : p - dtau * s * (gn - T(1));
-        dout[l] = r;
-        coef_store(M, e, g, s != T(0) && acc > T(0) ? dtau * fabs(s) * vrsqrt(acc) : T(0), I, b.i, b.j, b.k, cf, ld,
-                   l);
-        if (err && !vfinite(r)) atomicOr(err, (unsigned)kErrNonFinite);
     }
 }
 
@@ -1531,9 +1464,6 @@ LSM_BATCH_RUNNER(RunBcFull, k_bc_full,
                  (int grid, const Inst* inst, const Brick* bi, int nb, BC bc, const T* src, T* dst, unsigned* err,
                   cudaStream_t s),
                  (inst, bi, nb, bc, src, dst, err))
-LSM_BATCH_RUNNER(RunSign, k_sign,
-                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* p0, cudaStream_t s),
-                 (inst, bi, nb, f, p0))
 LSM_BATCH_RUNNER(RunReinit, k_reinit,
                  (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* din, T* dout,
                   unsigned* err, cudaStream_t s),
@@ -1542,10 +1472,6 @@ LSM_BATCH_RUNNER(RunSignReinit, k_sign_reinit,
                  (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* p0, T* dout,
                   unsigned* err, cudaStream_t s),
                  (inst, bi, nb, f, p0, dout, err))
-LSM_BATCH_RUNNER(RunSignReinitRec, k_sign_reinit_rec,
-                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* p0, T* dout, T* cf,
-                  long long ld, unsigned* err, cudaStream_t s),
-                 (inst, bi, nb, f, p0, dout, cf, ld, err))
 LSM_BATCH_RUNNER(RunVolume, k_volume,
                  (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi,
                   unsigned long long* part, cudaStream_t s),
@@ -1557,7 +1483,6 @@ struct Occupancy {
         const int nt = TX * TY * TZ;
         switch (kernel) {
         case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_contra<T, TX, TY, TZ>, nt, 0); break;
-        case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_reinit<T, TX, TY, TZ>, nt, 0); break;
         default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_volume<T, TX, TY, TZ>, nt, 0); break;
         }
     }
@@ -1596,10 +1521,6 @@ void bc_full(int shape, int grid, const Inst* inst, const Brick* bi, int nb, BC 
     dispatch<RunBcFull, T>(shape, grid, inst, bi, nb, bc, src, dst, err, s);
 }
 template <typename T>
-void sign(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi0, cudaStream_t s) {
-    dispatch<RunSign, T>(shape, grid, inst, bi, nb, f, phi0, s);
-}
-template <typename T>
 void reinit(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* din, T* dout,
             unsigned* err, cudaStream_t s) {
     dispatch<RunReinit, T>(shape, grid, inst, bi, nb, f, din, dout, err, s);
@@ -1610,21 +1531,36 @@ void sign_reinit(int shape, int grid, const Inst* inst, const Brick* bi, int nb,
     dispatch<RunSignReinit, T>(shape, grid, inst, bi, nb, f, phi0, dout, err, s);
 }
 template <typename T>
-void reinit_rec_z(int grid, const Inst* inst, const Brick* bmap2, int nb, FieldsT<T> f, const T* din, T* dout, T* cf,
-                  long long ld, unsigned* err, cudaStream_t s) {
-    ProfScope ps_("k_reinit_rec_z", s);
-    k_reinit_rec_z<T><<<grid, 256, 0, s>>>(inst, bmap2, nb, f, din, dout, cf, ld, err);
+void reinit_z(int kind, int grid, const Inst* inst, const Brick* bmap2, int nb, FieldsT<T> f, const T* din, T* dout,
+              T* cf, long long ld, unsigned* err, cudaStream_t s) {
+    switch (kind) {
+    case 0: {
+        ProfScope ps_("k_reinit_z", s);
+        k_reinit_z<T, false, false><<<grid, 256, 0, s>>>(inst, bmap2, nb, f, din, dout, cf, ld, err);
+        break;
+    }
+    case 1: {
+        ProfScope ps_("k_reinit_rec_z", s);
+        k_reinit_z<T, false, true><<<grid, 256, 0, s>>>(inst, bmap2, nb, f, din, dout, cf, ld, err);
+        break;
+    }
+    case 2: {
+        ProfScope ps_("k_sign_reinit_z", s);
+        k_reinit_z<T, true, false><<<grid, 256, 0, s>>>(inst, bmap2, nb, f, din, dout, cf, ld, err);
+        break;
+    }
+    default: {
+        ProfScope ps_("k_sign_reinit_rec_z", s);
+        k_reinit_z<T, true, true><<<grid, 256, 0, s>>>(inst, bmap2, nb, f, din, dout, cf, ld, err);
+        break;
+    }
+    }
 }
 template <typename T>
-int reinit_rec_z_blocks_per_sm() {
+int reinit_z_blocks_per_sm() {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_reinit_rec_z<T>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_reinit_z<T, true, true>, 256, 0);
     return n;
-}
-template <typename T>
-void sign_reinit_rec(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi0,
-                     T* dout, T* cf, long long ld, unsigned* err, cudaStream_t s) {
-    dispatch<RunSignReinitRec, T>(shape, grid, inst, bi, nb, f, phi0, dout, cf, ld, err, s);
 }
 template <typename T>
 void adj_reinit_c(int grid, const Inst* inst, const Brick* bmap2, int nb, const T* cf, long long ld, const T* lam,
@@ -1719,17 +1655,14 @@ void adj_contra(const Flat& fl, FieldsT<T> f, const T* w0, const T* w1, const T*
                            double, double, cudaStream_t);                                                                     \
     template void bc_stage<T>(const Inst*, int, long long, BC, const T*, const T*, T*, double, double, cudaStream_t);   \
     template void bc_full<T>(int, int, const Inst*, const Brick*, int, BC, const T*, T*, unsigned*, cudaStream_t);      \
-    template void sign<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, cudaStream_t);               \
+    template void bc_reinit<T>(const Inst*, int, long long, FieldsT<T>, BC, const T*, T*, cudaStream_t);              \
     template void reinit<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, unsigned*,             \
                             cudaStream_t);                                                                            \
-    template void bc_reinit<T>(const Inst*, int, long long, FieldsT<T>, BC, const T*, T*, cudaStream_t);              \
     template void sign_reinit<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, unsigned*,      \
                                  cudaStream_t);                                                                   \
-    template void reinit_rec_z<T>(int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, T*, long long,     \
-                                  unsigned*, cudaStream_t);                                                     \
-    template int reinit_rec_z_blocks_per_sm<T>();                                                               \
-    template void sign_reinit_rec<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, T*,        \
-                                     long long, unsigned*, cudaStream_t);                                       \
+    template void reinit_z<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, T*, long long,    \
+                              unsigned*, cudaStream_t);                                                         \
+    template int reinit_z_blocks_per_sm<T>();                                                                   \
     template void adj_reinit_c<T>(int, const Inst*, const Brick*, int, const T*, long long, const T*, T*,           \
                                   cudaStream_t);                                                                \
     template int adj_reinit_c_blocks_per_sm<T>();                                                               \

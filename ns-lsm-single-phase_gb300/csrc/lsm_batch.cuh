@@ -86,13 +86,11 @@ void bc_stage(const Inst* inst, int ninst, long long nface, BC bc, const T* phin
 template <typename T>
 void bc_full(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, BC bc, const T* src, T* dst,
              unsigned* err, cudaStream_t s);
-template <typename T>
-void sign(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f, const T* phi0,
-          cudaStream_t s);
+// one reinitialisation pseudo-step on the brick table (the sign field
+// fused with the first one in sign_reinit)
 template <typename T>
 void reinit(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f, const T* din,
             T* dout, unsigned* err, cudaStream_t s);
-// sign field of phi0 and the first pseudo-step from phi0 in one pass
 template <typename T>
 void sign_reinit(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f,
                  const T* phi0, T* dout, unsigned* err, cudaStream_t s);
@@ -101,18 +99,16 @@ void sign_reinit(int shape, int grid, const Inst* inst, const Brick* bricks, int
 template <typename T>
 void bc_reinit(const Inst* inst, int ninst, long long nface, FieldsT<T> f, BC bc, const T* din, T* dout,
                cudaStream_t s);
-// sign_reinit / reinit of a recorded step that also write the
-// pseudo-step's adjoint coefficients A'_0..2, B'_0..2 (cf, arrays ld apart)
+// One reinitialisation pseudo-step on the tiles of adjoint map 2 (z march;
+// grid from reinit_z_blocks_per_sm): kind 0 plain, 1 recorded (the
+// pseudo-step's adjoint coefficients A'_0..2, B'_0..2 also written to cf,
+// arrays ld apart), 2 the sign field of phi0 (din) fused with the first
+// pseudo-step, 3 the same recorded
 template <typename T>
-void sign_reinit_rec(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f,
-                     const T* phi0, T* dout, T* cf, long long ld, unsigned* err, cudaStream_t s);
-// reinit_rec on the tiles of adjoint map 2 (z march; grid from
-// reinit_rec_z_blocks_per_sm)
+void reinit_z(int kind, int grid, const Inst* inst, const Brick* bmap2, int nb, FieldsT<T> f, const T* din, T* dout,
+              T* cf, long long ld, unsigned* err, cudaStream_t s);
 template <typename T>
-void reinit_rec_z(int grid, const Inst* inst, const Brick* bmap2, int nb, FieldsT<T> f, const T* din, T* dout, T* cf,
-                  long long ld, unsigned* err, cudaStream_t s);
-template <typename T>
-int reinit_rec_z_blocks_per_sm();
+int reinit_z_blocks_per_sm();
 // water volume of every instance: k_volume adds 64-bit fixed-point sums
 // (K, S, bulk) to acc[3 * inst + c] (zero on entry); volume_final writes
 // vols[4 * inst + 0..3] = (K, S, bulk, total) and clears acc

@@ -53,7 +53,8 @@ struct lsm_batch {
     int nbricks = 0;
     lsm::batch::Brick* d_amap[4] = {};  // brick tables of the adjoint stencil kernels (lsm::batch::adj_shape)
     int namap[4] = {0, 0, 0, 0}, agrid[4] = {1, 1, 1, 1};
-    int sgrid = 1, acgrid = 1, rzgrid = 1;   // CTAs of the map-2 kernels: stage, k_adj_reinit_c, k_reinit_rec_z
+    int sgrid = 1, acgrid = 1, rzgrid = 1;   // CTAs of the map-2 kernels: stage, k_adj_reinit_c, reinit_z
+    bool reinit_march = true;   // plain pseudo-steps march in k (reinit_z) rather than walk the brick table
     unsigned long long* d_vacc = nullptr;   // volume accumulators, 3 per instance (k_volume)
     double* d_vols = nullptr;
     double* h_vols = nullptr;    // pinned
@@ -243,8 +244,8 @@ int build_bricks(lsm_batch* b, int shape) {
     const int pac = std::max(1, b->prec ? lsm::batch::adj_reinit_c_blocks_per_sm<double>()
                                         : lsm::batch::adj_reinit_c_blocks_per_sm<float>());
     b->acgrid = std::max(1, std::min(b->namap[2], sms * pac));
-    const int prz = std::max(1, b->prec ? lsm::batch::reinit_rec_z_blocks_per_sm<double>()
-                                        : lsm::batch::reinit_rec_z_blocks_per_sm<float>());
+    const int prz = std::max(1, b->prec ? lsm::batch::reinit_z_blocks_per_sm<double>()
+                                        : lsm::batch::reinit_z_blocks_per_sm<float>());
     b->rzgrid = std::max(1, std::min(b->namap[2], sms * prz));
     b->shape = shape;
     BCU(b, cudaStreamSynchronize(b->stream));
@@ -327,19 +328,14 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
             const bool last = it == R - 1;
             T* o = coef ? (last ? rec->D : f.d[it & 1]) : rec ? rec_d(b, *rec, it) : (last ? phi_out : f.d[it & 1]);
             unsigned* err = (last && !rec) ? b->d_err : nullptr;
-            if (coef) {
-                T* cf = rec->C + 6LL * it * (long long)b->ld;
-                if (it == 0)
-                    B::sign_reinit_rec<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, cf, (long long)b->ld, err,
-                                          b->stream);
-                else
-                    B::reinit_rec_z<T>(b->rzgrid, b->d_inst, b->d_amap[2], b->namap[2], f, cur, o, cf, (long long)b->ld,
-                                       err, b->stream);
-            } else if (it == 0) {
+            T* cf = coef ? rec->C + 6LL * it * (long long)b->ld : nullptr;
+            if (coef || b->reinit_march)
+                B::reinit_z<T>((it == 0 ? 2 : 0) + (coef ? 1 : 0), b->rzgrid, b->d_inst, b->d_amap[2], b->namap[2], f,
+                               cur, o, cf, (long long)b->ld, err, b->stream);
+            else if (it == 0)
                 B::sign_reinit<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, err, b->stream);
-            } else {
+            else
                 B::reinit<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, err, b->stream);
-            }
             if (last && !rec) B::bc_reinit<T>(b->d_inst, b->ninst, b->nface, f, bc, cur, phi_out, b->stream);
             cur = o;
         }
@@ -357,47 +353,81 @@ void enqueue_step(lsm_batch* b) {
     else enqueue_step_io<float>(b, b->f32.phi, b->f32.phi, nullptr, true);
 }
 
+// Chooses the tile shape of the brick-table kernels and whether the plain
+// pseudo-steps march in k (reinit_z) or walk the brick table: times, on
+// the batch itself, contra + volume and the brick pseudo-step for every
+// shape, and the marching pseudo-step once.
 int autotune(lsm_batch* b) {
     namespace B = lsm::batch;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    float best = 1e30f;
-    int best_shape = 0;
+    cudaEvent_t ev[3];
+    for (auto& e : ev) cudaEventCreate(&e);
+    auto done = [&](int st) {
+        for (auto& e : ev) cudaEventDestroy(e);
+        return st;
+    };
     FieldsT<float>& f = b->f32;
+    auto timed = [&](float* ms_a, float* ms_b, auto&& pa, auto&& pb) -> int {
+        pa();
+        pb();
+        cudaEventRecord(ev[0], b->stream);
+        for (int r = 0; r < 5; ++r) pa();
+        cudaEventRecord(ev[1], b->stream);
+        for (int r = 0; r < 5; ++r) pb();
+        cudaEventRecord(ev[2], b->stream);
+        const cudaError_t e = cudaEventSynchronize(ev[2]);
+        if (e != cudaSuccess) return fail(b, LSM_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(e));
+        cudaEventElapsedTime(ms_a, ev[0], ev[1]);
+        cudaEventElapsedTime(ms_b, ev[1], ev[2]);
+        return LSM_OK;
+    };
+    float a[B::kNumShapes], br[B::kNumShapes], zm = 0.f, dummy = 0.f;
     for (int s = 0; s < B::kNumShapes; ++s) {
-        BTRY(build_bricks(b, s));
-        B::sign<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, f.phi, b->stream);
-        auto pass = [&]() {
-            B::contra<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, b->stream);
-            B::reinit<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, f.phi, f.d[0], nullptr, b->stream);
-        };
-        pass();
-        cudaEventRecord(e0, b->stream);
-        for (int r = 0; r < 5; ++r) pass();
-        cudaEventRecord(e1, b->stream);
-        cudaError_t e = cudaEventSynchronize(e1);
-        if (e != cudaSuccess) {
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
-            return fail(b, LSM_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(e));
-        }
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best) {
-            best = ms;
-            best_shape = s;
-        }
+        const int bs = build_bricks(b, s);
+        if (bs != LSM_OK) return done(bs);
+        const int st = timed(
+            &a[s], &br[s],
+            [&]() {
+                B::contra<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, b->stream);
+                B::volume<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, f.phi, b->d_vacc, b->stream);
+                B::volume_final(b->ninst, b->d_vacc, b->d_vols, b->stream);
+            },
+            [&]() {
+                B::sign_reinit<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, f.phi, f.d[0], nullptr,
+                                      b->stream);
+                B::reinit<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, f.d[0], f.d[1], nullptr, b->stream);
+            });
+        if (st != LSM_OK) return done(st);
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    return build_bricks(b, best_shape);
+    // the marching pseudo-steps do not depend on the brick shape
+    const int st = timed(&dummy, &zm, [&]() {}, [&]() {
+        B::reinit_z<float>(2, b->rzgrid, b->d_inst, b->d_amap[2], b->namap[2], f, f.phi, f.d[0], nullptr, 0, nullptr,
+                           b->stream);
+        B::reinit_z<float>(0, b->rzgrid, b->d_inst, b->d_amap[2], b->namap[2], f, f.d[0], f.d[1], nullptr, 0, nullptr,
+                           b->stream);
+    });
+    if (st != LSM_OK) return done(st);
+    int best_b = 0, best_a = 0;
+    for (int s = 1; s < B::kNumShapes; ++s) {
+        if (a[s] + br[s] < a[best_b] + br[best_b]) best_b = s;
+        if (a[s] < a[best_a]) best_a = s;
+    }
+    const bool march = a[best_a] + zm < a[best_b] + br[best_b];
+    b->reinit_march = march;
+    return done(build_bricks(b, march ? best_a : best_b));
 }
 
 int prepare(lsm_batch* b) {
     if (!b->tuned) {
         const bool tune = b->cfg.autotune && !b->prec;
-        BTRY(tune ? autotune(b) : build_bricks(b, std::min(std::max(b->cfg.shape, 0), 4)));
+        if (tune) {
+            BTRY(autotune(b));
+        } else {
+            // shape 0..4: that tile shape, pseudo-steps on the brick table;
+            // 5: tile shape 0, pseudo-steps marching in k
+            const int sh = std::min(std::max(b->cfg.shape, 0), 5);
+            BTRY(build_bricks(b, sh == 5 ? 0 : sh));
+            b->reinit_march = sh == 5;
+        }
         b->tuned = true;
     }
     if (b->cfg.use_graph && !b->exec) {
@@ -873,7 +903,7 @@ int lsm_batch_get_grad_velocity(lsm_batch_handle b, int q, double* gq) {
 int lsm_batch_shape(lsm_batch_handle b, int* index, int* tx, int* ty, int* tz) {
     if (!b) return LSM_ERR_NULL;
     const auto sh = lsm::batch::kShapes[b->shape];
-    if (index) *index = b->shape;
+    if (index) *index = b->reinit_march ? 5 : b->shape;
     if (tx) *tx = sh.tx;
     if (ty) *ty = sh.ty;
     if (tz) *tz = sh.tz;

@@ -3,9 +3,10 @@
 Each instance of a small uneven batch runs the reference's level-set step
 (WENO3-RK3 + bcond + `reinitialization` + water volume) in FP32 inside one
 launch per pass; every instance is compared with the CPU FP64 oracle run on
-its own.  Bars (spec accuracy targets): L-infinity phi error within the
+its own.  Bars: L-infinity phi error within the
 6-cell narrow band |phi| < 4 eps <= 1e-5, relative volume error <= 1e-6.
-Tile shapes and graph/no-graph must give bit-identical phi.
+Tile shapes, brick or marching pseudo-steps and graph/no-graph must give
+bit-identical phi.
 """
 import numpy as np
 import pytest
@@ -74,7 +75,9 @@ def test_batch_matches_fp64_oracle(oracle, small_batch, R):
 
 def test_shapes_and_graph_bit_identical(small_batch):
     outs = []
+    # shape 5: the pseudo-steps march in k instead of walking the brick table
     for kw in (dict(autotune=False, shape=0, use_graph=True), dict(autotune=False, shape=3, use_graph=False),
+               dict(autotune=False, shape=5, use_graph=True), dict(autotune=False, shape=5, use_graph=False),
                dict(autotune=True, use_graph=True)):
         b = _make_batch(small_batch, 3, **kw)
         b.step(3)
