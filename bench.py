@@ -256,8 +256,9 @@ def load_peaks():
 
 
 # ------------------------------------------------------------- CPU baseline
-def cpu_oracle_time(case, steps, threads):
-    """Seconds per physical step of the CPU FP64 oracle (OpenMP build) on `case`."""
+def cpu_oracle_time(case, steps, threads, warmup=0):
+    """Seconds per physical step of the CPU FP64 oracle (OpenMP build) on
+    `case`, timed over `steps` steps after `warmup` untimed ones."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     os.environ["OMP_NUM_THREADS"] = str(threads)
     import oracle as O
@@ -275,8 +276,10 @@ def cpu_oracle_time(case, steps, threads):
                       OrderReinitialisationBoundaries=cp.OrderReinitialisationBoundaries,
                       ENOBCReinitialisation=int(cp.ENOBCReinitialisation))
     phi = case.phi0
+    for it in range(1, warmup + 1):
+        phi, _ = orc.levelsetmethod(g, p, q, csi, eta, zet, aj, phi, phi, case.x, case.y, case.z, it)
     t0 = time.perf_counter()
-    for it in range(1, steps + 1):
+    for it in range(warmup + 1, warmup + steps + 1):
         phi, _ = orc.levelsetmethod(g, p, q, csi, eta, zet, aj, phi, phi, case.x, case.y, case.z, it)
     return (time.perf_counter() - t0) / steps, orc.threads
 
@@ -1150,18 +1153,25 @@ def run_reference_fwdadj(args, world):
     R = W["reinit_iters"]
     case = configs.large_free_surface(W["ni"], W["nj"], W["nk"], reinit_iters=R)
     threads = host_threads()
-    steps = max(1, min(args.steps, 2))
-    sec, used = cpu_oracle_time(case, steps, threads)
+    # a physical step of the whole grid takes a few seconds on the box's 16
+    # cores: the requested counts, capped so the run stays within minutes
+    steps = max(1, min(args.steps if args.steps else 10, 10))
+    warm = max(0, min(args.warmup, 3))
+    sec, used = cpu_oracle_time(case, steps, threads, warm)
     v = case.grid.n / sec / 1e9
+    S = args.segment or W["segment"]
     line = {
         "impl": "reference",
         "metric": "Gcell-steps/s (batched FP32 level-set forward + adjoint: WENO3-RK3 + %d reinit pseudo-steps + "
                   "FP64 volume; vs the plain FP64 GPU path)" % R,
-        "value": v, "unit": "Gcell-steps/s", "n_gpus": world, "steps": steps, "warmup": 0,
+        "value": v, "unit": "Gcell-steps/s", "n_gpus": world, "steps": steps, "warmup": warm,
         "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": "large_free_surface %dx%dx%d curvilinear, %d reinit pseudo-steps/step"
-                               % (W["ni"], W["nj"], W["nk"], R)},
+        "config": {"workload": "large_free_surface %dx%dx%d curvilinear, CFL 0.4, %d reinit pseudo-steps/step, "
+                               "volume each step; one step = %d-step segment forward keeping its internals + "
+                               "adjoint (checkpoint every %d steps: no recompute)" % (W["ni"], W["nj"], W["nk"], R, S, S),
+                   "nodes": case.grid.n,
+                   "timed": "one physical forward step of the whole grid per step (the reference has no adjoint)"},
         "cpu_baseline": {"value": v, "unit": "Gcell-steps/s", "cores": used, "kind": "port",
                          "sample": "%d physical forward steps of the whole grid; CPU FP64 restatement of the "
                                    "reference (the Fortran/MPI original cannot be built here: no Fortran compiler); "
