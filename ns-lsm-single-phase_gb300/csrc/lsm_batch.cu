@@ -378,6 +378,23 @@ __global__ void k_bc_stage(const Inst* __restrict__ inst, int ninst, long long n
     out[I.off + i + p0.sj * j + p0.sk * k] = bval_k<T>(bc, p0, I.ni, I.nj, I.nk, i, j, k);
 }
 
+// bcond_lsm on the faces of dst from the pre-BC field src (interior nodes
+// of dst already hold src)
+template <typename T>
+__global__ void k_bc_faces(const Inst* __restrict__ inst, int ninst, long long nface, BC bc, const T* __restrict__ src,
+                           T* __restrict__ dst, unsigned* err) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= nface) return;
+    const Inst& I = inst[face_instance(inst, ninst, t)];
+    int i, j, k;
+    if (!face_coords(I, t - I.face0, &i, &j, &k)) return;
+    const long long sj = I.ni, sk = (long long)I.ni * I.nj;
+    P0Src<T> p0{src, I.off, sj, sk};
+    const T v = bval_k<T>(bc, p0, I.ni, I.nj, I.nk, i, j, k);
+    dst[I.off + i + sj * j + sk * k] = v;
+    if (err && !vfinite(v)) atomicOr(err, (unsigned)kErrNonFinite);
+}
+
 template <typename T, int TX, int TY, int TZ>
 __global__ void __launch_bounds__(TX * TY * TZ) k_bc_full(const Inst* __restrict__ inst,
         const Brick* __restrict__ bricks, int nbricks, BC bc, const T* __restrict__ src, T* __restrict__ dst,
@@ -540,11 +557,12 @@ __device__ __forceinline__ T godunov_sel_v(const T (&mas)[3], const T (&men)[3],
 //         Godunov branch is chosen by sign(phi0) (a node whose s is not 0
 //         has the sign of phi0), s is computed and stored;
 //   REC:  the pseudo-step's adjoint coefficients are stored as well.
-// d' equals reinit_node's arithmetic (one_sided, godunov) bit for bit.
+// dout2 (nullable) receives a second copy of d'.  d' equals reinit_node's
+// arithmetic (one_sided, godunov) bit for bit.
 template <typename T, bool SIGN, bool REC>
 __global__ void __launch_bounds__(256) k_reinit_z(const Inst* __restrict__ inst, const Brick* __restrict__ bmap,
-        int nb, FieldsT<T> f, const T* __restrict__ din, T* __restrict__ dout, T* __restrict__ cf, long long ld,
-        unsigned* err) {
+        int nb, FieldsT<T> f, const T* __restrict__ din, T* __restrict__ dout, T* __restrict__ dout2,
+        T* __restrict__ cf, long long ld, unsigned* err) {
     const unsigned FM = 0xffffffffu;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     for (int blk = blockIdx.x; blk < nb; blk += gridDim.x) {
@@ -607,6 +625,7 @@ __global__ void __launch_bounds__(256) k_reinit_z(const Inst* __restrict__ inst,
                 }
                 const T r = s == T(0) ? dc : dc - dtau * s * (vsqrt(acc) - T(1));
                 dout[l] = r;
+                if (dout2) dout2[l] = r;
                 if (REC) {
                     const T w = s != T(0) && acc > T(0) ? dtau * fabs(s) * vrsqrt(acc) : T(0);
 #pragma unroll
@@ -1521,6 +1540,12 @@ void bc_full(int shape, int grid, const Inst* inst, const Brick* bi, int nb, BC 
     dispatch<RunBcFull, T>(shape, grid, inst, bi, nb, bc, src, dst, err, s);
 }
 template <typename T>
+void bc_faces(const Inst* inst, int ninst, long long nface, BC bc, const T* src, T* dst, unsigned* err,
+              cudaStream_t s) {
+    ProfScope ps_("k_bc_faces", s);
+    k_bc_faces<T><<<flat_blocks(nface), 256, 0, s>>>(inst, ninst, nface, bc, src, dst, err);
+}
+template <typename T>
 void reinit(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* din, T* dout,
             unsigned* err, cudaStream_t s) {
     dispatch<RunReinit, T>(shape, grid, inst, bi, nb, f, din, dout, err, s);
@@ -1532,26 +1557,26 @@ void sign_reinit(int shape, int grid, const Inst* inst, const Brick* bi, int nb,
 }
 template <typename T>
 void reinit_z(int kind, int grid, const Inst* inst, const Brick* bmap2, int nb, FieldsT<T> f, const T* din, T* dout,
-              T* cf, long long ld, unsigned* err, cudaStream_t s) {
+              T* dout2, T* cf, long long ld, unsigned* err, cudaStream_t s) {
     switch (kind) {
     case 0: {
         ProfScope ps_("k_reinit_z", s);
-        k_reinit_z<T, false, false><<<grid, 256, 0, s>>>(inst, bmap2, nb, f, din, dout, cf, ld, err);
+        k_reinit_z<T, false, false><<<grid, 256, 0, s>>>(inst, bmap2, nb, f, din, dout, dout2, cf, ld, err);
         break;
     }
     case 1: {
         ProfScope ps_("k_reinit_rec_z", s);
-        k_reinit_z<T, false, true><<<grid, 256, 0, s>>>(inst, bmap2, nb, f, din, dout, cf, ld, err);
+        k_reinit_z<T, false, true><<<grid, 256, 0, s>>>(inst, bmap2, nb, f, din, dout, dout2, cf, ld, err);
         break;
     }
     case 2: {
         ProfScope ps_("k_sign_reinit_z", s);
-        k_reinit_z<T, true, false><<<grid, 256, 0, s>>>(inst, bmap2, nb, f, din, dout, cf, ld, err);
+        k_reinit_z<T, true, false><<<grid, 256, 0, s>>>(inst, bmap2, nb, f, din, dout, dout2, cf, ld, err);
         break;
     }
     default: {
         ProfScope ps_("k_sign_reinit_rec_z", s);
-        k_reinit_z<T, true, true><<<grid, 256, 0, s>>>(inst, bmap2, nb, f, din, dout, cf, ld, err);
+        k_reinit_z<T, true, true><<<grid, 256, 0, s>>>(inst, bmap2, nb, f, din, dout, dout2, cf, ld, err);
         break;
     }
     }
@@ -1655,12 +1680,13 @@ void adj_contra(const Flat& fl, FieldsT<T> f, const T* w0, const T* w1, const T*
                            double, double, cudaStream_t);                                                                     \
     template void bc_stage<T>(const Inst*, int, long long, BC, const T*, const T*, T*, double, double, cudaStream_t);   \
     template void bc_full<T>(int, int, const Inst*, const Brick*, int, BC, const T*, T*, unsigned*, cudaStream_t);      \
+    template void bc_faces<T>(const Inst*, int, long long, BC, const T*, T*, unsigned*, cudaStream_t);                 \
     template void bc_reinit<T>(const Inst*, int, long long, FieldsT<T>, BC, const T*, T*, cudaStream_t);              \
     template void reinit<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, unsigned*,             \
                             cudaStream_t);                                                                            \
     template void sign_reinit<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, unsigned*,      \
                                  cudaStream_t);                                                                   \
-    template void reinit_z<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, T*, long long,    \
+    template void reinit_z<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, T*, T*, T*, long long, \
                               unsigned*, cudaStream_t);                                                         \
     template int reinit_z_blocks_per_sm<T>();                                                                   \
     template void adj_reinit_c<T>(int, const Inst*, const Brick*, int, const T*, long long, const T*, T*,           \

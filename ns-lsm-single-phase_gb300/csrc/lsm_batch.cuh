@@ -86,6 +86,10 @@ void bc_stage(const Inst* inst, int ninst, long long nface, BC bc, const T* phin
 template <typename T>
 void bc_full(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, BC bc, const T* src, T* dst,
              unsigned* err, cudaStream_t s);
+// bcond_lsm on the face nodes of dst only, from the pre-BC field src (the
+// interior of dst already equals src)
+template <typename T>
+void bc_faces(const Inst* inst, int ninst, long long nface, BC bc, const T* src, T* dst, unsigned* err, cudaStream_t s);
 // one reinitialisation pseudo-step on the brick table (the sign field
 // fused with the first one in sign_reinit)
 template <typename T>
@@ -103,10 +107,11 @@ void bc_reinit(const Inst* inst, int ninst, long long nface, FieldsT<T> f, BC bc
 // grid from reinit_z_blocks_per_sm): kind 0 plain, 1 recorded (the
 // pseudo-step's adjoint coefficients A'_0..2, B'_0..2 also written to cf,
 // arrays ld apart), 2 the sign field of phi0 (din) fused with the first
-// pseudo-step, 3 the same recorded
+// pseudo-step, 3 the same recorded; dout2 (nullable) gets a second copy of
+// the output
 template <typename T>
 void reinit_z(int kind, int grid, const Inst* inst, const Brick* bmap2, int nb, FieldsT<T> f, const T* din, T* dout,
-              T* cf, long long ld, unsigned* err, cudaStream_t s);
+              T* dout2, T* cf, long long ld, unsigned* err, cudaStream_t s);
 template <typename T>
 int reinit_z_blocks_per_sm();
 // water volume of every instance: k_volume adds 64-bit fixed-point sums

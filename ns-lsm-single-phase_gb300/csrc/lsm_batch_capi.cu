@@ -324,14 +324,20 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
         // the sign field and the first pseudo-step in one pass, then one
         // launch per pseudo-step
         const T* cur = S[2];
+        bool twice = false;
         for (int it = 0; it < R; ++it) {
             const bool last = it == R - 1;
             T* o = coef ? (last ? rec->D : f.d[it & 1]) : rec ? rec_d(b, *rec, it) : (last ? phi_out : f.d[it & 1]);
-            unsigned* err = (last && !rec) ? b->d_err : nullptr;
+            const bool march = coef || b->reinit_march;
+            // a recorded step's last pseudo-step also writes phi^{n+1} (its
+            // faces are then redone from the raw output)
+            T* o2 = rec && last && phi_out && march ? phi_out : nullptr;
+            twice = twice || o2 != nullptr;
+            unsigned* err = (last && !rec) || (o2 && check) ? b->d_err : nullptr;
             T* cf = coef ? rec->C + 6LL * it * (long long)b->ld : nullptr;
-            if (coef || b->reinit_march)
+            if (march)
                 B::reinit_z<T>((it == 0 ? 2 : 0) + (coef ? 1 : 0), b->rzgrid, b->d_inst, b->d_amap[2], b->namap[2], f,
-                               cur, o, cf, (long long)b->ld, err, b->stream);
+                               cur, o, o2, cf, (long long)b->ld, err, b->stream);
             else if (it == 0)
                 B::sign_reinit<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, err, b->stream);
             else
@@ -340,7 +346,9 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
             cur = o;
         }
         // recorded steps keep the raw last pseudo-step and write phi^{n+1} apart
-        if (rec && phi_out)
+        if (rec && phi_out && twice)
+            B::bc_faces<T>(b->d_inst, b->ninst, b->nface, bc, cur, phi_out, check ? b->d_err : nullptr, b->stream);
+        else if (rec && phi_out)
             B::bc_full<T>(sh, gr, b->d_inst, b->d_brick, nb, bc, cur, phi_out, check ? b->d_err : nullptr, b->stream);
     } else if (phi_out) {
         B::bc_full<T>(sh, gr, b->d_inst, b->d_brick, nb, bc, S[2], phi_out, rec && !check ? nullptr : b->d_err,
@@ -400,10 +408,10 @@ int autotune(lsm_batch* b) {
     }
     // the marching pseudo-steps do not depend on the brick shape
     const int st = timed(&dummy, &zm, [&]() {}, [&]() {
-        B::reinit_z<float>(2, b->rzgrid, b->d_inst, b->d_amap[2], b->namap[2], f, f.phi, f.d[0], nullptr, 0, nullptr,
-                           b->stream);
-        B::reinit_z<float>(0, b->rzgrid, b->d_inst, b->d_amap[2], b->namap[2], f, f.d[0], f.d[1], nullptr, 0, nullptr,
-                           b->stream);
+        B::reinit_z<float>(2, b->rzgrid, b->d_inst, b->d_amap[2], b->namap[2], f, f.phi, f.d[0], nullptr, nullptr, 0,
+                           nullptr, b->stream);
+        B::reinit_z<float>(0, b->rzgrid, b->d_inst, b->d_amap[2], b->namap[2], f, f.d[0], f.d[1], nullptr, nullptr, 0,
+                           nullptr, b->stream);
     });
     if (st != LSM_OK) return done(st);
     int best_b = 0, best_a = 0;
