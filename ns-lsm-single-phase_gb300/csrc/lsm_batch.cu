@@ -770,6 +770,12 @@ __device__ __forceinline__ G tetvol_g(const G (&a)[3], const G (&b)[3], const G 
     return fabs(t) * G(1.0 / 6.0);
 }
 
+// 4-way selection without indexing (keeps the tetrahedron in registers)
+template <typename X>
+__device__ __forceinline__ X sel4(const X (&a)[4], int i) {
+    return i == 0 ? a[0] : (i == 1 ? a[1] : (i == 2 ? a[2] : a[3]));
+}
+
 template <typename G>
 __device__ __forceinline__ G tet_water(const G (&V)[4][3], const G (&ph)[4]) {
     const G TV = tetvol_g(V[0], V[1], V[2], V[3]);
@@ -799,7 +805,9 @@ __device__ __forceinline__ G tet_water(const G (&V)[4][3], const G (&ph)[4]) {
             else if (s[1] == 0 && s[3] == 0) water = s[0] == 1;
             else water = s[0] == 1;
         } else if (nz == 3) {
-            for (int v = 0; v < 4; ++v) if (s[v] != 0) { water = s[v] == 1; break; }
+#pragma unroll
+            for (int v = 0; v < 4; ++v)
+                if (water < 0 && s[v] != 0) water = s[v] == 1;   // the non-zero vertex
         }
         return water == 0 ? G(0) : TV;   // four zero vertices: full (FlagIndex 0)
     }
@@ -809,33 +817,45 @@ __device__ __forceinline__ G tet_water(const G (&V)[4][3], const G (&ph)[4]) {
     else if (fi == 4 || fi == 11) iso = 2; else if (fi == 8 || fi == 7) iso = 3;
     if (iso >= 0) {
         // prod_k p_iso / (p_iso - p_k) over one division (the differences
-        // all carry the sign of p_iso: no cancellation)
+        // all carry the sign of p_iso: no cancellation); the factor of k =
+        // iso is an exact 1
+        const G pI = sel4(ph, iso);
         G num = G(1), den = G(1);
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (k != iso) {
-                num *= ph[iso];
-                den *= ph[iso] - ph[k];
-            }
+        for (int k = 0; k < 4; ++k) {
+            num *= k != iso ? pI : G(1);
+            den *= k != iso ? pI - ph[k] : G(1);
+        }
         const G AV = TV * (num / den);
-        return (s[iso] == -1) ? TV - AV : AV;   // isolated vertex negative: the rest is water
+        return (sel4(s, iso) == -1) ? TV - AV : AV;   // isolated vertex negative: the rest is water
     }
     // two against two (cases 4/13, 6/11, 7/10): pair (A, B) as listed by the
-    // reference's sub-tetrahedra, C, D the other pair
-    int A, B, C, D;
-    if (fi == 3 || fi == 12) { A = 0; B = 1; C = 2; D = 3; }
-    else if (fi == 5 || fi == 10) { A = 0; B = 2; C = 1; D = 3; }
-    else { A = 1; B = 2; C = 0; D = 3; }
+    // reference's sub-tetrahedra, C, D the other pair:
+    //   fi 3/12: A 0, B 1, C 2;  fi 5/10: A 0, B 2, C 1;  else A 1, B 2, C 0;  D 3
+    const int cs = (fi == 3 || fi == 12) ? 0 : ((fi == 5 || fi == 10) ? 1 : 2);
     // with the edge fractions aX = pA / (pA - pX), bX = pB / (pB - pX) the
     // share is aC aD (1 - bD) + aC bD (1 - bC) + bC bD; over the common
     // denominator (pA - pC)(pA - pD)(pB - pC)(pB - pD), using 1 - bX =
     // -pX / (pB - pX), it needs one division, and its three numerator terms
     // share one sign (A, B on one side of the interface, C, D on the other)
-    const G pA = ph[A], pB = ph[B], pC = ph[C], pD = ph[D];
+    const G pA = cs == 2 ? ph[1] : ph[0];
+    const G pB = cs == 0 ? ph[1] : ph[2];
+    const G pC = cs == 0 ? ph[2] : (cs == 1 ? ph[1] : ph[0]);
+    const G pD = ph[3];
     const G dAC = pA - pC, dAD = pA - pD, dBC = pB - pC, dBD = pB - pD;
     const G num = pB * pB * dAC * dAD - pA * pA * pD * dBC - pA * pB * pC * dAD;
     const G AV = TV * (num / (dAC * dAD * dBC * dBD));
-    return (s[A] == -1) ? TV - AV : AV;
+    return ((cs == 2 ? s[1] : s[0]) == -1) ? TV - AV : AV;
+}
+
+// vertex v of tetrahedron t of CellAnalysis's split (the c_tets table
+// {0,5,1,6}, {0,1,2,6}, {0,2,3,6}, {0,3,7,6}, {0,7,4,6}, {0,4,5,6}) as a
+// constant expression, so that unrolled loops index registers
+__host__ __device__ constexpr int cell_tet(int t, int v) {
+    return v == 0 ? 0
+                  : v == 3 ? 6
+                           : v == 1 ? (t == 0 ? 5 : t == 1 ? 1 : t == 2 ? 2 : t == 3 ? 3 : t == 4 ? 7 : 4)
+                                    : (t == 0 ? 1 : t == 1 ? 2 : t == 2 ? 3 : t == 3 ? 7 : t == 4 ? 4 : 5);
 }
 
 // CellAnalysis's split of an interface cell (src/TetrahedronMethods.F90:
@@ -843,7 +863,8 @@ __device__ __forceinline__ G tet_water(const G (&V)[4][3], const G (&ph)[4]) {
 // The classification runs in the phi type P (eps_sims = 2^-52 and +-1 are
 // exact in FP32, so its compares equal the FP64 ones on the same values),
 // the geometry in P as well, on vertex coordinates relative to the cell's
-// first vertex (C, formed in FP64 by the caller).
+// first vertex (C, formed in FP64 by the caller).  Fully unrolled: every
+// array index is a constant (no local memory).
 template <typename P>
 __device__ void cell_water_fast(const P (&ph8)[8], const P (&C)[8][3], double* K, double* S) {
     const P es = P(kEpsSims);
@@ -853,32 +874,37 @@ __device__ void cell_water_fast(const P (&ph8)[8], const P (&C)[8][3], double* K
     for (int v = 0; v < 8; ++v) pcc |= fabs(ph8[v]) < es;
     if (!pcc) {
         const P sg = signbit(ph8[0]) ? P(-1) : P(1);   // copysign(1, phi)
-        for (int v = 1; v < 8; ++v)
-            if (sg * ph8[v] < P(0)) { pcc = true; break; }
+#pragma unroll
+        for (int v = 1; v < 8; ++v) pcc |= sg * ph8[v] < P(0);
     }
     if (pcc) {
+#pragma unroll
         for (int t = 0; t < 6; ++t) {
             bool pct = false, second = true;
-            const P pa = ph8[c_tets[t][0]];
+            const P pa = ph8[cell_tet(t, 0)];
             if (pa <= es) second = false;
             if (fabs(pa) < es) pct = true;
             const P sg = signbit(pa) ? P(-1) : P(1);
+#pragma unroll
             for (int v = 1; v < 4; ++v) {
-                const P pb = ph8[c_tets[t][v]];
+                const P pb = ph8[cell_tet(t, v)];
                 if (sg * pb < P(0) || fabs(pb) < es) {
                     if (pb <= es) second = false;
                     pct = true;
                 }
             }
-            if (!pct && !second) continue;
-            P V[4][3], ph[4];
-            for (int v = 0; v < 4; ++v) {
-                const int cv = c_tets[t][v];
-                V[v][0] = C[cv][0]; V[v][1] = C[cv][1]; V[v][2] = C[cv][2];
-                ph[v] = ph8[cv];
+            if (pct || second) {
+                P V[4][3], ph[4];
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    V[v][0] = C[cell_tet(t, v)][0];
+                    V[v][1] = C[cell_tet(t, v)][1];
+                    V[v][2] = C[cell_tet(t, v)][2];
+                    ph[v] = ph8[cell_tet(t, v)];
+                }
+                if (pct) k += tet_water(V, ph);
+                else s2 += tetvol_g(V[0], V[1], V[2], V[3]);
             }
-            if (pct) k += tet_water(V, ph);
-            else s2 += tetvol_g(V[0], V[1], V[2], V[3]);
         }
     }
     *K = (double)k; *S = (double)s2;
