@@ -920,10 +920,16 @@ __device__ void cell_water_fast(const P (&ph8)[8], const P (&C)[8][3], double* K
 // to the instance's accumulators with integer atomics when its CTA moves to
 // another instance and at the end (exact and order-independent: the result
 // does not depend on the schedule; no block-wide barrier).
-__device__ __forceinline__ long long warp_sum_ll(long long v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
+// exact warp sum of 64-bit integers (two's complement, modulo 2^64): three
+// limbs of 22, 22 and 20 bits, each summed by the warp's integer reduction
+// (32 x 2^22 < 2^32), recombined; every lane gets the sum
+__device__ __forceinline__ long long warp_sum_nn(long long v) {
+    const unsigned long long u = (unsigned long long)v;
+    const unsigned m = (1u << 22) - 1u;
+    const unsigned long long s0 = __reduce_add_sync(0xffffffffu, (unsigned)(u & m));
+    const unsigned long long s1 = __reduce_add_sync(0xffffffffu, (unsigned)((u >> 22) & m));
+    const unsigned long long s2 = __reduce_add_sync(0xffffffffu, (unsigned)(u >> 44));
+    return (long long)(s0 + (s1 << 22) + (s2 << 44));
 }
 
 template <typename T, int TX, int TY, int TZ>
@@ -938,7 +944,7 @@ __global__ void __launch_bounds__(TX * TY * TZ) k_volume(const Inst* __restrict_
     int cur = -1;
     // warp-uniform (every thread of the CTA walks the same bricks)
     auto flush = [&]() {
-        const long long v[3] = {warp_sum_ll(Kq), warp_sum_ll(Sq), warp_sum_ll(Bq)};
+        const long long v[3] = {warp_sum_nn(Kq), warp_sum_nn(Sq), warp_sum_nn(Bq)};
         if (lane == 0)
             for (int c = 0; c < 3; ++c)
                 if (v[c] != 0) atomicAdd(acc + 3 * (long long)cur + c, (unsigned long long)v[c]);
