@@ -2,30 +2,39 @@
 // and adjoint, templated on the scalar type (FP32 for throughput, FP64 for
 // gradient checks).
 //
-// Forward: one launch per pass covers every instance of the batch: the CTAs
-// are persistent (grid = SMs x resident CTAs) and walk a brick table in
-// which each brick of TX x TY x TZ nodes belongs to one instance.  The
-// kernels are HBM-bound by design; per-node algorithmic traffic (FP32 words)
-//   contra 15 (u 3, metrics 9; W 3), RK stage 5/6/6 (phi_prev, phi^n, W 3;
-//   phi), sign 11 (phi0, metrics 9; s), reinit pseudo-step 12 (d, s,
-//   metrics 9; d), volume 3 (phi + 64-bit fixed-point cell volume).
+// Every launch covers every instance of the batch with persistent CTAs
+// (grid = SMs x resident CTAs) walking a table of tiles, each tile inside
+// one instance:
+//  - brick tables (TX x TY x TZ nodes, one thread per node; the autotuned
+//    forward shape): contra, volume, boundary passes, and the brick
+//    variants of the pseudo-step;
+//  - adjoint-map tiles (adj_shape): the stencil passes that march in k
+//    over 32 x 8 columns (RK stage, pseudo-steps, the reverse pseudo-step
+//    from stored coefficients), march rows / lines (stage adjoint) or an
+//    overlapped 32 x kReinRY tile (reverse pseudo-step recomputing its
+//    coefficients).
+// Per-node algorithmic traffic (FP32 words): contra 15 (u 3, metrics 9;
+// W 3), RK stage 5/6/6 (phi_prev, phi^n, W 3; phi), pseudo-step 12 (d, s,
+// metrics 9; d) or 18 recorded (+ six adjoint coefficients), volume 3 (phi
+// + 64-bit fixed-point cell volume).
 //
 // Arithmetic: the reference's formulas rearranged for the GPU (one division
 // per WENO3 reconstruction); the water volume sums FP64 hexahedron volumes
 // of the bulk water cells and the interface cells' shares (in the stencil
-// precision) with exact 64-bit fixed-point sums.  The reinitialisation uses the closed form of the
-// reference's method-0 lambda correction: with lambda = -(d1 - phi0) /
-// (dtau delta |grad phi0|) the correction dtau lambda delta |grad phi0|
-// returns d to phi0 wherever delta(phi0) |grad phi0| != 0, i.e.
-// |phi0| < eps; those nodes are folded into the sign field as s = 0 (no
-// update) and a pseudo-step reads only d, s and the metrics.
+// precision) with exact 64-bit fixed-point sums.  The reinitialisation uses
+// the closed form of the reference's method-0 lambda correction: with
+// lambda = -(d1 - phi0) / (dtau delta |grad phi0|) the correction dtau
+// lambda delta |grad phi0| returns d to phi0 wherever delta(phi0) |grad
+// phi0| != 0, i.e. |phi0| < eps; those nodes are folded into the sign field
+// as s = 0 (no update) and a pseudo-step reads only d, s and the metrics.
 //
-// Adjoint: hand-written reverse kernels, one thread per node, gathering
-// (no atomics): bcond_lsm faces in reverse order; the WENO3 stage with the
-// upwind side of every face frozen from the forward pass and the nonlinear
-// weights differentiated; the Godunov reinitialisation step with its max /
-// clip selections frozen (two passes: per-node coefficients, then gather);
-// the contravariant-velocity chain rule.
+// Adjoint: hand-written reverse kernels gathering (no atomics): bcond_lsm
+// faces in reverse order; the WENO3 stage with the upwind side of every
+// face frozen from the forward pass and the nonlinear weights
+// differentiated; the Godunov pseudo-step with its max / clip selections
+// and the sign field frozen (a 7-point stencil on lam with coefficients the
+// recorded forward step stored, or recomputed from its input); the
+// contravariant-velocity chain rule.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -125,26 +134,6 @@ __device__ __forceinline__ T rec3(T fL, T fC, T fR) {
     return vfma(w0, T(0.5) * (fL + fR) - fC, u1);
 }
 
-// gradient of rec3 with respect to (fL, fC, fR)
-template <typename T>
-__device__ __forceinline__ void rec3_grad(T fL, T fC, T fR, T* dL, T* dC, T* dR) {
-    const T eL = fL - fC, eR = fC - fR;
-    const T t0 = eR * eR + T(1.0e-6), t1 = eL * eL + T(1.0e-6);
-    const T a0 = T(2) * t1 * t1, a1 = t0 * t0;
-    const T den = a0 + a1;
-    const T w0 = a0 / den;
-    const T inv2 = T(1) / (den * den);
-    const T dw_da0 = a1 * inv2, dw_da1 = -a0 * inv2;
-    const T da0 = T(4) * t1, da1 = T(2) * t0;     // d a0 / d t1, d a1 / d t0
-    const T g = T(0.5) * (fL + fR) - fC;
-    const T wL = dw_da0 * da0 * (T(2) * eL);                                   // d w0 / d fL
-    const T wC = dw_da0 * da0 * (T(-2) * eL) + dw_da1 * da1 * (T(2) * eR);    // d w0 / d fC
-    const T wR = dw_da1 * da1 * (T(-2) * eR);                                  // d w0 / d fR
-    *dL = T(-0.5) + g * wL + T(0.5) * w0;
-    *dC = T(1.5) + g * wC - w0;
-    *dR = g * wR + T(0.5) * w0;
-}
-
 // Phi_{+1/2} - Phi_{-1/2} along one axis for the node with stencil
 // (m2, m1, c, p1, p2); lo/hi force the reference's one-sided stencils on
 // the first / last interior node (calc_RH_AD_WENO3.F90:201-245).
@@ -157,18 +146,6 @@ __device__ __forceinline__ T weno_diff(T m2, T m1, T c, T p1, T p2, T w, bool lo
     const T fp = rec3(P ? m1 : p2, P ? c : p1, P ? p1 : c);
     const T fm = rec3(M ? m2 : p1, M ? m1 : c, M ? c : m1);
     return fp - fm;
-}
-
-// gradient of weno_diff w.r.t. (m2, m1, c, p1, p2), same frozen orientation
-template <typename T>
-__device__ __forceinline__ void weno_diff_grad(const T (&s)[5], T w, bool lo, bool hi, T (&g)[5]) {
-    g[0] = g[1] = g[2] = g[3] = g[4] = T(0);
-    const bool up = w > T(0);
-    T a, b, c;
-    if (up || hi) { rec3_grad(s[1], s[2], s[3], &a, &b, &c); g[1] += a; g[2] += b; g[3] += c; }
-    else { rec3_grad(s[4], s[3], s[2], &a, &b, &c); g[4] += a; g[3] += b; g[2] += c; }
-    if (up && !lo) { rec3_grad(s[0], s[1], s[2], &a, &b, &c); g[0] -= a; g[1] -= b; g[2] -= c; }
-    else { rec3_grad(s[3], s[2], s[1], &a, &b, &c); g[3] -= a; g[2] -= b; g[1] -= c; }
 }
 
 // ------------------------------------------------------------ contra
