@@ -127,14 +127,16 @@ void volume_final(int ninst, unsigned long long* acc, double* vols, cudaStream_t
 void cell_hex(long long off, int ni, int nj, int nk, const double* x, const double* y, const double* z,
               long long* cellfix, cudaStream_t s);
 // resident CTAs per SM of a brick kernel of tile shape `shape` (FP32):
-// kernel 0 k_contra, 1 k_reinit, other k_volume
+// kernel 0 k_contra, other k_volume
 int max_blocks_per_sm(int shape, int kernel);
 
 // ------------------------------------------------------------ adjoint
-// The stencil adjoints run on their own brick maps (output nodes per brick
-// ox x oy x oz, adj_shape): 0 stage x part (8 whole rows, one warp marching
-// each), 1 stage y march, 2 stage z march, 3 reinitialisation (overlapped
-// 32 x kReinRY tile marching in k).
+// Tile maps besides the forward brick table (output nodes per tile ox x oy
+// x oz, adj_shape): 0 stage adjoint x part (8 whole rows, one warp marching
+// each), 1 stage adjoint y march, 2 the k marches over 32 x 8 columns (RK
+// stage, pseudo-steps, stage adjoint z part, reverse pseudo-step from
+// stored coefficients), 3 reverse pseudo-step recomputing its coefficients
+// (overlapped 32 x kReinRY tile marching in k).
 // The face and velocity adjoints walk the packed nodes with one thread per
 // node (instance found by binary search over the node offsets `offs`).
 struct AdjShape { int ox, oy, oz; };

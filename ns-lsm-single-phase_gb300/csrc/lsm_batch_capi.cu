@@ -1,7 +1,8 @@
 // lsm_batch_capi.cu -- host side of include/lsm_batch.h: packed device
-// buffers of a batch of instances, the brick tables of the persistent
-// kernels, the tile-shape autotuner, the CUDA graph of one physical step and
-// the checkpointed adjoint (forward_record / backward).
+// buffers of a batch of instances, the brick and tile tables of the
+// persistent kernels, the autotuner (tile shape; brick or marching
+// pseudo-steps), the CUDA graph of one physical step and the checkpointed
+// adjoint (forward_record keeping the last segment's internals / backward).
 #include <cuda_runtime.h>
 
 #include <algorithm>
