@@ -86,7 +86,7 @@ typedef struct lsm_params {
     int    call_reinitialisation;    /* reinitialise */
     int    hybrid_reinitialisation;  /* must be 0 (geometric reinit is outside the path) */
     int    TotalVolumeComputation;   /* informational (volume is always computed) */
-    int    GlobalMassCorrection;     /* 1: post-advection volume pass as in the reference */
+    int    GlobalMassCorrection;     /* 1: post-advection volume pass (lsm_convergence_volume) */
     double BigPhi;                   /* |phi| cut-off for BC order and ghost-fluid list */
     double epsReinitialisation;      /* convergence threshold of reinitialisation_test2 */
     int    M_Sphi0;                  /* sign model in calc_sign_ini: 1 Kang piecewise, 0 phi/sqrt(phi^2+(|grad|eps)^2) */
@@ -138,7 +138,9 @@ int lsm_profile_entry(int i, char* name, int name_len, long long* launches, doub
    mod(iteraciontiempo, RNfreq) == 0, bcond_lsm.  phi is advected starting
    from phi_n (ad_RKTVD3 initialises phi^{n+1} = phi^n).  `volumes_out`
    (nullable, host, 4 doubles) receives the pre-advection K-tetrahedra,
-   second-tetrahedra, bulk-cell and total volumes. */
+   second-tetrahedra, bulk-cell and total volumes.  With
+   GlobalMassCorrection the advected phi's volume is computed too (see
+   lsm_convergence_volume). */
 int lsm_levelsetmethod(lsm_handle h, const lsm_grid* g, const lsm_params* p,
                        const double* q, const double* csi, const double* eta,
                        const double* zet, const double* aj,
@@ -279,6 +281,12 @@ int lsm_mg_metrics(lsm_handle h, const lsm_grid* g, const double* x, const doubl
 /* WriteTotalWaterVolume (src/WriteTotalWaterVolume.F90:1-29): append one
    list-directed REAL(8) line to `path` (NULL: "GlobalVolume.txt"). */
 int lsm_write_total_water_volume(double volume, const char* path);
+/* ConvergenceVolume of the last lsm_levelsetmethod call on `h`
+   (src/levelsetmethod.F90:245-264): the pre-advection total volume minus the
+   K- and second-tetrahedra volumes of the advected phi when
+   GlobalMassCorrection is set, else the pre-advection total.  The reference
+   hands it to the geometric (hybrid) reinitialisation. */
+int lsm_convergence_volume(lsm_handle h, double* volume);
 
 #ifdef __cplusplus
 }

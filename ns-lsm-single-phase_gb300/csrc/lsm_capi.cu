@@ -32,6 +32,7 @@ struct lsm_context {
     unsigned* d_err = nullptr;
     double* d_result = nullptr;
     int* d_count = nullptr;
+    double conv_volume = 0.0;   // ConvergenceVolume of the last lsm_levelsetmethod
 };
 
 namespace {
@@ -819,6 +820,12 @@ int lsm_get_gfm_list(lsm_handle h, const lsm_grid* g, const lsm_params* p, const
 }
 
 // ------------------------------------------------------------------ V2
+int lsm_convergence_volume(lsm_handle h, double* out) {
+    if (!h || !out) return LSM_ERR_NULL;
+    *out = h->conv_volume;
+    return LSM_OK;
+}
+
 int lsm_write_total_water_volume(double v, const char* path) {
     FILE* f = std::fopen(path ? path : "GlobalVolume.txt", "a");
     if (!f) return set_err(nullptr, LSM_ERR_BAD_PARAM, "cannot open the global volume file");
@@ -890,6 +897,15 @@ int lsm_levelsetmethod(lsm_handle h, const lsm_grid* g, const lsm_params* p, con
             cur = X;
         }
     }
+    // 2b. GlobalMassCorrection: TotalWaterVolume of the advected phi,
+    //     levelsetmethod.F90:245-264 (the same routine and tetrahedra split
+    //     as the pre-advection pass); its K and second-tetrahedra volumes
+    //     give ConvergenceVolume below
+    if (p->GlobalMassCorrection) {
+        lsm::launch_volume(dg, cur, (const double*)dx, (const double*)dy, (const double*)dz, part, c->d_result + 4,
+                           nullptr, nullptr, c->d_err, c->stream);
+        LSM_TRY(after_launch(c));
+    }
     // 3. reinitialisation, levelsetmethod.F90:290-326
     const bool do_rn = p->call_reinitialisation && p->RNfreq > 0 && iter % p->RNfreq == 0;
     if (do_rn) {
@@ -916,10 +932,14 @@ int lsm_levelsetmethod(lsm_handle h, const lsm_grid* g, const lsm_params* p, con
         lsm::launch_copy(cur, (double*)dphi, (long long)N, c->stream);
         LSM_TRY(after_launch(c));
     }
-    double res[4];
+    double res[8];
     LSM_CU(c, cudaMemcpyAsync(res, c->d_result, sizeof(res), cudaMemcpyDeviceToHost, c->stream));
     LSM_TRY(S.finish());
-    if (vols_out) std::memcpy(vols_out, res, sizeof(res));
+    if (vols_out) std::memcpy(vols_out, res, 4 * sizeof(double));
+    // ConvergenceVolume = TotVol_PreAdv - (K + second tetrahedra after
+    // advection) with GlobalMassCorrection, else TotVol_PreAdv
+    // (levelsetmethod.F90:245-264; one rank: the reductions are identities)
+    c->conv_volume = p->GlobalMassCorrection ? res[3] - (res[4] + res[5]) : res[3];
     if (p->write_global_volume) LSM_TRY(lsm_write_total_water_volume(res[3], nullptr));
     unsigned fl = 0;
     LSM_TRY(read_err(c, &fl));

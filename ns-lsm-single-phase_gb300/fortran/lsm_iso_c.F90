@@ -189,6 +189,12 @@ module lsm_iso_c
          integer(c_int), intent(out) :: nodes(*)
       end function
 
+      integer(c_int) function lsm_convergence_volume(h, vol) bind(C, name="lsm_convergence_volume")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         real(c_double), intent(out) :: vol
+      end function
+
       integer(c_int) function lsm_get_gfm_list(h, g, p, phi, count, list, ld) bind(C, name="lsm_get_gfm_list")
          import :: c_int, c_ptr, c_double, lsm_grid, lsm_params
          type(c_ptr), value :: h

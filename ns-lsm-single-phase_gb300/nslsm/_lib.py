@@ -94,6 +94,7 @@ SIGNATURES = {
     "lsm_cell_water_volumes": (_i, [_vp, _G] + [_vp] * 5),
     "lsm_get_gfm_list": (_i, [_vp, _G, _P, _vp, C.POINTER(_i), _vp, _i]),
     "lsm_write_total_water_volume": (_i, [_d, C.c_char_p]),
+    "lsm_convergence_volume": (_i, [_vp, C.POINTER(C.c_double)]),
     "lsm_mg_metrics": (_i, [_vp, _G] + [_vp] * 7),
     "lsm_total_water_volume_noalloc": (_i, [_G] + [_vp] * 6),
     "lsm_batch_create": (_i, [C.POINTER(_vp), _i, _vp, _i, C.POINTER(LsmBatchInstance),

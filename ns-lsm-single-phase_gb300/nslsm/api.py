@@ -155,6 +155,15 @@ class LevelSet:
                    _addr(z, grid, 1, np.float64), int(iteraciontiempo), vols.ctypes.data)
         return vols
 
+    def convergence_volume(self) -> float:
+        """ConvergenceVolume of the last levelsetmethod call
+        (src/levelsetmethod.F90:245-264): the pre-advection total minus the
+        K- and second-tetrahedra volumes of the advected phi when
+        GlobalMassCorrection is set, else the pre-advection total."""
+        v = C.c_double(0.0)
+        self._call("lsm_convergence_volume", C.byref(v))
+        return v.value
+
     # ---------------------------------------------------------------- A1
     def rhs_contra_j(self, grid: Grid, q, csi, eta, zet, aj):
         self._sync_stream(q)

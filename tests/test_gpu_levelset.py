@@ -116,3 +116,27 @@ def test_error_codes(ls):
 
 def test_kernels_were_launched(ls):
     assert ls.launches > 0
+
+
+def test_global_mass_correction_convergence_volume(ls, oracle):
+    """GlobalMassCorrection (src/levelsetmethod.F90:245-264): the advected
+    phi's K- and second-tetrahedra volumes, subtracted from the
+    pre-advection total, against the oracle's volume of its advected phi;
+    without the flag the convergence volume is the pre-advection total."""
+    n = 20
+    g, x, y, z, phi, q = cases.sphere(n)
+    h = 1.0 / (n - 1)
+    kw = dict(epslsm=1.5 * h, RNtimestep=0.5 * h, RNitermax=3, delti_lsm=0.25 * h, narrowcoef=4.0, isnarrow=1)
+    csi, eta, zet, aj = oracle.mg_metrics(g, x, y, z)
+    # the oracle's advected phi: the same step without reinitialisation
+    padv = O.make_params(call_reinitialisation=0, **kw)
+    adv, rv = oracle.levelsetmethod(g, padv, q, csi, eta, zet, aj, phi, phi, x, y, z, 1)
+    post = oracle.total_water_volume(g, adv, x, y, z)
+    want = rv[3] - (post[0] + post[1])
+    for gmc, expect in ((1, want), (0, rv[3])):
+        p = O.make_params(GlobalMassCorrection=gmc, **kw)
+        cur = dev(phi)
+        v = ls.levelsetmethod(G(g), P(p), dev(q), dev(csi), dev(eta), dev(zet), dev(aj), cur, cur.clone(), dev(x),
+                              dev(y), dev(z), 1)
+        assert abs(v[3] - rv[3]) <= 1e-12 * abs(rv[3])
+        assert abs(ls.convergence_volume() - expect) <= 1e-12 * abs(rv[3]), (gmc, ls.convergence_volume(), expect)
