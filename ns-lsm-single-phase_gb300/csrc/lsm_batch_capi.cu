@@ -536,6 +536,7 @@ AdjView<T> adj_view(lsm_batch* b) {
 
 template <typename T>
 int forward_record_t(lsm_batch* b, int nsteps, int ck) {
+    ck = std::min(ck, nsteps);   // one segment either way: no slots beyond the recorded steps
     const size_t bytes = adj_elems(b, nsteps, ck) * sizeof(T);
     if (bytes > b->adj_bytes) {
         if (b->adj) {

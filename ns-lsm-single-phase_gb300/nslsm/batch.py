@@ -131,7 +131,7 @@ class LevelSetBatch:
         """Device bytes forward_record allocates for the adjoint state (padding ignored):
         N (ceil(nsteps / k) + k (5 + c R) + 9) elements, c = 6 (store) or 1 (recompute)."""
         c = 6 if adjoint_mode == "store" else 1
-        k = int(checkpoint_every)
+        k = min(int(checkpoint_every), int(nsteps))
         arrays = -(-int(nsteps) // k) + k * (5 + c * int(RNitermax)) + 9
         return int(nodes) * arrays * (8 if precision == "fp64" else 4)
 
