@@ -277,3 +277,29 @@ def test_adjoint_modes_agree(adj_cases):
         for k in range(len(adj_cases)):
             assert _rel(res["store"][0][k], res["recompute"][0][k]) <= tol
             assert _rel(res["store"][1][k], res["recompute"][1][k]) <= tol
+
+
+@pytest.mark.parametrize("mode", ["store", "recompute"])
+def test_tiny_ragged_instances_adjoint(oracle, lib_built, mode):
+    """The adjoint on instances of 4..9 nodes per axis (partial tiles in every
+    kernel) against the FP64 torch tape."""
+    from nslsm import configs
+    cases_ = []
+    for it in configs.batched_instances(n_inst=3, lo=4, hi=9, seed=8, cfl=0.5):
+        g = O.make_grid(*it.grid.shape)
+        csi, eta, zet, aj = oracle.mg_metrics(g, it.x, it.y, it.z)
+        cases_.append(dict(it=it, g=g, csi=csi, eta=eta, zet=zet, aj=aj, dt=it.time_step(csi, eta, zet)))
+    R = 2
+    b = _batch(cases_, R, adjoint_mode=mode)
+    wts = _weights(cases_)
+    gphi, gq = _adjoint(b, cases_, wts)
+    b.close()
+    for k, c in enumerate(cases_):
+        it = c["it"]
+        M = T.metrics_torch(c["csi"], c["eta"], c["zet"], "cuda")
+        p = T.to_torch(it.phi0, "cuda").requires_grad_(True)
+        q = T.to_torch(it.q, "cuda").requires_grad_(True)
+        out = T.run(p, q, M, c["dt"], it.dtau, it.eps, R, NSTEPS)
+        (out * T.to_torch(wts[k], "cuda")).sum().backward()
+        assert _rel(gphi[k], np.asfortranarray(p.grad.cpu().numpy().T)) <= 1e-10
+        assert _rel(gq[k], np.asfortranarray(q.grad.cpu().numpy().T)) <= 1e-10

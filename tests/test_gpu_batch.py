@@ -101,3 +101,32 @@ def test_batch_device_arrays_and_launch_count(small_batch):
     assert np.array_equal(np.asfortranarray(got.cpu().numpy().T), b.get_phi(0))
     assert b.nodes == sum(p["inst"].grid.n for p in small_batch)
     b.close()
+
+
+def test_tiny_ragged_instances(oracle):
+    """Instances of 4..9 nodes per axis (every tile partial in x and z, most
+    in y): brick and k-marching pseudo-steps agree bit for bit and match the
+    FP64 oracle in the band."""
+    from nslsm import configs
+    prep = []
+    for it in configs.batched_instances(n_inst=5, lo=4, hi=9, seed=5, cfl=0.5):
+        g = O.make_grid(*it.grid.shape)
+        csi, eta, zet, aj = oracle.mg_metrics(g, it.x, it.y, it.z)
+        prep.append(dict(inst=it, g=g, csi=csi, eta=eta, zet=zet, aj=aj, dt=it.time_step(csi, eta, zet)))
+    R, nsteps = 3, 3
+    outs = []
+    for shape in (0, 5):
+        b = _make_batch(prep, R, autotune=False, shape=shape)
+        vols = b.step(nsteps)
+        outs.append([b.get_phi(k) for k in range(len(prep))])
+        b.close()
+    for a, c in zip(*outs):
+        assert np.array_equal(a, c)
+    for k, p in enumerate(prep):
+        ref, rv = _oracle_run(oracle, p, R, nsteps)
+        got = outs[1][k]
+        band = np.abs(ref) < 4.0 * p["inst"].eps
+        if band.any():
+            assert float(np.abs(got - ref)[band].max()) <= BAND_TOL
+        assert float(np.abs(got - ref).max()) <= 1e-4
+        assert abs(vols[k, 3] - rv[3]) / rv[3] <= VOL_TOL
