@@ -70,3 +70,29 @@ def test_no_device_is_an_error_not_a_crash(lib_built):
     h = C.c_void_p()
     st = lib.lsm_create(C.byref(h), 0, None)
     assert st == _lib.LSM_ERR_NO_DEVICE
+
+
+def test_batch_create_validates_before_touching_a_device(lib_built):
+    """Empty and malformed batches are rejected with their status codes
+    (checked before any device call, so this runs without a GPU)."""
+    from nslsm import _lib
+    lib = _lib.load()
+    h = C.c_void_p()
+    cfg = _lib.LsmBatchConfig()
+    cfg.RNitermax, cfg.BigPhi, cfg.use_graph, cfg.autotune = 5, 5.0, 1, 1
+    for f in range(6):
+        cfg.btype_lsm[f] = 1
+    inst = (_lib.LsmBatchInstance * 2)()
+    for k in range(2):
+        inst[k].ni, inst[k].nj, inst[k].nk = 8, 8, 8
+        inst[k].dt, inst[k].dtau, inst[k].eps = 1e-3, 1e-3, 1e-2
+    assert lib.lsm_batch_create(C.byref(h), 0, None, 0, inst, C.byref(cfg)) == _lib.LSM_ERR_NULL
+    inst[1].nk = 3                                          # below the 4-node minimum
+    assert lib.lsm_batch_create(C.byref(h), 0, None, 2, inst, C.byref(cfg)) == _lib.LSM_ERR_BAD_SHAPE
+    inst[1].nk = 8
+    for field, bad in (("RNitermax", -1), ("precision", 2), ("adjoint_mode", 3)):
+        setattr(cfg, field, bad)
+        assert lib.lsm_batch_create(C.byref(h), 0, None, 2, inst, C.byref(cfg)) == _lib.LSM_ERR_BAD_PARAM, field
+        setattr(cfg, field, 0 if field != "RNitermax" else 5)
+    cfg.btype_lsm[3] = 7
+    assert lib.lsm_batch_create(C.byref(h), 0, None, 2, inst, C.byref(cfg)) == _lib.LSM_ERR_BAD_PARAM
