@@ -84,7 +84,8 @@ typedef struct lsm_params {
     int    sussman_correction_method;/* 0 only (method 1 needs testfilter, outside the path) */
     int    call_levelsetmethod;      /* advect */
     int    call_reinitialisation;    /* reinitialise */
-    int    hybrid_reinitialisation;  /* must be 0 (geometric reinit is outside the path) */
+    int    hybrid_reinitialisation;  /* 1: geometric reinitialisation (src/levelsetmethod.F90:300-309) and
+                                        advection on the AdvectionNodes band only (:218-219) */
     int    TotalVolumeComputation;   /* informational (volume is always computed) */
     int    GlobalMassCorrection;     /* 1: post-advection volume pass (lsm_convergence_volume) */
     double BigPhi;                   /* |phi| cut-off for BC order and ghost-fluid list */
@@ -98,6 +99,9 @@ typedef struct lsm_params {
     int    OrderReinitialisationBoundaries; /* 1, 2 or 3: one-sided derivative order on physical faces
                                                in calc_NormGrad_d (BiasedDerivative) */
     int    ENOBCReinitialisation;    /* 1: with order 2, ENO2Boundary instead of the 2nd-order formula */
+    double ConvergenceToleranceGeomReini; /* volume tolerance of the geometric reinitialisation's
+                                             global (Newton) and per-tetrahedron (secant, /1000)
+                                             corrections; the deck's 1.0E-09 */
 } lsm_params;
 
 /* Fill a params struct with the values of the reference's example deck
@@ -140,7 +144,12 @@ int lsm_profile_entry(int i, char* name, int name_len, long long* launches, doub
    (nullable, host, 4 doubles) receives the pre-advection K-tetrahedra,
    second-tetrahedra, bulk-cell and total volumes.  With
    GlobalMassCorrection the advected phi's volume is computed too (see
-   lsm_convergence_volume). */
+   lsm_convergence_volume).  With call_reinitialisation and
+   hybrid_reinitialisation (the deck's choice, control.dat) only the
+   AdvectionNodes band is advected and the reinitialisation is
+   lsm_geometric_reinitialisation (one subdomain without ghost planes);
+   otherwise every node is advected and reinit_scheme picks the Sussman
+   routine. */
 int lsm_levelsetmethod(lsm_handle h, const lsm_grid* g, const lsm_params* p,
                        const double* q, const double* csi, const double* eta,
                        const double* zet, const double* aj,
@@ -281,6 +290,46 @@ int lsm_mg_metrics(lsm_handle h, const lsm_grid* g, const double* x, const doubl
 /* WriteTotalWaterVolume (src/WriteTotalWaterVolume.F90:1-29): append one
    list-directed REAL(8) line to `path` (NULL: "GlobalVolume.txt"). */
 int lsm_write_total_water_volume(double volume, const char* path);
+/* geometric_reinitialisation (src/geometric_reinitialisation.F90:1-94), the
+   hybrid path's reinitialisation, TriangulationCase 1, one subdomain without
+   ghost planes (every face physical):
+    1. GetTetrahedraList (src/GetTetrahedraList.F90:1-450): the phase-change
+       ("K") tetrahedra of the six-tetrahedra split of every cell
+       (CellPnodeTetrahedronIdentification, src/TetrahedronMethods.F90:2124-2361)
+       and their vertices, the pnodes, numbered 1.. in k, j, i order;
+    2. GetIsosurfaceAndDistances (src/GetIsosurfaceAndDistances.F90:1-335):
+       the marching-tetrahedra isosurface of every K tetrahedron and, per
+       pnode, the signed distance to the triangles of the K tetrahedra of the
+       pnodes within 4 nodes; non-pnodes within 4 nodes of a pnode are tagged -1;
+    3. with GlobalMassCorrection: PiecewiseConstantFunction (secant method per
+       tetrahedron, src/PiecewiseConstantFunction.F90:1-102,
+       src/TetrahedronMethods.F90:2439-2588), OrthogonalProjection
+       (src/OrthogonalProjection.F90:1-49) and the global constant C of
+       NewtonRaphson (src/NewtonRaphsonSolver.F90) that makes the K
+       tetrahedra hold `total_water_volume`;
+    4. NeighboursPhiCorrection (src/NeighboursPhiCorrection.F90:1-346):
+       phicorrected = distance + C xi on the pnodes, and on the -1 nodes the
+       smaller of |phicorrected| and their distance to those triangles, sign
+       kept.
+   phicorrected is in/out: nodes that are neither pnodes nor tagged keep the
+   caller's value (levelsetmethod sets +-9.9 off the interface, :303-304).
+   interface_nodes_id (in/out, int) is set to 0 first, as levelsetmethod does
+   (:293), and returns the pnode ids, -1 and 0.  info (nullable, host)
+   receives the list sizes and the Newton result. */
+typedef struct lsm_geom_info {
+    int    nnodes;             /* pnodes */
+    int    ntetrahedra;        /* K tetrahedra */
+    int    nsecond;            /* nodes tagged -1 */
+    int    newton_iterations;  /* `its` after newt (0 without GlobalMassCorrection) */
+    int    newton_converged;   /* 1 when NewtonRaphson kept its C */
+    double C;                  /* CCorrected (0 without GlobalMassCorrection) */
+} lsm_geom_info;
+int lsm_geometric_reinitialisation(lsm_handle h, const lsm_grid* g, const lsm_params* p,
+                                   const double* phizero, const double* x, const double* y,
+                                   const double* z, double total_water_volume,
+                                   double* phicorrected, int* interface_nodes_id,
+                                   lsm_geom_info* info);
+
 /* ConvergenceVolume of the last lsm_levelsetmethod call on `h`
    (src/levelsetmethod.F90:245-264): the pre-advection total volume minus the
    K- and second-tetrahedra volumes of the advected phi when

@@ -18,6 +18,7 @@
 
 #include "lsm_c.h"
 #include "lsm_common.cuh"
+#include "lsm_geometric.h"
 #include "lsm_kernels.h"
 
 struct lsm_context {
@@ -408,6 +409,7 @@ void lsm_params_default(lsm_params* p) {
     p->write_global_volume = 0;
     p->OrderReinitialisationBoundaries = 1;  // control.dat
     p->ENOBCReinitialisation = 0;            // control.dat: .false.
+    p->ConvergenceToleranceGeomReini = 1.0e-9;  // control.dat
 }
 
 int lsm_create(lsm_handle* h, int device, void* stream) {
@@ -819,6 +821,64 @@ int lsm_get_gfm_list(lsm_handle h, const lsm_grid* g, const lsm_params* p, const
     return S.finish();
 }
 
+// ------------------------------------------------ geometric reinitialisation
+namespace {
+void* geo_alloc(void* ctx, const char* name, size_t bytes, cudaError_t* e) {
+    return pool_get(static_cast<lsm_context*>(ctx), name, bytes, e);
+}
+
+int geo_check(lsm_context* c, const lsm_grid* g) {
+    if (g->igp || g->jgp || g->kgp)
+        return set_err(c, LSM_ERR_UNSUPPORTED, "geometric reinitialisation runs on a grid without ghost planes");
+    for (int f = 0; f < 6; ++f)
+        if (!g->physical_face[f])
+            return set_err(c, LSM_ERR_UNSUPPORTED, "geometric reinitialisation needs every face physical");
+    return LSM_OK;
+}
+
+int geo_run(lsm_context* c, const DevGrid& dg, const lsm_params* p, const double* phi0, const double* x,
+            const double* y, const double* z, double target, double* pc, int* tag, lsm_geom_info* info) {
+    lsm::GeoInfo gi{};
+    cudaError_t e = lsm::geo_reinit(dg, phi0, x, y, z, target, p->GlobalMassCorrection ? 1 : 0,
+                                    p->ConvergenceToleranceGeomReini, pc, tag, geo_alloc, c, c->d_err, c->d_count,
+                                    &gi, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "geometric reinitialisation");
+    if (info) {
+        info->nnodes = gi.nnodes; info->ntetrahedra = gi.ntetrahedra; info->nsecond = gi.nsecond;
+        info->newton_iterations = gi.newton_iterations; info->newton_converged = gi.newton_converged;
+        info->C = gi.C;
+    }
+    return LSM_OK;
+}
+}  // namespace
+
+int lsm_geometric_reinitialisation(lsm_handle h, const lsm_grid* g, const lsm_params* p, const double* phizero,
+                                   const double* x, const double* y, const double* z, double total_water_volume,
+                                   double* phicorrected, int* interface_nodes_id, lsm_geom_info* info) {
+    LSM_PROLOGUE(h, g);
+    if (!p) return set_err(c, LSM_ERR_NULL, "params is NULL");
+    LSM_TRY(geo_check(c, g));
+    if (!phizero || !x || !y || !z || !phicorrected || !interface_nodes_id)
+        return set_err(c, LSM_ERR_NULL, "array is NULL");
+    void *dp, *dx, *dy, *dz, *dpc, *did;
+    Staging S(c);
+    S.add(phizero, 8 * N, Staging::IN, &dp);
+    S.add(x, 8 * N, Staging::IN, &dx);
+    S.add(y, 8 * N, Staging::IN, &dy);
+    S.add(z, 8 * N, Staging::IN, &dz);
+    S.add(phicorrected, 8 * N, Staging::INOUT, &dpc);
+    S.add(interface_nodes_id, 4 * N, Staging::OUT, &did);
+    LSM_TRY(S.resolve());
+    LSM_CU(c, cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), c->stream));
+    LSM_TRY(geo_run(c, dg, p, (const double*)dp, (const double*)dx, (const double*)dy, (const double*)dz,
+                    total_water_volume, (double*)dpc, (int*)did, info));
+    LSM_TRY(S.finish());
+    unsigned fl = 0;
+    LSM_TRY(read_err(c, &fl));
+    if (fl & lsm::kErrNegativeVolume) return set_err(c, LSM_ERR_NEGATIVE_VOLUME, "negative tetrahedron water volume");
+    return LSM_OK;
+}
+
 // ------------------------------------------------------------------ V2
 int lsm_convergence_volume(lsm_handle h, double* out) {
     if (!h || !out) return LSM_ERR_NULL;
@@ -842,8 +902,8 @@ int lsm_levelsetmethod(lsm_handle h, const lsm_grid* g, const lsm_params* p, con
                        const double* x, const double* y, const double* z, int iter, double* vols_out) {
     LSM_PROLOGUE(h, g);
     LSM_TRY(check_params(c, p));
-    if (p->hybrid_reinitialisation)
-        return set_err(c, LSM_ERR_UNSUPPORTED, "hybrid (geometric) reinitialisation is outside the path");
+    const bool hybrid = p->call_reinitialisation && p->hybrid_reinitialisation;
+    if (hybrid) LSM_TRY(geo_check(c, g));
     if (p->reinit_scheme != 0 && p->reinit_scheme != 1)
         return set_err(c, LSM_ERR_UNSUPPORTED, "reinit_scheme must be 0 or 1");
     if (p->sussman_correction_method != 0)
@@ -871,12 +931,20 @@ int lsm_levelsetmethod(lsm_handle h, const lsm_grid* g, const lsm_params* p, con
     const int nblk = lsm::volume_partial_blocks(dg);
     double* part = B2 ? (double*)pool_get(c, "vol_part", 24 * (size_t)nblk, &e) : nullptr;
     if (!part) return cuda_fail(c, e, "cudaMalloc(levelsetmethod)");
+    unsigned char* pcf = nullptr;
+    int* adv = nullptr;
+    if (hybrid) {
+        pcf = (unsigned char*)pool_get(c, "vol_pcflag", N, &e);
+        adv = pcf ? (int*)pool_get(c, "lsm_adv", 4 * N, &e) : nullptr;
+        if (!adv) return cuda_fail(c, e, "cudaMalloc(levelsetmethod)");
+    }
     LSM_CU(c, cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), c->stream));
-    // 1. pre-advection water volume, levelsetmethod.F90:178-196.  With the
-    //    hybrid reinitialisation off every node is advected (:218-219), so
-    //    the AdvectionNodes band is not needed here.
+    // 1. pre-advection water volume, levelsetmethod.F90:178-196.  Without the
+    //    hybrid reinitialisation every node is advected (:218-219); with it
+    //    the advection runs on the AdvectionNodes band of this pass.
     lsm::launch_volume(dg, (const double*)dphi, (const double*)dx, (const double*)dy, (const double*)dz, part,
-                       c->d_result, nullptr, nullptr, c->d_err, c->stream);
+                       c->d_result, pcf, nullptr, c->d_err, c->stream);
+    if (hybrid) lsm::launch_adv_nodes(dg, pcf, adv, c->stream);
     LSM_TRY(after_launch(c));
     // 2. advection, levelsetmethod.F90:221-243
     const double* cur = (const double*)dphi;
@@ -893,7 +961,7 @@ int lsm_levelsetmethod(lsm_handle h, const lsm_grid* g, const lsm_params* p, con
                 if (b == cur) continue;
                 if (!X) X = b; else if (!Y) Y = b;
             }
-            LSM_TRY(rk3_device(c, g, dg, p, cur, ucn, (const double*)daj, nullptr, X, Y));
+            LSM_TRY(rk3_device(c, g, dg, p, cur, ucn, (const double*)daj, adv, X, Y));
             cur = X;
         }
     }
@@ -916,7 +984,24 @@ int lsm_levelsetmethod(lsm_handle h, const lsm_grid* g, const lsm_params* p, con
             if (!X) X = b; else if (!Y) Y = b;
         }
         double* res = nullptr;
-        if (p->reinit_scheme == 1) {
+        if (p->hybrid_reinitialisation) {
+            // levelsetmethod.F90:300-309: phicorrected is the advected phi
+            // (zero without advection) with +-9.9 away from the interface,
+            // then the geometric reinitialisation against ConvergenceVolume
+            double rv[8];
+            LSM_CU(c, cudaMemcpyAsync(rv, c->d_result, sizeof(rv), cudaMemcpyDeviceToHost, c->stream));
+            LSM_CU(c, cudaStreamSynchronize(c->stream));
+            const double conv = p->GlobalMassCorrection ? rv[3] - (rv[4] + rv[5]) : rv[3];
+            if (p->call_levelsetmethod) LSM_CU(c, cudaMemcpyAsync(X, cur, 8 * N, cudaMemcpyDeviceToDevice, c->stream));
+            else LSM_CU(c, cudaMemsetAsync(X, 0, 8 * N, c->stream));
+            lsm::launch_geo_seed((long long)N, cur, X, c->stream);
+            LSM_TRY(after_launch(c));
+            int* tag = (int*)pool_get(c, "geo_tag", 4 * N, &e);
+            if (!tag) return cuda_fail(c, e, "cudaMalloc(levelsetmethod)");
+            LSM_TRY(geo_run(c, dg, p, cur, (const double*)dx, (const double*)dy, (const double*)dz, conv, X, tag,
+                            nullptr));
+            res = X;
+        } else if (p->reinit_scheme == 1) {
             // the reference's live call, src/levelsetmethod.F90:313
             LSM_TRY(sussman_device(c, dg, p, cur, (const double*)dcsi, (const double*)deta, (const double*)dzet, X,
                                    Y, nullptr));

@@ -40,7 +40,13 @@ module lsm_iso_c
       real(c_double) :: BigPhi, epsReinitialisation
       integer(c_int) :: M_Sphi0, reinit_scheme, write_global_volume
       integer(c_int) :: OrderReinitialisationBoundaries, ENOBCReinitialisation
+      real(c_double) :: ConvergenceToleranceGeomReini
    end type lsm_params
+
+   type, bind(C) :: lsm_geom_info
+      integer(c_int) :: nnodes, ntetrahedra, nsecond, newton_iterations, newton_converged
+      real(c_double) :: C
+   end type lsm_geom_info
 
    type, bind(C) :: lsm_batch_instance
       integer(c_int) :: ni, nj, nk
@@ -193,6 +199,21 @@ module lsm_iso_c
          import :: c_int, c_ptr, c_double
          type(c_ptr), value :: h
          real(c_double), intent(out) :: vol
+      end function
+
+      ! geometric_reinitialisation (the hybrid path): phicorrected in/out,
+      ! interface_nodes_id out (pnode ids, -1, 0)
+      integer(c_int) function lsm_geometric_reinitialisation(h, g, p, phizero, x, y, z, total_water_volume, &
+            phicorrected, interface_nodes_id, info) bind(C, name="lsm_geometric_reinitialisation")
+         import :: c_int, c_ptr, c_double, lsm_grid, lsm_params, lsm_geom_info
+         type(c_ptr), value :: h
+         type(lsm_grid), intent(in) :: g
+         type(lsm_params), intent(in) :: p
+         real(c_double), intent(in) :: phizero(*), x(*), y(*), z(*)
+         real(c_double), value :: total_water_volume
+         real(c_double), intent(inout) :: phicorrected(*)
+         integer(c_int), intent(out) :: interface_nodes_id(*)
+         type(lsm_geom_info), intent(out) :: info
       end function
 
       integer(c_int) function lsm_get_gfm_list(h, g, p, phi, count, list, ld) bind(C, name="lsm_get_gfm_list")

@@ -43,7 +43,13 @@ class LsmParams(C.Structure):
                 ("BigPhi", C.c_double), ("epsReinitialisation", C.c_double),
                 ("M_Sphi0", C.c_int), ("reinit_scheme", C.c_int),
                 ("write_global_volume", C.c_int), ("OrderReinitialisationBoundaries", C.c_int),
-                ("ENOBCReinitialisation", C.c_int)]
+                ("ENOBCReinitialisation", C.c_int), ("ConvergenceToleranceGeomReini", C.c_double)]
+
+
+class LsmGeomInfo(C.Structure):
+    """struct lsm_geom_info"""
+    _fields_ = [("nnodes", C.c_int), ("ntetrahedra", C.c_int), ("nsecond", C.c_int),
+                ("newton_iterations", C.c_int), ("newton_converged", C.c_int), ("C", C.c_double)]
 
 
 class LsmBatchInstance(C.Structure):
@@ -95,6 +101,7 @@ SIGNATURES = {
     "lsm_get_gfm_list": (_i, [_vp, _G, _P, _vp, C.POINTER(_i), _vp, _i]),
     "lsm_write_total_water_volume": (_i, [_d, C.c_char_p]),
     "lsm_convergence_volume": (_i, [_vp, C.POINTER(C.c_double)]),
+    "lsm_geometric_reinitialisation": (_i, [_vp, _G, _P] + [_vp] * 4 + [_d, _vp, _vp, C.POINTER(LsmGeomInfo)]),
     "lsm_mg_metrics": (_i, [_vp, _G] + [_vp] * 7),
     "lsm_total_water_volume_noalloc": (_i, [_G] + [_vp] * 6),
     "lsm_batch_create": (_i, [C.POINTER(_vp), _i, _vp, _i, C.POINTER(LsmBatchInstance),

@@ -264,6 +264,26 @@ class LevelSet:
                    _addr(zet, grid, 3, np.float64), _addr(out, grid, 1, np.float64), C.byref(it))
         return out, it.value
 
+    def geometric_reinitialisation(self, grid: Grid, p: LsmParams, phizero, x, y, z, total_water_volume: float,
+                                   phicorrected):
+        """geometric_reinitialisation (the hybrid path): -> (phicorrected, InterfaceNodesID, info dict).
+        `phicorrected` is not modified; nodes away from the interface keep its values."""
+        self._sync_stream(phizero)
+        out = _new(phizero, grid)
+        if _is_torch(out):
+            out.copy_(phicorrected)
+            self._sync_stream(out)
+        else:
+            out[...] = phicorrected
+        ids = _new(phizero, grid, dtype=np.int32)
+        g, cp = grid.to_c(), p.to_c()
+        info = _lib.LsmGeomInfo()
+        self._call("lsm_geometric_reinitialisation", C.byref(g), C.byref(cp), _addr(phizero, grid, 1, np.float64),
+                   _addr(x, grid, 1, np.float64), _addr(y, grid, 1, np.float64), _addr(z, grid, 1, np.float64),
+                   float(total_water_volume), _addr(out, grid, 1, np.float64), _addr(ids, grid, 1, np.int32),
+                   C.byref(info))
+        return out, ids, {f: getattr(info, f) for f, _ in _lib.LsmGeomInfo._fields_}
+
     # ------------------------------------------------------------ N1 - N3
     def narrowband(self, grid: Grid, p: LsmParams, phi_n):
         self._sync_stream(phi_n)

@@ -31,6 +31,7 @@ UNITS = {
     "lsm_fp64.cu": ["--fmad=false"],
     "lsm_volume.cu": ["--fmad=false"],
     "lsm_sussman.cu": ["--fmad=false"],
+    "lsm_geometric.cu": ["--fmad=false"],
     "lsm_capi.cu": ["-Xcompiler", "-fvisibility=default"],
     "lsm_batch.cu": ["--fmad=true"],
     "lsm_batch_capi.cu": ["-Xcompiler", "-fvisibility=default"],

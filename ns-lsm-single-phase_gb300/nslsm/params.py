@@ -40,6 +40,7 @@ class LsmParams:
     write_global_volume: bool = False
     OrderReinitialisationBoundaries: int = 1
     ENOBCReinitialisation: bool = False
+    ConvergenceToleranceGeomReini: float = 1.0e-9
 
     def to_c(self) -> _CParams:
         p = _CParams()
@@ -136,7 +137,7 @@ def read_ind3dmg_lsm(path_or_text: str, delti: float, nzone: int = 1, myzone: in
     p.hybrid_reinitialisation = _logical(r.read(1)[0])
     r.read(1)          # sweep_lsqm
     r.read(1)          # radius_lsqm
-    r.read(1)          # ConvergenceToleranceGeomReini
+    p.ConvergenceToleranceGeomReini = _real(r.read(1)[0])
     p.TotalVolumeComputation = _logical(r.read(1)[0])
     p.GlobalMassCorrection = _logical(r.read(1)[0])
     nsave = int(r.read(1)[0])

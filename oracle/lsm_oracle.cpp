@@ -1111,19 +1111,572 @@ int oracle_reinitialisation_test2(const lsm_grid* gg, const lsm_params* p, const
     return LSM_OK;
 }
 
+} /* extern "C" */
+
+/* ====================================== geometric reinitialisation ====== */
+/* The hybrid path's reinitialisation, src/geometric_reinitialisation.F90:1-94,
+   restated with the reference's own data structures (lists built by the
+   three loops of GetTetrahedraList) so that it checks the GPU version, which
+   enumerates the same lists implicitly. */
+namespace {
+
+/* NORM2 of a 3-vector as gfortran expands the intrinsic: a scaled sum of
+   squares (skip zeros; rescale when a larger magnitude appears) and
+   sqrt(sum) * scale. */
+inline double norm2v(const double* a) {
+    double scale = 1.0, r = 0.0;
+    for (int c = 0; c < 3; ++c) {
+        if (a[c] != 0.0) {
+            const double ax = std::fabs(a[c]);
+            if (scale < ax) {
+                const double v = scale / ax;
+                r = 1.0 + r * v * v;
+                scale = ax;
+            } else {
+                const double v = ax / scale;
+                r = r + v * v;
+            }
+        }
+    }
+    return std::sqrt(r) * scale;
+}
+inline void sub3(const double* a, const double* b, double* c) {
+    c[0] = a[0] - b[0]; c[1] = a[1] - b[1]; c[2] = a[2] - b[2];
+}
+inline double fsign1(double x) { return std::copysign(1.0, x); } /* sign(one, x) */
+
+/* GetTriangleArea, src/TetrahedronMethods.F90:691-707 */
+double tri_area(const double T[3][3]) {
+    double u[3], v[3], c[3];
+    sub3(T[1], T[0], u); sub3(T[2], T[0], v); cross3(u, v, c);
+    return 0.5 * norm2v(c);
+}
+
+/* TetrahedronTriangles, src/TetrahedronMethods.F90:86-104 (edge numbers 0..5) */
+const int kTetTris[16][6] = {{-1, -1, -1, -1, -1, -1}, {0, 3, 2, -1, -1, -1}, {0, 1, 4, -1, -1, -1},
+                             {1, 4, 2, 2, 4, 3},       {1, 2, 5, -1, -1, -1}, {0, 3, 5, 0, 5, 1},
+                             {0, 2, 5, 0, 5, 4},       {5, 4, 3, -1, -1, -1}, {3, 4, 5, -1, -1, -1},
+                             {4, 5, 0, 5, 2, 0},       {1, 5, 0, 5, 3, 0},    {5, 2, 1, -1, -1, -1},
+                             {3, 4, 2, 2, 4, 1},       {4, 1, 0, -1, -1, -1}, {2, 3, 0, -1, -1, -1},
+                             {-1, -1, -1, -1, -1, -1}};
+
+struct MTOut { int ntri; double tri[2][3][3]; double area, wv; };
+
+/* MarchingTetrahedron with all its outputs, src/TetrahedronMethods.F90:26-664 */
+void marching_tet_full(const double V[4][3], const double ph[4], MTOut* o, int* err) {
+    o->ntri = 0; o->area = 0.0; o->wv = 0.0;
+    std::memset(o->tri, 0, sizeof(o->tri));
+    int s[4], nz = 0;
+    bool allp = true, alln = true, allge = true, allle = true;
+    for (int v = 0; v < 4; ++v) {
+        s[v] = ph[v] > kTiny ? 1 : (ph[v] < -kTiny ? -1 : 0);
+        allp &= s[v] == 1; alln &= s[v] == -1; nz += s[v] == 0;
+        allge &= s[v] >= 0; allle &= s[v] <= 0;
+    }
+    if (allp) { o->wv = tet_volume(V[0], V[1], V[2], V[3]); return; }
+    if (alln) return;
+    int fi = 0;
+    auto put = [&](int a, int b, int c) {
+        for (int q = 0; q < 3; ++q) { o->tri[0][0][q] = V[a][q]; o->tri[0][1][q] = V[b][q]; o->tri[0][2][q] = V[c][q]; }
+    };
+    auto vol_if = [&](bool water) { o->wv = water ? tet_volume(V[0], V[1], V[2], V[3]) : 0.0; };
+    if (nz > 0 && (allge || allle)) {
+        if (nz == 1) { /* one zero vertex: a point "isosurface", ntriangles = -1 */
+            o->ntri = -1;
+            if (s[0] == 0) { put(0, 0, 0); vol_if(s[1] == 1); return; }
+            if (s[1] == 0) { put(1, 1, 1); vol_if(s[0] == 1); return; }
+            if (s[2] == 0) { put(2, 2, 2); vol_if(s[0] == 1); return; }
+            put(3, 3, 3); vol_if(s[0] == 1); return;
+        }
+        if (nz == 2) { /* an edge, ntriangles = -2 */
+            o->ntri = -2;
+            if (s[0] == 0 && s[1] == 0) { put(0, 1, 1); vol_if(s[2] == 1); return; }
+            if (s[1] == 0 && s[2] == 0) { put(1, 2, 2); vol_if(s[0] == 1); return; }
+            if (s[2] == 0 && s[0] == 0) { put(2, 0, 0); vol_if(s[1] == 1); return; }
+            if (s[0] == 0 && s[3] == 0) { put(0, 3, 3); vol_if(s[1] == 1); return; }
+            if (s[1] == 0 && s[3] == 0) { put(1, 3, 3); vol_if(s[0] == 1); return; }
+            put(2, 3, 3); vol_if(s[0] == 1); return;
+        }
+        if (nz == 3) { /* a face, one triangle */
+            o->ntri = 1;
+            const int f[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+            for (int v = 0; v < 4; ++v)
+                if (s[v] != 0) {
+                    put(f[v][0], f[v][1], f[v][2]);
+                    o->area = tri_area(o->tri[0]);
+                    vol_if(s[v] == 1);
+                    return;
+                }
+        }
+        /* four zero vertices: FlagIndex stays 0 */
+    } else {
+        for (int v = 0; v < 4; ++v)
+            if (s[v] == -1) fi |= 1 << v;
+    }
+    if (fi == 0) o->wv = tet_volume(V[0], V[1], V[2], V[3]);
+    if (fi == 15) o->wv = 0.0;
+    const int ef = kEdgeFlags[fi];
+    if (ef == 0) return;
+    double E[6][3];
+    for (int e = 0; e < 6; ++e) E[e][0] = E[e][1] = E[e][2] = -9.9;
+    for (int e = 0; e < 6; ++e) {
+        if (!(ef >> e & 1)) continue;
+        const int sv = kEdge[e][0], ev = kEdge[e][1];
+        const double den = ph[ev] - ph[sv];
+        const double sc = std::fabs(den) < kEpsSims * kEpsSims * kEpsSims ? 0.0 : ph[ev] / den;
+        for (int c = 0; c < 3; ++c) E[e][c] = V[ev][c] + sc * (V[sv][c] - V[ev][c]);
+    }
+    for (int t = 0; t < 2; ++t) {
+        if (kTetTris[fi][3 * t] < 0) break;
+        o->ntri += 1;
+        for (int v = 0; v < 3; ++v)
+            for (int c = 0; c < 3; ++c) o->tri[t][v][c] = E[kTetTris[fi][3 * t + v]][c];
+        o->area = o->area + tri_area(o->tri[t]);
+    }
+    if (fi == 0) o->wv = tet_volume(V[0], V[1], V[2], V[3]);
+    else if (fi == 15) o->wv = 0.0;
+    else o->wv = water_volume(V, E, fi, err);
+}
+
+/* DistancePointLine, src/TetrahedronMethods.F90:1356-1399 */
+double dist_point_line(const double* A, const double* B, const double* P) {
+    double AB[3], AP[3], BA[3], BP[3];
+    sub3(B, A, AB); sub3(P, A, AP); sub3(A, B, BA); sub3(P, B, BP);
+    bool valid = true;
+    if (norm2v(AB) < kEpsSims) valid = false;
+    if (dot3(AB, AP) < 0.0) valid = false;
+    if (dot3(BA, BP) < 0.0) valid = false;
+    if (valid) {
+        double c[3];
+        cross3(AP, BP, c);
+        return norm2v(c) / norm2v(AB);
+    }
+    const double a = norm2v(AP), b = norm2v(BP);
+    return b < a ? b : a;
+}
+
+/* CheckProjectionPointOnATriangle3, src/TetrahedronMethods.F90:1593-1684.
+   Kept from the reference: alpha (the weight of P3 in the standard
+   barycentric form) multiplies P1 and gamma multiplies P3. */
+bool projection3(const double T[3][3], const double* P, double* pd) {
+    double d[3];
+    sub3(T[0], T[1], d); if (norm2v(d) <= kEpsSims) return false;
+    sub3(T[0], T[2], d); if (norm2v(d) <= kEpsSims) return false;
+    sub3(T[1], T[2], d); if (norm2v(d) <= kEpsSims) return false;
+    double u[3], v[3], w[3], nv[3], cu[3], cw[3];
+    sub3(T[1], T[0], u); sub3(T[2], T[0], v); sub3(P, T[0], w);
+    cross3(u, v, nv);
+    cross3(u, w, cu); cross3(w, v, cw);
+    const double nn = dot3(nv, nv);
+    const double alpha = dot3(cu, nv) / nn;
+    const double beta = dot3(cw, nv) / nn;
+    const double gamma = 1.0 - beta - alpha;
+    double pp[3], dd[3];
+    for (int c = 0; c < 3; ++c) pp[c] = alpha * T[0][c] + beta * T[1][c] + gamma * T[2][c];
+    sub3(P, pp, dd);
+    const double dist = norm2v(dd);
+    const bool inside = alpha > 0.0 && alpha < 1.0 && beta > 0.0 && beta < 1.0 && gamma > 0.0 && gamma < 1.0;
+    *pd = inside ? dist : 999.9;
+    return inside;
+}
+
+/* DistancePointTriangle, src/TetrahedronMethods.F90:1008-1070 */
+double dist_point_triangle(const double T[3][3], const double* P) {
+    double d[3];
+    sub3(P, T[0], d); double m = norm2v(d);
+    sub3(P, T[1], d); m = std::min(m, norm2v(d));
+    sub3(P, T[2], d); m = std::min(m, norm2v(d));
+    m = std::min(m, dist_point_line(T[0], T[1], P));
+    m = std::min(m, dist_point_line(T[1], T[2], P));
+    m = std::min(m, dist_point_line(T[2], T[0], P));
+    double pd;
+    if (projection3(T, P, &pd)) m = std::min(m, pd);
+    return m;
+}
+
+/* the reference's running minimum: d + exsign (da - d), exsign = 1 when da <= d */
+inline double run_min(double d, double da) {
+    const double ex = (fsign1(d - da) + 1.0) / 2.0;
+    return d + ex * (da - d);
+}
+
+const int kCellOff[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+const int kCellTets[6][4] = {{0, 5, 1, 6}, {0, 1, 2, 6}, {0, 2, 3, 6}, {0, 3, 7, 6}, {0, 7, 4, 6}, {0, 4, 5, 6}};
+
+/* CellPnodeTetrahedronIdentification, src/TetrahedronMethods.F90:2124-2361
+   (TriangulationCase 1): bit t (1..6) of *tets marks a phase-change
+   tetrahedron, bit v (0..7) of *verts a vertex of one. */
+void cell_pnodes(const double P[8], int* verts, int* tets) {
+    *verts = 0; *tets = 0;
+    bool allw = true, alla = true, anyz = false;
+    for (int v = 0; v < 8; ++v) {
+        allw &= P[v] > kEpsSims; alla &= P[v] < -kEpsSims; anyz |= std::fabs(P[v]) < kEpsSims;
+    }
+    if (allw || alla) return;
+    bool pc = anyz;
+    if (!pc) {
+        const double s0 = fsign1(P[0]);
+        for (int v = 1; v < 8 && !pc; ++v) pc = s0 * P[v] < 0.0;
+    }
+    if (!pc) return;
+    for (int t = 0; t < 6; ++t) {
+        double a = P[kCellTets[t][0]];
+        bool change = std::fabs(a) < kEpsSims, second = !(a <= kEpsSims);
+        const double sg = fsign1(a);
+        for (int q = 1; q < 4; ++q) {
+            a = P[kCellTets[t][q]];
+            if (sg * a < 0.0 || std::fabs(a) < kEpsSims) {
+                if (a <= kEpsSims) second = false;
+                change = true;
+            }
+        }
+        if (change && !second) {
+            *tets |= 1 << (t + 1);
+            for (int q = 0; q < 4; ++q) *verts |= 1 << kCellTets[t][q];
+        }
+    }
+}
+
+struct GPNode { int i, j, k; double x, y, z, phi, sd, xi; int nasoc; int asoc[24]; };
+struct GKTet { int v[4]; int nis; double tri[2][3][3]; double area, wv, etaK; };
+
+struct Geo {
+    const Grid& g;
+    std::vector<GPNode> nodes;
+    std::vector<GKTet> tets;
+    explicit Geo(const Grid& gg) : g(gg) {}
+
+    void vertices(const GKTet& t, double V[4][3]) const {
+        for (int q = 0; q < 4; ++q) {
+            const GPNode& n = nodes[t.v[q]];
+            V[q][0] = n.x; V[q][1] = n.y; V[q][2] = n.z;
+        }
+    }
+    /* the distance loop body shared by GetIsosurfaceAndDistances and
+       NeighboursPhiCorrection: triangles of tetrahedron t against point P */
+    double tet_min(const GKTet& t, const double* P, double d) const {
+        if (t.nis > 0 && t.area > 0.0) {
+            d = run_min(d, dist_point_triangle(t.tri[0], P));
+            if (t.nis > 1) d = run_min(d, dist_point_triangle(t.tri[1], P));
+        }
+        return d;
+    }
+};
+
+/* LocalVolumeVariation, src/TetrahedronMethods.F90:2390-2437 */
+double local_dv(double eta, const double V[4][3], const double ph[4], double v0, int* err) {
+    double a[4];
+    for (int q = 0; q < 4; ++q) a[q] = ph[q] + eta;
+    MTOut o;
+    marching_tet_full(V, a, &o, err);
+    return v0 - o.wv;
+}
+
+/* SecantMethodLocalCorrection, src/TetrahedronMethods.F90:2439-2588 */
+double secant_eta(const double V[4][3], double vol0, double area0, const double ph[4], double tol, int maxit,
+                  bool* conv, int* err) {
+    *conv = false;
+    MTOut o;
+    marching_tet_full(V, ph, &o, err);
+    const double dv0 = vol0 - o.wv;
+    if (std::fabs(dv0) < tol) { *conv = true; return 0.0; }
+    double x0 = o.area > kEpsSims ? dv0 / o.area : 0.0;
+    double x1 = area0 > kEpsSims ? dv0 / area0 : 0.0;
+    double f0 = local_dv(x0, V, ph, vol0, err);
+    double f1 = local_dv(x1, V, ph, vol0, err);
+    if (std::fabs(f0) < tol || std::fabs(f1) < tol) {
+        *conv = true;
+        return std::fabs(f1) < std::fabs(f0) ? x1 : x0;
+    }
+    double x2 = 0.0; /* unset in the reference when the loop exits at once (then not converged) */
+    for (int it = 1; it <= maxit; ++it) {
+        if (std::fabs(f1 - f0) < kEpsSims) break;
+        x2 = x1 - f1 * (x1 - x0) / (f1 - f0);
+        x0 = x1; x1 = x2; f0 = f1;
+        f1 = local_dv(x1, V, ph, vol0, err);
+        if (std::fabs(f1) < tol) { *conv = true; break; }
+    }
+    if (std::fabs(f1) > dv0) x2 = 0.0;
+    return x2;
+}
+
+/* funcv, src/NewtonRaphsonSolver.F90: target - K-tetrahedra volume of
+   phi* + C xi (a node's correction is dropped where it changes the sign) */
+double geo_funcv(const Geo& G, double target, double C, int* err) {
+    double tot = 0.0;
+    for (const GKTet& t : G.tets) {
+        double V[4][3], a[4];
+        G.vertices(t, V);
+        for (int q = 0; q < 4; ++q) {
+            const GPNode& n = G.nodes[t.v[q]];
+            const double sd = n.sd, ca = C * n.xi;
+            a[q] = sd + ca / 2.0 * std::fabs(fsign1(sd) + fsign1(sd + ca));
+        }
+        MTOut o;
+        marching_tet_full(V, a, &o, err);
+        tot = tot + o.wv;
+    }
+    return target - tot;
+}
+
+/* NewtonRaphson + newt/fdjac/fmin/lnsrch/ludcmp/lubksb for one unknown,
+   src/NewtonRaphsonSolver.F90 (Numerical Recipes' globally convergent
+   Newton).  The PARAMETERs written as default-real literals (1.e-12, 1.e-7,
+   1.e-4, .1) are single precision promoted to REAL(8).  Returns C. */
+double geo_newton(const Geo& G, double target, double tol, int* its_out, bool* converged, int* err) {
+    const int MAXITS = 20;
+    const double TOLF = (double)1.e-12f, TOLMIN = (double)1.e-12f, TOLX = (double)1.e-12f, STPMX = 100.0;
+    const double ALF = (double)1.e-4f, TOLXL = (double)1.e-7f, P1 = (double)0.1f;
+    const double EPS = std::sqrt(kEpsSims);
+    double x = 0.0;            /* C_initial_guest */
+    bool check = false;        /* not set by newt on its zero-Jacobian return */
+    int its = 1;
+    double fvec = geo_funcv(G, target, x, err);
+    double f = 0.5 * (0.0 + fvec * fvec);
+    auto finish = [&](bool conv_path) {
+        (void)conv_path;
+        *its_out = its;
+        *converged = its < MAXITS && !check;
+        return *converged ? x : 0.0;
+    };
+    if (std::fabs(fvec) < 0.01 * TOLF && std::fabs(fvec) < tol) { check = false; return finish(true); }
+    const double stpmax = STPMX * std::max(std::sqrt(0.0 + x * x), 1.0);
+    for (its = 1; its <= MAXITS; ++its) {
+        /* fdjac */
+        const double temp = x;
+        double h = EPS * std::fabs(temp);
+        if (h < kEpsSims) h = EPS;
+        x = temp + h;
+        h = x - temp;
+        const double fh = geo_funcv(G, target, x, err);
+        x = temp;
+        double fjac = (fh - fvec) / h;
+        if (std::fabs(0.0 + fjac) < tol) return finish(false); /* zero Jacobian */
+        fvec = geo_funcv(G, target, x, err);
+        const double gr = 0.0 + fjac * fvec;
+        const double xold = x, fold = f;
+        double p = -fvec;
+        /* ludcmp / lubksb, n = 1 */
+        if (fjac == 0.0) fjac = 1.0e-20;
+        p = p / fjac;
+        /* lnsrch */
+        check = false;
+        const double sum = std::sqrt(0.0 + p * p);
+        if (sum > stpmax) p = p * stpmax / sum;
+        const double slope = 0.0 + gr * p;
+        const double test = std::fabs(p) / std::max(std::fabs(xold), 1.0);
+        const double alamin = TOLXL / test;
+        double alam = 1.0, alam2 = 2.0, f2 = 2.0, tmplam = 0.0;
+        for (;;) {
+            x = xold + alam * p;
+            fvec = geo_funcv(G, target, x, err);
+            f = 0.5 * (0.0 + fvec * fvec);
+            if (alam < alamin) { x = xold; check = true; break; }
+            if (f <= fold + ALF * alam * slope) break;
+            if (alam == 1.0) {
+                tmplam = -slope / (2.0 * (f - fold - slope));
+            } else {
+                const double rhs1 = f - fold - alam * slope, rhs2 = f2 - fold - alam2 * slope;
+                const double a = (rhs1 / (alam * alam) - rhs2 / (alam2 * alam2)) / (alam - alam2);
+                const double b = (-alam2 * rhs1 / (alam * alam) + alam * rhs2 / (alam2 * alam2)) / (alam - alam2);
+                if (a == 0.0) {
+                    tmplam = -slope / (2.0 * b);
+                } else {
+                    const double disc = b * b - 3.0 * a * slope;
+                    if (disc < 0.0) tmplam = 0.5 * alam;
+                    else if (b <= 0.0) tmplam = (-b + std::sqrt(disc)) / (3.0 * a);
+                    else tmplam = -slope / (b + std::sqrt(disc));
+                }
+                if (tmplam > 0.5 * alam) tmplam = 0.5 * alam;
+            }
+            alam2 = alam; f2 = f;
+            alam = std::max(tmplam, P1 * alam);
+        }
+        if (std::fabs(fvec) < TOLF && std::fabs(fvec) < tol) { check = false; return finish(true); }
+        if (check) {
+            const double den = std::max(f, 0.5 * 1);
+            const double t2 = std::fabs(gr) * std::max(std::fabs(x), 1.0) / den;
+            check = !(t2 < TOLMIN);
+            return finish(false);
+        }
+        const double t3 = std::fabs(x - xold) / std::max(std::fabs(x), 1.0);
+        if (t3 < TOLX && std::fabs(fvec) < tol) return finish(true);
+    }
+    return finish(false); /* its = MAXITS + 1 */
+}
+
+} /* namespace */
+
+extern "C" {
+
+/* geometric_reinitialisation, src/geometric_reinitialisation.F90:1-94
+   (TriangulationCase 1, one rank, no ghost planes, no blanking).
+   info (nullable): [nnodes, ntetrahedra, nsecond, newton its, converged]. */
+int oracle_geometric_reinitialisation(const lsm_grid* gg, const lsm_params* p, const double* phi0, const double* x,
+                                      const double* y, const double* z, double total_water_volume, double* pc,
+                                      int* ids, int* info_i, double* info_c) {
+    int st = check_grid(gg); if (st) return st;
+    if (gg->igp || gg->jgp || gg->kgp) return LSM_ERR_UNSUPPORTED;
+    for (int f = 0; f < 6; ++f) if (!gg->physical_face[f]) return LSM_ERR_UNSUPPORTED;
+    Grid g(gg);
+    Geo G(g);
+    int err = 0;
+    std::memset(ids, 0, sizeof(int) * g.n);
+    /* GetTetrahedraList, first loop: cells, pnode flags and K-tetrahedra bits */
+    std::vector<int> cellbits(g.n, 0);
+    for (int k = g.kl; k < g.ku; ++k)
+        for (int j = g.jl; j < g.ju; ++j)
+            for (int i = g.il; i < g.iu; ++i) {
+                double P[8];
+                for (int v = 0; v < 8; ++v) P[v] = phi0[g.id(i + kCellOff[v][0], j + kCellOff[v][1], k + kCellOff[v][2])];
+                int verts, tets;
+                cell_pnodes(P, &verts, &tets);
+                for (int v = 0; v < 8; ++v)
+                    if (verts >> v & 1) ids[g.id(i + kCellOff[v][0], j + kCellOff[v][1], k + kCellOff[v][2])] = 1;
+                cellbits[g.id(i, j, k)] = tets;
+            }
+    /* second loop: number the pnodes in k, j, i order */
+    for (int k = g.kl; k <= g.ku; ++k)
+        for (int j = g.jl; j <= g.ju; ++j)
+            for (int i = g.il; i <= g.iu; ++i) {
+                const long l = g.id(i, j, k);
+                if (ids[l] > 0) {
+                    GPNode n{};
+                    n.i = i; n.j = j; n.k = k;
+                    n.x = x[l]; n.y = y[l]; n.z = z[l]; n.phi = phi0[l];
+                    n.sd = 99.9; n.xi = 0.0; n.nasoc = 0;
+                    G.nodes.push_back(n);
+                    ids[l] = (int)G.nodes.size();
+                }
+            }
+    /* third loop: the K tetrahedra and each pnode's list of them */
+    for (int k = g.kl; k < g.ku; ++k)
+        for (int j = g.jl; j < g.ju; ++j)
+            for (int i = g.il; i < g.iu; ++i) {
+                const int bits = cellbits[g.id(i, j, k)];
+                if (!bits) continue;
+                int nid[8];
+                for (int v = 0; v < 8; ++v) nid[v] = ids[g.id(i + kCellOff[v][0], j + kCellOff[v][1], k + kCellOff[v][2])];
+                for (int t = 0; t < 6; ++t) {
+                    if (!(bits >> (t + 1) & 1)) continue;
+                    GKTet T{};
+                    for (int q = 0; q < 4; ++q) T.v[q] = nid[kCellTets[t][q]] - 1;
+                    const int tid = (int)G.tets.size();
+                    G.tets.push_back(T);
+                    for (int q = 0; q < 4; ++q) {
+                        GPNode& n = G.nodes[T.v[q]];
+                        n.asoc[n.nasoc++] = tid;
+                    }
+                }
+            }
+    /* GetIsosurfaceAndDistances: marching tetrahedra on the K tetrahedra */
+    for (GKTet& t : G.tets) {
+        double V[4][3], ph[4];
+        G.vertices(t, V);
+        for (int q = 0; q < 4; ++q) ph[q] = G.nodes[t.v[q]].phi;
+        MTOut o;
+        marching_tet_full(V, ph, &o, &err);
+        t.area = o.area; t.wv = o.wv;
+        t.nis = o.ntri > 0 ? o.ntri : 0;
+        std::memcpy(t.tri, o.tri, sizeof(t.tri));
+    }
+    /* ... and the pnodes' distances over the +-4 box, tagging non-pnodes -1 */
+    for (GPNode& n : G.nodes) {
+        const double P[3] = {n.x, n.y, n.z};
+        double dp = 10.0;
+        for (int ks = std::max(n.k - 4, g.kl); ks <= std::min(n.k + 4, g.ku); ++ks)
+            for (int js = std::max(n.j - 4, g.jl); js <= std::min(n.j + 4, g.ju); ++js)
+                for (int is = std::max(n.i - 4, g.il); is <= std::min(n.i + 4, g.iu); ++is) {
+                    const long l = g.id(is, js, ks);
+                    if (ids[l] > 0) {
+                        const GPNode& m = G.nodes[ids[l] - 1];
+                        for (int a = 0; a < m.nasoc; ++a) {
+                            dp = G.tet_min(G.tets[m.asoc[a]], P, dp);
+                            const double asd = std::fabs(n.sd);
+                            const double ex2 = (fsign1(asd - dp) + 1.0) / 2.0;
+                            n.sd = asd + ex2 * (dp - asd);
+                            n.sd = fsign1(n.phi) * n.sd;
+                        }
+                    } else {
+                        ids[l] = -1;
+                    }
+                }
+    }
+    /* GlobalMassCorrection: per-tetrahedron eta (secant), xi, Newton's C */
+    double Cc = 0.0;
+    int its = 0;
+    bool conv = false;
+    if (p->GlobalMassCorrection) {
+        const double tol = p->ConvergenceToleranceGeomReini / 1000.0;
+        for (GKTet& t : G.tets) {
+            double V[4][3], ph[4];
+            G.vertices(t, V);
+            for (int q = 0; q < 4; ++q) ph[q] = G.nodes[t.v[q]].sd;
+            bool c = false;
+            const double e = secant_eta(V, t.wv, t.area, ph, tol, 40, &c, &err);
+            t.etaK = c ? e : 0.0;
+        }
+        for (GPNode& n : G.nodes)
+            for (int a = 0; a < n.nasoc; ++a) n.xi = n.xi + G.tets[n.asoc[a]].etaK / (double)n.nasoc;
+        Cc = geo_newton(G, total_water_volume, p->ConvergenceToleranceGeomReini, &its, &conv, &err);
+    }
+    /* NeighboursPhiCorrection: pnodes ... */
+    for (GPNode& n : G.nodes) {
+        const double pcf = std::fabs(fsign1(n.sd) + fsign1(n.sd + Cc * n.xi)) / 2.0;
+        const double aux = pcf * Cc * n.xi;
+        n.phi = n.sd + aux;
+        pc[g.id(n.i, n.j, n.k)] = n.phi;
+    }
+    /* ... and the -1 nodes */
+    int nsecond = 0;
+    for (int k = g.kl; k <= g.ku; ++k)
+        for (int j = g.jl; j <= g.ju; ++j)
+            for (int i = g.il; i <= g.iu; ++i) {
+                const long l0 = g.id(i, j, k);
+                if (ids[l0] >= 0) continue;
+                ++nsecond;
+                const int km = std::max(k - 4, g.kl), kp = std::min(k + 4, g.ku);
+                const int jm = std::max(j - 4, g.jl), jp = std::min(j + 4, g.ju);
+                const int im = std::max(i - 4, g.il), ip = std::min(i + 4, g.iu);
+                const double P[3] = {x[l0], y[l0], z[l0]};
+                for (int ks = km; ks <= kp; ++ks)
+                    for (int js = jm; js <= jp; ++js)
+                        for (int is = im; is <= ip; ++is) {
+                            const long l = g.id(is, js, ks);
+                            if (ids[l] <= 0) continue;
+                            const GPNode& m = G.nodes[ids[l] - 1];
+                            double dp = 10.0;
+                            for (int a = 0; a < m.nasoc; ++a) {
+                                dp = G.tet_min(G.tets[m.asoc[a]], P, dp);
+                                const double apc = std::fabs(pc[l0]);
+                                const double ex2 = (fsign1(apc - dp) + 1.0) / 2.0;
+                                const double aux = apc + ex2 * (dp - apc);
+                                pc[l0] = fsign1(pc[l0]) * aux;
+                            }
+                        }
+            }
+    if (info_i) {
+        info_i[0] = (int)G.nodes.size(); info_i[1] = (int)G.tets.size(); info_i[2] = nsecond;
+        info_i[3] = its; info_i[4] = conv ? 1 : 0;
+    }
+    if (info_c) *info_c = Cc;
+    return err ? LSM_ERR_NEGATIVE_VOLUME : LSM_OK;
+}
+
+
 /* ------------------------------------------------------------------ A0 --- */
-/* levelsetmethod, src/levelsetmethod.F90:1-372, Sussman-Fatemi branch
-   (hybrid_reinitialisation = .false.) with `reinitialization` (reinit_scheme
-   0) or the live `reinitialisation_test2` (reinit_scheme 1) as the
-   reinitialisation routine. */
+/* levelsetmethod, src/levelsetmethod.F90:1-372: the hybrid branch
+   (geometric reinitialisation, advection on the AdvectionNodes band) or the
+   Sussman-Fatemi branch with `reinitialization` (reinit_scheme 0) or the
+   live `reinitialisation_test2` (reinit_scheme 1). */
 int oracle_levelsetmethod_x(const lsm_grid* gg, const lsm_params* p, const double* q, const double* csi,
                             const double* eta, const double* zet, const double* aj, double* phi,
                             const double* phin, const double* x, const double* y, const double* z, int iter,
                             double* vols, lsm_exchange_fn fn, void* user) {
     int st = check_grid(gg); if (st) return st;
-    if (p->hybrid_reinitialisation || p->reinit_scheme < 0 || p->reinit_scheme > 1 ||
-        p->sussman_correction_method != 0)
+    if (p->reinit_scheme < 0 || p->reinit_scheme > 1 || p->sussman_correction_method != 0)
         return LSM_ERR_UNSUPPORTED;
+    const bool hybrid = p->call_reinitialisation && p->hybrid_reinitialisation;
     Grid g(gg);
     Exch ex{fn, user, gg};
     std::vector<int> adv(g.n);
@@ -1132,9 +1685,10 @@ int oracle_levelsetmethod_x(const lsm_grid* gg, const lsm_params* p, const doubl
     if (st) return st;
     if (vols) std::memcpy(vols, v, sizeof(v));
     /* AdvectionNodes = 1 unless (reinit .and. hybrid), levelsetmethod.F90:218-219 */
-    std::fill(adv.begin(), adv.end(), 1);
-    std::vector<double> pc(phin, phin + g.n);
+    if (!hybrid) std::fill(adv.begin(), adv.end(), 1);
+    std::vector<double> pc(g.n, 0.0); /* phicorrected = zero, :147 */
     if (p->call_levelsetmethod) {
+        std::memcpy(pc.data(), phin, sizeof(double) * g.n);
         std::vector<double> ucn(3 * g.n);
         oracle_rhs_contra_j(gg, q, csi, eta, zet, aj, ucn.data());
         for (int it = 0; it < p->numiter_lsm; ++it) {
@@ -1142,8 +1696,26 @@ int oracle_levelsetmethod_x(const lsm_grid* gg, const lsm_params* p, const doubl
             std::memcpy(pc.data(), phi, sizeof(double) * g.n);
         }
     }
+    /* ConvergenceVolume, :245-264 */
+    double conv = v[3];
+    if (p->GlobalMassCorrection) {
+        double w[4];
+        st = oracle_total_water_volume(gg, phi, x, y, z, w, nullptr);
+        if (st) return st;
+        conv = v[3] - (w[0] + w[1]);
+    }
     if (p->call_reinitialisation && p->RNfreq > 0 && iter % p->RNfreq == 0) {
-        if (p->reinit_scheme == 1) oracle_reinitialisation_test2(gg, p, phi, csi, eta, zet, pc.data(), nullptr);
+        if (p->hybrid_reinitialisation) {
+            /* :300-309: +-9.9 off the interface, then the geometric reinitialisation */
+            for (long l = 0; l < g.n; ++l) {
+                if (phi[l] < -kEpsSims) pc[l] = -9.9;
+                if (phi[l] > kEpsSims) pc[l] = 9.9;
+            }
+            std::vector<int> ids(g.n);
+            st = oracle_geometric_reinitialisation(gg, p, phi, x, y, z, conv, pc.data(), ids.data(), nullptr,
+                                                   nullptr);
+            if (st) return st;
+        } else if (p->reinit_scheme == 1) oracle_reinitialisation_test2(gg, p, phi, csi, eta, zet, pc.data(), nullptr);
         else oracle_reinitialization_x(gg, p, phi, csi, eta, zet, pc.data(), fn, user);
         bcond(g, p, pc.data());
         std::memcpy(phi, pc.data(), sizeof(double) * g.n);

@@ -48,7 +48,7 @@ class Params(C.Structure):
                 ("BigPhi", C.c_double), ("epsReinitialisation", C.c_double),
                 ("M_Sphi0", C.c_int), ("reinit_scheme", C.c_int),
                 ("write_global_volume", C.c_int), ("OrderReinitialisationBoundaries", C.c_int),
-                ("ENOBCReinitialisation", C.c_int)]
+                ("ENOBCReinitialisation", C.c_int), ("ConvergenceToleranceGeomReini", C.c_double)]
 
 
 def make_grid(ni, nj, nk, igp=0, jgp=0, kgp=0, physical=(1, 1, 1, 1, 1, 1), dc=1.0, de=1.0, dz=1.0):
@@ -88,6 +88,7 @@ def make_params(**kw):
     p.write_global_volume = 0
     p.OrderReinitialisationBoundaries = 1
     p.ENOBCReinitialisation = 0
+    p.ConvergenceToleranceGeomReini = 1.0e-9
     for k, v in kw.items():
         if k == "btype_lsm":
             for f in range(6):
@@ -137,6 +138,8 @@ class Oracle:
             "oracle_cell_water_volumes": [_GP, _D, _D, _D, _D, _D],
             "oracle_mg_metrics": [_GP, _D, _D, _D, _D, _D, _D, _D],
             "oracle_levelsetmethod": [_GP, _PP, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D, C.c_int, _D],
+            "oracle_geometric_reinitialisation": [_GP, _PP, _D, _D, _D, _D, C.c_double, _D, _I,
+                                                  C.POINTER(C.c_int), C.POINTER(C.c_double)],
         }
         for fn, args in sig.items():
             f = getattr(L, fn)
@@ -250,6 +253,19 @@ class Oracle:
         zet = np.zeros((3,) + sh, order="F"); aj = np.zeros(sh, order="F")
         self._chk(self.lib.oracle_mg_metrics(C.byref(g), x, y, z, csi, eta, zet, aj), "metrics")
         return csi, eta, zet, aj
+
+    def geometric_reinitialisation(self, g, p, phi0, x, y, z, total_water_volume, phicorrected):
+        """geometric_reinitialisation: returns (phicorrected, InterfaceNodesID, info dict)"""
+        pc = np.array(phicorrected, order="F", copy=True)
+        ids = np.zeros(phi0.shape, dtype=np.int32, order="F")
+        ii = (C.c_int * 5)()
+        cc = C.c_double(0.0)
+        self._chk(self.lib.oracle_geometric_reinitialisation(C.byref(g), C.byref(p), phi0, x, y, z,
+                                                             float(total_water_volume), pc, ids, ii, C.byref(cc)),
+                  "geometric_reinitialisation")
+        info = dict(nnodes=ii[0], ntetrahedra=ii[1], nsecond=ii[2], newton_iterations=ii[3],
+                    newton_converged=ii[4], C=cc.value)
+        return pc, ids, info
 
     def levelsetmethod(self, g, p, q, csi, eta, zet, aj, phi, phin, x, y, z, it):
         out = np.array(phi, order="F", copy=True)

@@ -58,5 +58,6 @@ def test_bound_names_are_declared():
 
 def test_struct_layouts_match():
     for c, f in (("lsm_grid", "lsm_grid"), ("lsm_params", "lsm_params"),
-                 ("lsm_batch_instance", "lsm_batch_instance"), ("lsm_batch_config", "lsm_batch_config")):
+                 ("lsm_batch_instance", "lsm_batch_instance"), ("lsm_batch_config", "lsm_batch_config"),
+                 ("lsm_geom_info", "lsm_geom_info")):
         assert [(a.lower(), k, n) for a, k, n in _c_struct(c)] == [(a.lower(), k, n) for a, k, n in _f_type(f)], c

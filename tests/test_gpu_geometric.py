@@ -1,0 +1,139 @@
+"""The geometric reinitialisation (lsm_geometric_reinitialisation) and the
+hybrid level-set step on the GPU against the CPU oracle.
+
+Parity bar:
+ - without GlobalMassCorrection: phicorrected and InterfaceNodesID identical
+   to the oracle's, bit for bit (each node's value is the reference's FP64
+   sequence of operations in the reference's order), and the same list sizes;
+ - with GlobalMassCorrection: the Newton volume sum is a parallel reduction on
+   the GPU (sequential in the oracle; across MPI ranks the reference's own
+   order changes too).  Newton stops once |target - volume| < the deck's
+   tolerance (1e-9), with a finite-difference Jacobian of step ~1.5e-8 |C|,
+   so rounding-level differences in the sums move the converged C by up to
+   ~1e-8 relative: the bar is C within 1e-7 relative, phicorrected within
+   1e-8 normwise relative, the same iteration count, and the K-tetrahedra
+   volume of the GPU's result within the tolerance of the target;
+ - the hybrid lsm_levelsetmethod step: 1e-12 normwise relative, as the other
+   level-set steps.
+"""
+import numpy as np
+import pytest
+
+import cases
+import oracle as O
+from test_gpu_parity import G, P, dev, host
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+EPS = np.finfo(np.float64).eps
+
+
+def seed(phi):
+    return cases.F(np.where(phi < -EPS, -9.9, np.where(phi > EPS, 9.9, phi)))
+
+
+def tilted(n=18):
+    X, Y, Z = np.meshgrid(*(np.linspace(0, 1, n),) * 3, indexing="ij")
+    nv = np.array([0.3, -0.2, 1.0]) / np.linalg.norm([0.3, -0.2, 1.0])
+    phi = cases.F(3.0 * (0.4371 - (nv[0] * (X - 0.5) + nv[1] * (Y - 0.5) + nv[2] * Z)))
+    return O.make_grid(n, n, n), cases.F(X), cases.F(Y), cases.F(Z), phi
+
+
+def _case(kind):
+    if kind == "sphere":
+        g, x, y, z, phi, _ = cases.sphere(22)
+        return g, x, y, z, cases.F(1.6 * phi)
+    if kind == "curvilinear":
+        g, x, y, z, phi, _ = cases.curvilinear(20, 14, 16, seed=3)
+        return g, x, y, z, phi
+    return tilted()
+
+
+@pytest.mark.parametrize("kind", ["sphere", "curvilinear", "tilted"])
+@pytest.mark.parametrize("on_device", [True, False])
+def test_geometric_bit_identical(ls, oracle, kind, on_device):
+    g, x, y, z, phi = _case(kind)
+    p = O.make_params()
+    pc0 = seed(phi)
+    ref, rids, rinfo = oracle.geometric_reinitialisation(g, p, phi, x, y, z, 0.0, pc0)
+    args = [dev(a) if on_device else a for a in (phi, x, y, z, pc0)]
+    out, ids, info = ls.geometric_reinitialisation(G(g), P(p), args[0], args[1], args[2], args[3], 0.0, args[4])
+    if on_device:
+        out, ids = host(out), host(ids)
+    assert np.array_equal(ids, rids)
+    assert np.array_equal(out, ref), float(np.abs(out - ref).max())
+    for k in ("nnodes", "ntetrahedra", "nsecond"):
+        assert info[k] == rinfo[k], k
+    assert info["C"] == 0.0 and info["newton_iterations"] == 0
+
+
+@pytest.mark.parametrize("kind", ["sphere", "curvilinear"])
+def test_geometric_global_mass_correction(ls, oracle, kind):
+    g, x, y, z, phi = _case(kind)
+    v = oracle.total_water_volume(g, phi, x, y, z)
+    p = O.make_params(GlobalMassCorrection=1)
+    pc0 = seed(phi)
+    ref, rids, rinfo = oracle.geometric_reinitialisation(g, p, phi, x, y, z, v[0], pc0)
+    assert rinfo["newton_converged"] == 1
+    out, ids, info = ls.geometric_reinitialisation(G(g), P(p), dev(phi), dev(x), dev(y), dev(z), v[0], dev(pc0))
+    out, ids = host(out), host(ids)
+    assert np.array_equal(ids, rids)
+    assert info["newton_converged"] == 1 and info["newton_iterations"] == rinfo["newton_iterations"]
+    assert abs(info["C"] - rinfo["C"]) <= 1e-7 * abs(rinfo["C"])
+    assert cases.relerr(out, ref) <= 1e-8
+    # the K volume of the corrected phi is the target
+    w = oracle.total_water_volume(g, out, x, y, z)
+    assert abs(w[0] - v[0]) <= 1e-9 * v[0]
+
+
+def test_geometric_unreachable_target_matches(ls, oracle):
+    """ConvergenceVolume as the reference forms it: Newton fails, C = 0 on both."""
+    g, x, y, z, phi = _case("curvilinear")
+    v = oracle.total_water_volume(g, phi, x, y, z)
+    p = O.make_params(GlobalMassCorrection=1)
+    target = v[3] - (v[0] + v[1])
+    ref, _, rinfo = oracle.geometric_reinitialisation(g, p, phi, x, y, z, target, seed(phi))
+    out, _, info = ls.geometric_reinitialisation(G(g), P(p), phi, x, y, z, target, seed(phi))
+    assert info["newton_converged"] == rinfo["newton_converged"]
+    if not rinfo["newton_converged"]:
+        assert info["C"] == 0.0 and np.array_equal(out, ref)
+
+
+def test_hybrid_levelsetmethod_steps(ls, oracle):
+    g, x, y, z, phi, q = cases.curvilinear(20, 14, 22, seed=8)
+    csi, eta, zet, aj = oracle.mg_metrics(g, x, y, z)
+    h = 1.0 / 19
+    p = O.make_params(epslsm=1.5 * h, delti_lsm=0.01, hybrid_reinitialisation=1, RNfreq=2)
+    gg, pp = G(g), P(p)
+    args = [dev(a) for a in (q, csi, eta, zet, aj, x, y, z)]
+    ref = phi
+    cur = dev(phi)
+    for it in range(1, 4):
+        ref, rv = oracle.levelsetmethod(g, p, q, csi, eta, zet, aj, ref, ref, x, y, z, it)
+        v = ls.levelsetmethod(gg, pp, args[0], args[1], args[2], args[3], args[4], cur, cur.clone(), args[5],
+                              args[6], args[7], it)
+        got = host(cur)
+        assert cases.relerr(got, ref) <= 1e-12, (it, cases.relerr(got, ref))
+        assert cases.relerr(v, rv) <= 1e-12
+    assert np.any(np.abs(ref) == 9.9)
+
+
+def test_hybrid_levelsetmethod_with_mass_correction(ls, oracle):
+    g, x, y, z, phi, q = cases.curvilinear(20, 14, 22, seed=9)
+    csi, eta, zet, aj = oracle.mg_metrics(g, x, y, z)
+    h = 1.0 / 19
+    p = O.make_params(epslsm=1.5 * h, delti_lsm=0.01, hybrid_reinitialisation=1, GlobalMassCorrection=1)
+    ref, rv = oracle.levelsetmethod(g, p, q, csi, eta, zet, aj, phi, phi, x, y, z, 1)
+    cur = phi.copy(order="F")
+    v = ls.levelsetmethod(G(g), P(p), q, csi, eta, zet, aj, cur, phi.copy(order="F"), x, y, z, 1)
+    assert cases.relerr(cur, ref) <= 1e-8
+    assert cases.relerr(v, rv) <= 1e-12
+
+
+def test_geometric_rejects_ghost_planes(ls):
+    from nslsm import LsmError
+    g, x, y, z, phi = _case("curvilinear")
+    gg = O.make_grid(20, 14, 16, igp=2, physical=(0, 1, 1, 1, 1, 1))
+    with pytest.raises(LsmError) as e:
+        ls.geometric_reinitialisation(G(gg), P(O.make_params()), phi, x, y, z, 0.0, seed(phi))
+    assert e.value.status == 4

@@ -82,7 +82,12 @@ def test_error_codes(ls):
     gg = Grid(n, n, n)
     m3 = np.zeros((3, n, n, n), order="F")
     with pytest.raises(LsmError) as e:
-        ls.levelsetmethod(gg, LsmParams(hybrid_reinitialisation=True), q, m3, m3, m3, x, phi, phi, x, y, z, 1)
+        ls.levelsetmethod(gg, LsmParams(sussman_correction_method=1), q, m3, m3, m3, x, phi, phi, x, y, z, 1)
+    assert e.value.status == _lib.LSM_ERR_UNSUPPORTED
+    # the hybrid (geometric) branch runs on one subdomain without ghost planes
+    with pytest.raises(LsmError) as e:
+        ls.levelsetmethod(Grid(n, n, n, igp=2, physical=(0, 0, 1, 1, 1, 1)), LsmParams(hybrid_reinitialisation=True),
+                          q, m3, m3, m3, x, phi, phi, x, y, z, 1)
     assert e.value.status == _lib.LSM_ERR_UNSUPPORTED
     with pytest.raises(LsmError) as e:
         ls.bcond_lsm(Grid(3, n, n), LsmParams(), np.zeros((3, n, n), order="F"))
