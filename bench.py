@@ -1,7 +1,7 @@
 """Benchmark of the level-set transport step on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload fwdadj|batched|fp64]
+                    [--workload fwdadj|batched|fp64|sussman|hybrid|adjcheck]
 
 Default workload ("fwdadj"): the large free-surface case, 512 x 256 x 256
 curvilinear nodes (x = 16 xi + 0.05 sin(2 pi eta), y = 4 eta, z = 2 zeta^1.3),
@@ -26,6 +26,8 @@ step, forward only.
 10 reinitialisation pseudo-steps per step, through `lsm_levelsetmethod` in
 the reference's FP64 arithmetic.  "sussman": the same with the
 reference's live reinitialisation (`reinitialisation_test2`, reinit_scheme 1).
+"hybrid": the same with the reference deck's hybrid branch (advection of the
+AdvectionNodes band, geometric reinitialisation).
 
 Metric: Gcell-steps/s = grid nodes x physical steps / second (whole job;
 for "fwdadj" each cell-step is forward + adjoint).
@@ -179,15 +181,23 @@ FP64_METRIC = {
     0: "Gcell-steps/s (plain FP64 level-set step: WENO3-RK3 advection + reinitialisation + volume)",
     1: "Gcell-steps/s (plain FP64 level-set step with the live Sussman reinitialisation: WENO3-RK3 advection + "
        "reinitialisation_test2 + volume)",
+    2: "Gcell-steps/s (plain FP64 level-set step, hybrid branch: WENO3-RK3 advection of the AdvectionNodes band + "
+       "geometric reinitialisation + volume)",
 }
-FP64_REINIT = {0: "reinitialization", 1: "reinitialisation_test2, ENO2 gradients, TVD-RK3 pseudo time"}
+FP64_REINIT = {0: "reinitialization", 1: "reinitialisation_test2, ENO2 gradients, TVD-RK3 pseudo time",
+               2: "geometric_reinitialisation: marching-tetrahedra isosurface, distances of the nodes within 4 of it"}
+FP64_SCHEME = {"fp64": 0, "sussman": 1, "hybrid": 2}
 
 
 def make_case(ni, nj, nk, reinit_iters, scheme=0):
-    """scheme 0: `reinitialization`; 1: the reference's live `reinitialisation_test2`"""
+    """scheme 0: `reinitialization`; 1: the reference's live `reinitialisation_test2`;
+    2: the hybrid branch (geometric reinitialisation, the reference deck's setting)"""
     from nslsm import configs
     case = configs.solitary_wave(ni, nj, nk, reinit_iters=reinit_iters)
-    case.params = case.params.replace(reinit_scheme=scheme)
+    if scheme == 2:
+        case.params = case.params.replace(hybrid_reinitialisation=True)
+    else:
+        case.params = case.params.replace(reinit_scheme=scheme)
     return case
 
 
@@ -224,6 +234,13 @@ def roofline_from_profile(prof, n_nodes, peaks):
     peak = float(peaks.get("hbm_gbs", 6800.0)) if peaks else 6800.0
     traffic = read_traffic(name, n_nodes)
     total = sum(v[1] for v in prof.values())
+    if words is None and name.startswith("k_geo_"):
+        # the geometric reinitialisation's distance loops: FP64 arithmetic on
+        # irregular lists, no HBM roofline (the FP64 pipe is the limit)
+        total = sum(v[1] for v in prof.values())
+        return {"bound": "fp64", "kernel": name, "achieved": None, "peak": None, "unit": None, "frac": None,
+                "traffic": None, "avg_launch_us": avg_s * 1e6, "share": ms / total if total else None,
+                "note": "FP64-issue bound distance loops over the interface lists; see the ncu summary"}
     return {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": None if achieved is None else achieved / peak, "traffic": traffic,
             "algorithmic_bytes_per_launch": None if words is None else words * 8.0 * n_nodes,
@@ -273,6 +290,7 @@ def cpu_oracle_time(case, steps, threads, warmup=0):
     p = O.make_params(epslsm=cp.epslsm, delti_lsm=case.cfl / smax, RNitermax=cp.RNitermax,
                       RNtimestep=cp.RNtimestep, isnarrow=cp.isnarrow, narrowcoef=cp.narrowcoef,
                       reinit_scheme=cp.reinit_scheme, epsReinitialisation=cp.epsReinitialisation,
+                      hybrid_reinitialisation=int(cp.hybrid_reinitialisation),
                       OrderReinitialisationBoundaries=cp.OrderReinitialisationBoundaries,
                       ENOBCReinitialisation=int(cp.ENOBCReinitialisation))
     phi = case.phi0
@@ -799,7 +817,7 @@ def run_fp64(args):
     rank, world = dist_setup(args.gpus)
     dev_index = torch.cuda.current_device()
     W = workload(args)
-    scheme = 1 if args.workload == "sussman" else 0
+    scheme = FP64_SCHEME[args.workload]
     case = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"], scheme)
     case.redistance_iters = W["redistance"]
     n = case.grid.n
@@ -881,12 +899,21 @@ def run_fp64(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        sample = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"], scheme)
         threads = host_threads()
-        sec, used = cpu_oracle_time(sample, 1, threads)
-        cpu = {"value": n / sec / 1e9, "unit": "Gcell-steps/s", "cores": used, "kind": "port",
-               "sample": "1 physical step of the full 256x128x96 workload (FP64 oracle, OpenMP, %d threads, "
-                         "phi0 not redistanced)" % used}
+        if scheme == 2:
+            # the oracle's geometric reinitialisation is serial: an eighth of the grid
+            sg = (W["ni"] // 2, W["nj"] // 2, W["nk"] // 2)
+            sample = make_case(sg[0], sg[1], sg[2], W["reinit_iters"], scheme)
+            sec, used = cpu_oracle_time(sample, 1, threads)
+            cpu = {"value": sample.grid.n / sec / 1e9, "unit": "Gcell-steps/s", "cores": used, "kind": "port",
+                   "sample": "1 physical step of the same case on %dx%dx%d nodes (FP64 oracle; advection on %d "
+                             "OpenMP threads, the geometric reinitialisation serial)" % (sg + (used,))}
+        else:
+            sample = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"], scheme)
+            sec, used = cpu_oracle_time(sample, 1, threads)
+            cpu = {"value": n / sec / 1e9, "unit": "Gcell-steps/s", "cores": used, "kind": "port",
+                   "sample": "1 physical step of the full 256x128x96 workload (FP64 oracle, OpenMP, %d threads, "
+                             "phi0 not redistanced)" % used}
     if rank == 0:
         line = {
             "metric": FP64_METRIC[scheme],
@@ -923,7 +950,10 @@ def run_reference(args):
         print(json.dumps({"impl": "reference", "unavailable": "the reference has no adjoint"}))
         return
     W = workload(args)
-    scheme = 1 if args.workload == "sussman" else 0
+    scheme = FP64_SCHEME[args.workload]
+    if scheme == 2 and not args.grid:
+        # the oracle's geometric reinitialisation is serial: an eighth of the grid
+        W["ni"], W["nj"], W["nk"] = W["ni"] // 2, W["nj"] // 2, W["nk"] // 2
     case = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"], scheme)
     threads = host_threads()
     # warm-up (page-in, thread pool) then timed steps, each a full physical step
@@ -1196,7 +1226,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", default=None, help="NIxNJxNK instead of the workload's grid (profiling runs)")
-    ap.add_argument("--workload", choices=["fwdadj", "batched", "fp64", "sussman", "adjcheck"], default="fwdadj")
+    ap.add_argument("--workload", choices=["fwdadj", "batched", "fp64", "sussman", "hybrid", "adjcheck"],
+                    default="fwdadj")
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--n-inst", type=int, default=None, help="instances of the batched workload (profiling runs)")
     ap.add_argument("--segment", type=int, default=None,

@@ -50,7 +50,7 @@ __device__ __forceinline__ double norm2v(const double* a) {
                 r = 1.0 + r * v * v;
                 scale = ax;
             } else {
-                const double v = ax / scale;
+                const double v = scale == 1.0 ? ax : ax / scale;  // ax / 1 is ax exactly
                 r = r + v * v;
             }
         }
@@ -178,44 +178,49 @@ __device__ void marching_full(const double (&V)[4][3], const double (&ph)[4], MT
     o.wv = water_volume<true>(V, E, fi, err);
 }
 
-// DistancePointLine, src/TetrahedronMethods.F90:1356-1399
-__device__ double dist_point_line(const double* A, const double* B, const double* P) {
-    double AB[3], AP[3], BA[3], BP[3];
-    sub3(B, A, AB); sub3(P, A, AP); sub3(A, B, BA); sub3(P, B, BP);
+// DistancePointLine, src/TetrahedronMethods.F90:1356-1399, given the
+// vectors and norms the caller already has: AP = P - A, BP = P - B,
+// AB = B - A and their norms (BA = A - B is -AB exactly)
+__device__ __forceinline__ double dist_point_line(const double* AP, const double* BP, const double* AB, double nAP,
+                                                  double nBP, double nAB) {
+    const double BA[3] = {-AB[0], -AB[1], -AB[2]};
     bool valid = true;
-    if (norm2v(AB) < kEpsSims) valid = false;
+    if (nAB < kEpsSims) valid = false;
     if (dot3g(AB, AP) < 0.0) valid = false;
     if (dot3g(BA, BP) < 0.0) valid = false;
     if (valid) {
         double c[3];
         cross3g(AP, BP, c);
-        return norm2v(c) / norm2v(AB);
+        return norm2v(c) / nAB;
     }
-    return dmin(norm2v(AP), norm2v(BP));
+    return dmin(nAP, nBP);
 }
 
 // DistancePointTriangle + CheckProjectionPointOnATriangle3,
-// src/TetrahedronMethods.F90:1008-1070,1593-1684.  Kept from the reference:
-// the projected point weights P1 by alpha (the weight of P3 in the standard
-// barycentric form) and P3 by gamma.
+// src/TetrahedronMethods.F90:1008-1070,1593-1684.  Each norm the reference
+// evaluates more than once on the same vector (|P - A| as a vertex distance
+// and inside DistancePointLine, |B - A| twice per edge, |A - B| = |B - A| in
+// the degenerate-triangle test) is evaluated once here: same inputs, same
+// value.  Kept from the reference: the projected point weights P1 by alpha
+// (the weight of P3 in the standard barycentric form) and P3 by gamma.
 __device__ double dist_point_triangle(const double* T, const double* P) {
     const double* A = T;
     const double* B = T + 3;
     const double* Cv = T + 6;
-    double d[3];
-    sub3(P, A, d); double m = norm2v(d);
-    sub3(P, B, d); m = dmin(m, norm2v(d));
-    sub3(P, Cv, d); m = dmin(m, norm2v(d));
-    m = dmin(m, dist_point_line(A, B, P));
-    m = dmin(m, dist_point_line(B, Cv, P));
-    m = dmin(m, dist_point_line(Cv, A, P));
-    sub3(A, B, d); if (norm2v(d) <= kEpsSims) return m;
-    sub3(A, Cv, d); if (norm2v(d) <= kEpsSims) return m;
-    sub3(B, Cv, d); if (norm2v(d) <= kEpsSims) return m;
-    double u[3], v[3], w[3], nv[3], cu[3], cw[3];
-    sub3(B, A, u); sub3(Cv, A, v); sub3(P, A, w);
-    cross3g(u, v, nv);
-    cross3g(u, w, cu); cross3g(w, v, cw);
+    double PA[3], PB[3], PC[3], AB[3], BC[3], CA[3];
+    sub3(P, A, PA); sub3(P, B, PB); sub3(P, Cv, PC);
+    sub3(B, A, AB); sub3(Cv, B, BC); sub3(A, Cv, CA);
+    const double nA = norm2v(PA), nB = norm2v(PB), nC = norm2v(PC);
+    const double nAB = norm2v(AB), nBC = norm2v(BC), nCA = norm2v(CA);
+    double m = dmin(dmin(nA, nB), nC);
+    m = dmin(m, dist_point_line(PA, PB, AB, nA, nB, nAB));
+    m = dmin(m, dist_point_line(PB, PC, BC, nB, nC, nBC));
+    m = dmin(m, dist_point_line(PC, PA, CA, nC, nA, nCA));
+    if (nAB <= kEpsSims || nCA <= kEpsSims || nBC <= kEpsSims) return m;
+    double v[3], nv[3], cu[3], cw[3];
+    sub3(Cv, A, v);
+    cross3g(AB, v, nv);
+    cross3g(AB, PA, cu); cross3g(PA, v, cw);
     const double nn = dot3g(nv, nv);
     const double alpha = dot3g(cu, nv) / nn;
     const double beta = dot3g(cw, nv) / nn;
@@ -334,14 +339,36 @@ __device__ __forceinline__ void for_each_tet(const DevGrid& g, int i, int j, int
 }
 
 // one K tetrahedron: its isosurface triangles (18 doubles), area and water
-// volume of the linear reconstruction, and its four pnode ids (0-based)
+// volume of the linear reconstruction, its four pnode ids (0-based) and a
+// bounding box per triangle (FP32, rounded outwards) used only to skip
+// distance evaluations that cannot change a running minimum
 struct alignas(16) GeoTet {
     double tri[2][9];
+    float box[2][6];  // lo x y z, hi x y z
     double area, wv;
     int nis;
     int v[4];
     int pad;
 };
+
+// A distance evaluation is skipped only when a lower bound of the exact
+// point-triangle distance -- the distance from the point to the triangle's
+// bounding box -- exceeds the running minimum d by a margin.  Every candidate
+// point of DistancePointTriangle (vertices, feet on the edges, the
+// projection step's convex combination of the vertices) lies in the
+// triangle, so the computed distance is at least the exact distance less a
+// few ulps of the coordinates.  The bound is evaluated in FP32 (the FP64
+// units are scarce) on a box rounded outwards: the point and d rounded to
+// FP32 and the FP32 norm keep its error below 1e-6 of the sizes involved,
+// and the margin is 1e-5 of them.  A skipped triangle therefore leaves
+// d + exsign (da - d) = d exactly as the full evaluation would.
+__device__ __forceinline__ bool beyond_box(const float* p, float pscale, const float* lo, const float* hi, float d) {
+    const float dx = fmaxf(fmaxf(lo[0] - p[0], p[0] - hi[0]), 0.0f);
+    const float dy = fmaxf(fmaxf(lo[1] - p[1], p[1] - hi[1]), 0.0f);
+    const float dz = fmaxf(fmaxf(lo[2] - p[2], p[2] - hi[2]), 0.0f);
+    const float lb = sqrtf(dx * dx + dy * dy + dz * dz);
+    return lb > d + 1.0e-5f * (lb + d + pscale);
+}
 
 // -------------------------------------------------------------- kernels
 
@@ -401,6 +428,7 @@ __device__ int block_exclusive_scan(int v, int* total) {
 template <int MODE>
 __device__ __forceinline__ int scan_count(const void* src, long long l) {
     if (MODE == 0) return static_cast<const int*>(src)[l] ? 1 : 0;
+    if (MODE == 2) return static_cast<const int*>(src)[l] < 0 ? 1 : 0;
     return __popc(static_cast<const unsigned char*>(src)[l]);
 }
 
@@ -433,7 +461,8 @@ __global__ void __launch_bounds__(kThreads) k_scan_top(int ntiles, int* __restri
 }
 
 // mode 0: ids[l] = pnode id + 1 (0: not a pnode), node_of[id] = l;
-// mode 1: tetbase[l] = first K-tetrahedron id of cell l
+// mode 1: tetbase[l] = first K-tetrahedron id of cell l;
+// mode 2: node_of[c] = the c-th node tagged -1
 template <int MODE>
 __global__ void __launch_bounds__(kThreads) k_scan_apply(long long n, const void* __restrict__ src,
                                                          const int* __restrict__ tile_off, int* __restrict__ out,
@@ -453,8 +482,10 @@ __global__ void __launch_bounds__(kThreads) k_scan_apply(long long n, const void
         if (MODE == 0) {
             out[base + q] = c[q] ? off + 1 : 0;
             if (c[q]) node_of[off] = base + q;
-        } else {
+        } else if (MODE == 1) {
             out[base + q] = off;
+        } else if (c[q]) {
+            node_of[off] = base + q;
         }
         off += c[q];
     }
@@ -493,9 +524,16 @@ __global__ void k_geo_tets(DevGrid g, const double* __restrict__ phi, const doub
             T.wv = o.wv;
             T.pad = 0;
 #pragma unroll
-            for (int q = 0; q < 2; ++q)
+            for (int q = 0; q < 2; ++q) {
 #pragma unroll
                 for (int c = 0; c < 9; ++c) T.tri[q][c] = q < T.nis ? o.tri[q][c / 3][c % 3] : 0.0;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const double a = T.tri[q][c], b = T.tri[q][3 + c], e = T.tri[q][6 + c];
+                    T.box[q][c] = __double2float_rd(fmin(a, fmin(b, e)));
+                    T.box[q][3 + c] = __double2float_ru(fmax(a, fmax(b, e)));
+                }
+            }
             tets[tid++] = T;
         }
     }
@@ -517,40 +555,103 @@ __global__ void k_geo_mark(DevGrid g, int npn, const long long* __restrict__ nod
     }
 }
 
-// the triangles of tetrahedron t against point P (running minimum d)
-__device__ __forceinline__ double tet_min(const GeoTet* __restrict__ tets, int t, const double* P, double d) {
+// a point in both precisions (the FP32 copy for the culling bounds)
+struct Pt {
+    double d[3];
+    float f[3];
+    float scale;
+};
+__device__ __forceinline__ Pt make_pt(double a, double b, double c) {
+    Pt p;
+    p.d[0] = a; p.d[1] = b; p.d[2] = c;
+    p.f[0] = (float)a; p.f[1] = (float)b; p.f[2] = (float)c;
+    p.scale = fmaxf(fabsf(p.f[0]), fmaxf(fabsf(p.f[1]), fabsf(p.f[2])));
+    return p;
+}
+
+// the triangles of tetrahedron t against point P (running minimum d); a
+// triangle whose bounding box lies beyond d is not evaluated
+__device__ __forceinline__ double tet_min(const GeoTet* __restrict__ tets, int t, const Pt& P, double d) {
     const GeoTet& T = tets[t];
     const int nis = T.nis;
     if (nis > 0 && T.area > 0.0) {
-        d = run_min(d, dist_point_triangle(T.tri[0], P));
-        if (nis > 1) d = run_min(d, dist_point_triangle(T.tri[1], P));
+        for (int q = 0; q < nis; ++q) {
+            if (beyond_box(P.f, P.scale, T.box[q], T.box[q] + 3, (float)d)) continue;
+            d = run_min(d, dist_point_triangle(T.tri[q], P.d));
+        }
     }
     return d;
+}
+
+// per pnode: the bounding box of every triangle of its K tetrahedra
+// (lo.w = 0: none of them has a triangle)
+__global__ void k_geo_prad(DevGrid g, int npn, const long long* __restrict__ node_of,
+                           const unsigned char* __restrict__ cellbits, const int* __restrict__ tetbase,
+                           const GeoTet* __restrict__ tets, const double* __restrict__ x,
+                           const double* __restrict__ y, const double* __restrict__ z, float4* __restrict__ pbox) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npn; p += gridDim.x * blockDim.x) {
+        int i, j, k;
+        node_ijk(g, node_of[p], &i, &j, &k);
+        float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+        float any = 0.0f;
+        for_each_tet(g, i, j, k, cellbits, tetbase, [&](int t) {
+            const GeoTet& T = tets[t];
+            if (T.nis > 0 && T.area > 0.0)
+                for (int q = 0; q < T.nis; ++q) {
+                    any = 1.0f;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        lo[c] = fminf(lo[c], T.box[q][c]);
+                        hi[c] = fmaxf(hi[c], T.box[q][3 + c]);
+                    }
+                }
+        });
+        pbox[2 * p] = make_float4(lo[0], lo[1], lo[2], any);
+        pbox[2 * p + 1] = make_float4(hi[0], hi[1], hi[2], 0.0f);
+    }
+}
+
+// true when pnode m's triangles all lie beyond d from P
+__device__ __forceinline__ bool pnode_beyond(int m, const Pt& P, double d, const float4* __restrict__ pbox) {
+    const float4 a = pbox[2 * m], b = pbox[2 * m + 1];
+    if (a.w == 0.0f) return true;
+    const float lo[3] = {a.x, a.y, a.z}, hi[3] = {b.x, b.y, b.z};
+    return beyond_box(P.f, P.scale, lo, hi, (float)d);
 }
 
 // the pnodes' signed distances (src/GetIsosurfaceAndDistances.F90:166-330)
 __global__ void k_geo_sd(DevGrid g, int npn, const long long* __restrict__ node_of, const int* __restrict__ ids,
                          const unsigned char* __restrict__ cellbits, const int* __restrict__ tetbase,
-                         const GeoTet* __restrict__ tets, const double* __restrict__ phi,
-                         const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z,
-                         double* __restrict__ sd_out) {
+                         const GeoTet* __restrict__ tets, const float4* __restrict__ prad,
+                         const double* __restrict__ phi, const double* __restrict__ x,
+                         const double* __restrict__ y, const double* __restrict__ z, double* __restrict__ sd_out) {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npn; p += gridDim.x * blockDim.x) {
         const long long l0 = node_of[p];
         int i, j, k;
         node_ijk(g, l0, &i, &j, &k);
-        const double P[3] = {x[l0], y[l0], z[l0]};
+        const Pt P = make_pt(x[l0], y[l0], z[l0]);
         const double s = sgn1(phi[l0]);
         double dp = 10.0, sd = 99.9;
+        auto sd_step = [&]() {
+            const double asd = fabs(sd);
+            const double ex2 = (sgn1(asd - dp) + 1.0) / 2.0;
+            sd = asd + ex2 * (dp - asd);
+            sd = s * sd;
+        };
         for (int ks = max(k - 4, 0); ks <= min(k + 4, g.nk - 1); ++ks)
             for (int js = max(j - 4, 0); js <= min(j + 4, g.nj - 1); ++js)
                 for (int is = max(i - 4, 0); is <= min(i + 4, g.ni - 1); ++is) {
-                    if (ids[gid(g, is, js, ks)] <= 0) continue;
+                    const int m = ids[gid(g, is, js, ks)] - 1;
+                    if (m < 0) continue;
+                    // every triangle of this pnode beyond dp: dp stays, the
+                    // signed distance update still runs once per tetrahedron
+                    if (pnode_beyond(m, P, dp, prad)) {
+                        for_each_tet(g, is, js, ks, cellbits, tetbase, [&](int) { sd_step(); });
+                        continue;
+                    }
                     for_each_tet(g, is, js, ks, cellbits, tetbase, [&](int t) {
                         dp = tet_min(tets, t, P, dp);
-                        const double asd = fabs(sd);
-                        const double ex2 = (sgn1(asd - dp) + 1.0) / 2.0;
-                        sd = asd + ex2 * (dp - asd);
-                        sd = s * sd;
+                        sd_step();
                     });
                 }
         sd_out[p] = sd;
@@ -693,26 +794,37 @@ __global__ void k_geo_pnode_phi(int npn, const long long* __restrict__ node_of, 
 }
 
 // NeighboursPhiCorrection on the -1 nodes (src/NeighboursPhiCorrection.F90:186-343)
-__global__ void k_geo_neigh(DevGrid g, const int* __restrict__ tag, const int* __restrict__ ids,
+__global__ void k_geo_neigh(DevGrid g, const int* __restrict__ ids,
                             const unsigned char* __restrict__ cellbits, const int* __restrict__ tetbase,
-                            const GeoTet* __restrict__ tets, const double* __restrict__ x,
+                            const GeoTet* __restrict__ tets, const long long* __restrict__ node_of,
+                            const float4* __restrict__ prad, const double* __restrict__ x,
                             const double* __restrict__ y, const double* __restrict__ z, double* __restrict__ pc,
-                            int* __restrict__ count) {
-    const long long n = (long long)g.ni * g.nj * g.nk;
-    for (long long l0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; l0 < n;
-         l0 += (long long)gridDim.x * blockDim.x) {
-        const bool mine = tag[l0] < 0;
-        const unsigned bal = __ballot_sync(__activemask(), mine);
-        if ((threadIdx.x & 31) == __ffs(bal) - 1) atomicAdd(count, __popc(bal));
-        if (!mine) continue;
+                            int nsec, const long long* __restrict__ second) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nsec; c += gridDim.x * blockDim.x) {
+        const long long l0 = second[c];
         int i, j, k;
         node_ijk(g, l0, &i, &j, &k);
-        const double P[3] = {x[l0], y[l0], z[l0]};
+        const Pt P = make_pt(x[l0], y[l0], z[l0]);
         double v = pc[l0];
         for (int ks = max(k - 4, 0); ks <= min(k + 4, g.nk - 1); ++ks)
             for (int js = max(j - 4, 0); js <= min(j + 4, g.nj - 1); ++js)
                 for (int is = max(i - 4, 0); is <= min(i + 4, g.ni - 1); ++is) {
-                    if (ids[gid(g, is, js, ks)] <= 0) continue;
+                    const int m = ids[gid(g, is, js, ks)] - 1;
+                    if (m < 0) continue;
+                    // every triangle of this pnode beyond |v|: each of its
+                    // running minima stays above |v|, so v cannot change
+                    // (first the box of all its triangles, then the
+                    // triangles' own boxes)
+                    const double av0 = fabs(v);
+                    if (pnode_beyond(m, P, av0, prad)) continue;
+                    const float avf = (float)av0;
+                    bool near = false;
+                    for_each_tet(g, is, js, ks, cellbits, tetbase, [&](int t) {
+                        const GeoTet& T = tets[t];
+                        if (near || !(T.nis > 0 && T.area > 0.0)) return;
+                        for (int q = 0; q < T.nis; ++q) near |= !beyond_box(P.f, P.scale, T.box[q], T.box[q] + 3, avf);
+                    });
+                    if (!near) continue;
                     double dp = 10.0;
                     for_each_tet(g, is, js, ks, cellbits, tetbase, [&](int t) {
                         dp = tet_min(tets, t, P, dp);
@@ -738,8 +850,8 @@ __global__ void k_geo_seed(long long n, const double* __restrict__ phi, double* 
     }
 }
 
-int grid_for(long long n) {
-    long long b = (n + kThreads - 1) / kThreads;
+int grid_for(long long n, int bs = kThreads) {
+    long long b = (n + bs - 1) / bs;
     return (int)(b < 1 ? 1 : (b > 152LL * 64 ? 152LL * 64 : b));
 }
 
@@ -820,6 +932,8 @@ cudaError_t geo_reinit(const DevGrid& g, const double* phi0, const double* x, co
     GEO_CU(e);
     auto* xi = static_cast<double*>(alloc(actx, "geo_xi", 8 * (size_t)npn, &e));
     GEO_CU(e);
+    auto* prad = static_cast<float4*>(alloc(actx, "geo_prad", 32 * (size_t)npn, &e));
+    GEO_CU(e);
     {
         ProfScope ps("k_geo_tets", s);
         k_geo_tets<<<grid_for(n), kThreads, 0, s>>>(g, phi0, x, y, z, cellbits, tetbase, ids, tets, d_err);
@@ -831,8 +945,14 @@ cudaError_t geo_reinit(const DevGrid& g, const double* phi0, const double* x, co
         GEO_CU(cudaGetLastError());
     }
     {
+        ProfScope ps("k_geo_prad", s);
+        k_geo_prad<<<grid_for(npn), kThreads, 0, s>>>(g, npn, node_of, cellbits, tetbase, tets, x, y, z, prad);
+        GEO_CU(cudaGetLastError());
+    }
+    {
         ProfScope ps("k_geo_sd", s);
-        k_geo_sd<<<grid_for(npn), 128, 0, s>>>(g, npn, node_of, ids, cellbits, tetbase, tets, phi0, x, y, z, sd);
+        k_geo_sd<<<grid_for(npn), 128, 0, s>>>(g, npn, node_of, ids, cellbits, tetbase, tets, prad, phi0, x, y, z,
+                                               sd);
         GEO_CU(cudaGetLastError());
     }
     GEO_CU(cudaMemsetAsync(xi, 0, 8 * (size_t)npn, s));
@@ -881,16 +1001,32 @@ cudaError_t geo_reinit(const DevGrid& g, const double* phi0, const double* x, co
         k_geo_pnode_phi<<<grid_for(npn), kThreads, 0, s>>>(npn, node_of, sd, xi, C, pc);
         GEO_CU(cudaGetLastError());
     }
-    GEO_CU(cudaMemsetAsync(d_count + 2, 0, sizeof(int), s));
+    // the nodes tagged -1, listed in order
     {
-        ProfScope ps("k_geo_neigh", s);
-        k_geo_neigh<<<grid_for(n), 128, 0, s>>>(g, tag, ids, cellbits, tetbase, tets, x, y, z, pc, d_count + 2);
+        ProfScope ps("k_geo_scan", s);
+        k_scan_tiles<2><<<ntiles, kThreads, 0, s>>>(n, tag, tiles);
+        k_scan_top<<<1, kThreads, 0, s>>>(ntiles, tiles, d_count + 2);
         GEO_CU(cudaGetLastError());
     }
     int ns = 0;
     GEO_CU(cudaMemcpyAsync(&ns, d_count + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
     GEO_CU(cudaStreamSynchronize(s));
     info->nsecond = ns;
+    if (ns == 0) return cudaSuccess;
+    auto* second = static_cast<long long*>(alloc(actx, "geo_second", 8 * (size_t)ns, &e));
+    GEO_CU(e);
+    {
+        ProfScope ps("k_geo_scan", s);
+        k_scan_apply<2><<<ntiles, kThreads, 0, s>>>(n, tag, tiles, nullptr, second);
+        GEO_CU(cudaGetLastError());
+    }
+    {
+        ProfScope ps("k_geo_neigh", s);
+        k_geo_neigh<<<grid_for(ns, 128), 128, 0, s>>>(g, ids, cellbits, tetbase, tets, node_of, prad, x, y, z, pc, ns,
+                                                 second);
+        GEO_CU(cudaGetLastError());
+    }
+    GEO_CU(cudaStreamSynchronize(s));
     return cudaSuccess;
 }
 
