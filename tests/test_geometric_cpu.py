@@ -156,3 +156,64 @@ def test_geometric_rejects_subdomains(oracle, bad):
         g.jgp = 2
     with pytest.raises(RuntimeError):
         oracle.geometric_reinitialisation(g, O.make_params(), phi, x, y, z, 0.0, seed(phi))
+
+
+def _zero_plane(n=13):
+    """phi exactly 0 on the node plane z = 0.5 (n odd): tetrahedra with three
+    zero vertices (a face on the surface) and with one or two"""
+    X, Y, Z = np.meshgrid(*(np.linspace(0, 1, n),) * 3, indexing="ij")
+    k = np.arange(n)[None, None, :] - (n - 1) // 2
+    phi = cases.F(-2.0 * k / (n - 1) + 0.0 * X)
+    return O.make_grid(n, n, n), cases.F(X), cases.F(Y), cases.F(Z), phi
+
+
+def _zero_slab(n=13):
+    """phi exactly 0 on three node planes: tetrahedra with four zero vertices"""
+    g, x, y, z, phi = _zero_plane(n)
+    k = np.arange(n)[None, None, :] - (n - 1) // 2
+    phi = cases.F(np.where(np.abs(k) <= 1, 0.0, phi) + 0.0 * x)
+    return g, x, y, z, phi
+
+
+def test_zero_plane_is_exact(oracle):
+    g, x, y, z, phi = _zero_plane()
+    out, ids, info = oracle.geometric_reinitialisation(g, O.make_params(), phi, x, y, z, 0.0, seed(phi))
+    sd = 0.5 - z
+    m = ids != 0
+    # the surface is the node plane itself: its faces are the triangles
+    assert info["ntetrahedra"] > 0
+    assert np.abs(np.abs(out[m]) - np.abs(sd[m])).max() <= 1e-13
+    assert np.all(out[(ids > 0) & (phi == 0.0)] == 0.0)
+
+
+def test_zero_slab_runs(oracle):
+    g, x, y, z, phi = _zero_slab()
+    out, ids, info = oracle.geometric_reinitialisation(g, O.make_params(), phi, x, y, z, 0.0, seed(phi))
+    assert np.isfinite(out).all() and info["nnodes"] > 0
+    # nodes of the slab are pnodes; the nearest triangles are the faces of
+    # the tetrahedra that touch the slab's outer planes
+    assert np.all(ids[phi == 0.0] > 0)
+
+
+def _near_zero(n=13):
+    """the zero plane with its nodes perturbed to +-1e-17 (below epsilon),
+    +-1e-310 (below tiny), +0.0 and -0.0, in a seeded pattern"""
+    g, x, y, z, phi = _zero_plane(n)
+    rng = np.random.default_rng(12)
+    vals = np.array([1e-17, -1e-17, 1e-310, -1e-310, 0.0, -0.0])
+    kz = (n - 1) // 2
+    phi[:, :, kz] = vals[rng.integers(0, len(vals), size=(n, n))]
+    return g, x, y, z, phi
+
+
+def test_near_zero_values_run(oracle):
+    g, x, y, z, phi = _near_zero()
+    out, ids, info = oracle.geometric_reinitialisation(g, O.make_params(), phi, x, y, z, 0.0, seed(phi))
+    assert np.isfinite(out).all() and info["ntetrahedra"] > 0
+    kz = (phi.shape[2] - 1) // 2
+    assert np.all(ids[:, :, kz] > 0)
+    # every triangle lies on the plane to ~1e-17: no distance falls below the
+    # plane's (vertices and edges on the zero level give no triangle in the
+    # reference, so some distances come from farther triangles)
+    m = ids != 0
+    assert (np.abs(out[m]) - np.abs(0.5 - z[m])).min() >= -1e-12

@@ -40,6 +40,12 @@ def tilted(n=18):
 
 
 def _case(kind):
+    if kind in ("zero_plane", "zero_slab", "near_zero"):
+        # phi exactly 0 on node planes (the vertex / edge / face / whole-
+        # tetrahedron zero cases of MarchingTetrahedron), or a plane of
+        # +-1e-17, +-1e-310 and signed zeros
+        import test_geometric_cpu as T
+        return {"zero_plane": T._zero_plane, "zero_slab": T._zero_slab, "near_zero": T._near_zero}[kind](15)
     if kind == "sphere":
         g, x, y, z, phi, _ = cases.sphere(22)
         return g, x, y, z, cases.F(1.6 * phi)
@@ -49,7 +55,7 @@ def _case(kind):
     return tilted()
 
 
-@pytest.mark.parametrize("kind", ["sphere", "curvilinear", "tilted"])
+@pytest.mark.parametrize("kind", ["sphere", "curvilinear", "tilted", "zero_plane", "zero_slab", "near_zero"])
 @pytest.mark.parametrize("on_device", [True, False])
 def test_geometric_bit_identical(ls, oracle, kind, on_device):
     g, x, y, z, phi = _case(kind)
