@@ -37,25 +37,42 @@ constexpr int kTile = 4 * kThreads;  // elements per scan tile
 
 // ------------------------------------------------------------- geometry
 
+// Comparisons on the integer pipe: for non-negative doubles (+0 included)
+// the IEEE order is the order of the bit patterns as signed integers, and
+// x < 0 holds exactly when the sign bit is set and x is not -0.  GB300's
+// FP64 pipe is its scarce resource; these are exact (no NaN reaches them).
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ bool nn_lt(double a, double b) { return dbits(a) < dbits(b); }   // a, b >= +0
+__device__ __forceinline__ bool nn_le(double a, double b) { return dbits(a) <= dbits(b); }  // a, b >= +0
+__device__ __forceinline__ bool neg(double x) {
+    const long long b = dbits(x);
+    return b < 0 && b != (long long)0x8000000000000000ULL;
+}
+__device__ __forceinline__ bool pos(double x) { return dbits(x) > 0; }  // x > 0
+constexpr long long kOneBits = 0x3FF0000000000000LL;                    // 1.0
+__device__ __forceinline__ bool lt1(double x) { return dbits(x) < kOneBits; }  // x < 1
+
 // NORM2 of a 3-vector as gfortran expands the intrinsic: a scaled sum of
-// squares, zeros skipped, sqrt(sum) * scale
+// squares, zeros skipped, sqrt(sum) * scale.  While the scale is exactly 1
+// the divisions ax / 1 and the final * 1 are skipped (both are exact).
 __device__ __forceinline__ double norm2v(const double* a) {
     double scale = 1.0, r = 0.0;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        if (a[c] != 0.0) {
-            const double ax = fabs(a[c]);
-            if (scale < ax) {
+        const long long b = dbits(a[c]) & 0x7FFFFFFFFFFFFFFFLL;  // |a[c]|
+        if (b != 0) {
+            const double ax = __longlong_as_double(b);
+            if (dbits(scale) < b) {
                 const double v = scale / ax;
                 r = 1.0 + r * v * v;
                 scale = ax;
             } else {
-                const double v = scale == 1.0 ? ax : ax / scale;  // ax / 1 is ax exactly
+                const double v = dbits(scale) == kOneBits ? ax : ax / scale;
                 r = r + v * v;
             }
         }
     }
-    return sqrt(r) * scale;
+    return dbits(scale) == kOneBits ? sqrt(r) : sqrt(r) * scale;
 }
 __device__ __forceinline__ void sub3(const double* a, const double* b, double* c) {
     c[0] = a[0] - b[0]; c[1] = a[1] - b[1]; c[2] = a[2] - b[2];
@@ -72,7 +89,7 @@ __device__ __forceinline__ void cross3g(const double* a, const double* b, double
     c[1] = a[2] * b[0] - a[0] * b[2];
     c[2] = a[0] * b[1] - a[1] * b[0];
 }
-__device__ __forceinline__ double dmin(double a, double b) { return b < a ? b : a; }
+__device__ __forceinline__ double dmin(double a, double b) { return nn_lt(b, a) ? b : a; }  // a, b >= +0
 __device__ __forceinline__ double sgn1(double x) { return copysign(1.0, x); }  // sign(one, x)
 
 // GetTriangleArea, src/TetrahedronMethods.F90:691-707
@@ -185,9 +202,9 @@ __device__ __forceinline__ double dist_point_line(const double* AP, const double
                                                   double nBP, double nAB) {
     const double BA[3] = {-AB[0], -AB[1], -AB[2]};
     bool valid = true;
-    if (nAB < kEpsSims) valid = false;
-    if (dot3g(AB, AP) < 0.0) valid = false;
-    if (dot3g(BA, BP) < 0.0) valid = false;
+    if (nn_lt(nAB, kEpsSims)) valid = false;
+    if (neg(dot3g(AB, AP))) valid = false;
+    if (neg(dot3g(BA, BP))) valid = false;
     if (valid) {
         double c[3];
         cross3g(AP, BP, c);
@@ -216,7 +233,7 @@ __device__ double dist_point_triangle(const double* T, const double* P) {
     m = dmin(m, dist_point_line(PA, PB, AB, nA, nB, nAB));
     m = dmin(m, dist_point_line(PB, PC, BC, nB, nC, nBC));
     m = dmin(m, dist_point_line(PC, PA, CA, nC, nA, nCA));
-    if (nAB <= kEpsSims || nCA <= kEpsSims || nBC <= kEpsSims) return m;
+    if (nn_le(nAB, kEpsSims) || nn_le(nCA, kEpsSims) || nn_le(nBC, kEpsSims)) return m;
     double v[3], nv[3], cu[3], cw[3];
     sub3(Cv, A, v);
     cross3g(AB, v, nv);
@@ -225,7 +242,7 @@ __device__ double dist_point_triangle(const double* T, const double* P) {
     const double alpha = dot3g(cu, nv) / nn;
     const double beta = dot3g(cw, nv) / nn;
     const double gamma = 1.0 - beta - alpha;
-    if (alpha > 0.0 && alpha < 1.0 && beta > 0.0 && beta < 1.0 && gamma > 0.0 && gamma < 1.0) {
+    if (pos(alpha) && lt1(alpha) && pos(beta) && lt1(beta) && pos(gamma) && lt1(gamma)) {
         double pp[3], dd[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) pp[c] = alpha * A[c] + beta * B[c] + gamma * Cv[c];
@@ -235,10 +252,17 @@ __device__ double dist_point_triangle(const double* T, const double* P) {
     return m;
 }
 
-// the reference's running minimum d + exsign (da - d), exsign = 1 when da <= d
+// the reference's running minimum d + exsign (da - d), exsign = (sign(1,
+// d - da) + 1) / 2: 1 when da <= d (d - da >= +0), and then d + (da - d);
+// 0 otherwise, and then d + 0 = d.  d, da >= +0.
 __device__ __forceinline__ double run_min(double d, double da) {
-    const double ex = (sgn1(d - da) + 1.0) / 2.0;
-    return d + ex * (da - d);
+    return nn_le(da, d) ? d + (da - d) : d;
+}
+
+// the reference's signed update of a running |value| by a distance dp
+// (exsign2 = 1 when |value| >= dp): the new magnitude
+__device__ __forceinline__ double mag_step(double a, double dp) {
+    return nn_le(dp, a) ? a + (dp - a) : a;
 }
 
 // ------------------------------------------------------------ the lists
@@ -633,10 +657,8 @@ __global__ void k_geo_sd(DevGrid g, int npn, const long long* __restrict__ node_
         const double s = sgn1(phi[l0]);
         double dp = 10.0, sd = 99.9;
         auto sd_step = [&]() {
-            const double asd = fabs(sd);
-            const double ex2 = (sgn1(asd - dp) + 1.0) / 2.0;
-            sd = asd + ex2 * (dp - asd);
-            sd = s * sd;
+            // sd = |sd| + exsign2 (dp - |sd|), then sign(one, phi) * sd
+            sd = copysign(mag_step(fabs(sd), dp), s);
         };
         for (int ks = max(k - 4, 0); ks <= min(k + 4, g.nk - 1); ++ks)
             for (int js = max(j - 4, 0); js <= min(j + 4, g.nj - 1); ++js)
@@ -828,10 +850,8 @@ __global__ void k_geo_neigh(DevGrid g, const int* __restrict__ ids,
                     double dp = 10.0;
                     for_each_tet(g, is, js, ks, cellbits, tetbase, [&](int t) {
                         dp = tet_min(tets, t, P, dp);
-                        const double av = fabs(v);
-                        const double ex2 = (sgn1(av - dp) + 1.0) / 2.0;
-                        const double aux = av + ex2 * (dp - av);
-                        v = sgn1(v) * aux;
+                        // |v| + exsign2 (dp - |v|), with the sign of v
+                        v = copysign(mag_step(fabs(v), dp), v);
                     });
                 }
         pc[l0] = v;
