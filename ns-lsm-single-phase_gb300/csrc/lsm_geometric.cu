@@ -213,34 +213,52 @@ __device__ __forceinline__ double dist_point_line(const double* AP, const double
     return dmin(nAP, nBP);
 }
 
+// What DistancePointTriangle computes from the triangle alone, evaluated
+// once per triangle with the same operations: the edge vectors
+// AB = B - A, BC = C - B, CA = A - C, their norms, and the projection
+// step's normal nv = AB x (C - A) (C - A is -CA exactly) with nv . nv.
+struct TriGeo {
+    double AB[3], BC[3], CA[3];
+    double nAB, nBC, nCA;
+    double nv[3], nn;
+};
+
+__device__ void tri_geo(const double* T, TriGeo& g) {
+    const double* A = T;
+    const double* B = T + 3;
+    const double* Cv = T + 6;
+    sub3(B, A, g.AB); sub3(Cv, B, g.BC); sub3(A, Cv, g.CA);
+    g.nAB = norm2v(g.AB); g.nBC = norm2v(g.BC); g.nCA = norm2v(g.CA);
+    const double v[3] = {-g.CA[0], -g.CA[1], -g.CA[2]};
+    cross3g(g.AB, v, g.nv);
+    g.nn = dot3g(g.nv, g.nv);
+}
+
 // DistancePointTriangle + CheckProjectionPointOnATriangle3,
 // src/TetrahedronMethods.F90:1008-1070,1593-1684.  Each norm the reference
 // evaluates more than once on the same vector (|P - A| as a vertex distance
 // and inside DistancePointLine, |B - A| twice per edge, |A - B| = |B - A| in
-// the degenerate-triangle test) is evaluated once here: same inputs, same
-// value.  Kept from the reference: the projected point weights P1 by alpha
-// (the weight of P3 in the standard barycentric form) and P3 by gamma.
-__device__ double dist_point_triangle(const double* T, const double* P) {
+// the degenerate-triangle test) is evaluated once here, and the parts that
+// depend on the triangle alone come from TriGeo: same inputs, same value.
+// Kept from the reference: the projected point weights P1 by alpha (the
+// weight of P3 in the standard barycentric form) and P3 by gamma.
+__device__ double dist_point_triangle(const double* T, const TriGeo& g, const double* P) {
     const double* A = T;
     const double* B = T + 3;
     const double* Cv = T + 6;
-    double PA[3], PB[3], PC[3], AB[3], BC[3], CA[3];
+    double PA[3], PB[3], PC[3];
     sub3(P, A, PA); sub3(P, B, PB); sub3(P, Cv, PC);
-    sub3(B, A, AB); sub3(Cv, B, BC); sub3(A, Cv, CA);
     const double nA = norm2v(PA), nB = norm2v(PB), nC = norm2v(PC);
-    const double nAB = norm2v(AB), nBC = norm2v(BC), nCA = norm2v(CA);
     double m = dmin(dmin(nA, nB), nC);
-    m = dmin(m, dist_point_line(PA, PB, AB, nA, nB, nAB));
-    m = dmin(m, dist_point_line(PB, PC, BC, nB, nC, nBC));
-    m = dmin(m, dist_point_line(PC, PA, CA, nC, nA, nCA));
-    if (nn_le(nAB, kEpsSims) || nn_le(nCA, kEpsSims) || nn_le(nBC, kEpsSims)) return m;
-    double v[3], nv[3], cu[3], cw[3];
-    sub3(Cv, A, v);
-    cross3g(AB, v, nv);
-    cross3g(AB, PA, cu); cross3g(PA, v, cw);
-    const double nn = dot3g(nv, nv);
-    const double alpha = dot3g(cu, nv) / nn;
-    const double beta = dot3g(cw, nv) / nn;
+    m = dmin(m, dist_point_line(PA, PB, g.AB, nA, nB, g.nAB));
+    m = dmin(m, dist_point_line(PB, PC, g.BC, nB, nC, g.nBC));
+    m = dmin(m, dist_point_line(PC, PA, g.CA, nC, nA, g.nCA));
+    if (nn_le(g.nAB, kEpsSims) || nn_le(g.nCA, kEpsSims) || nn_le(g.nBC, kEpsSims)) return m;
+    const double v[3] = {-g.CA[0], -g.CA[1], -g.CA[2]};
+    double cu[3], cw[3];
+    cross3g(g.AB, PA, cu); cross3g(PA, v, cw);
+    const double alpha = dot3g(cu, g.nv) / g.nn;
+    const double beta = dot3g(cw, g.nv) / g.nn;
     const double gamma = 1.0 - beta - alpha;
     if (pos(alpha) && lt1(alpha) && pos(beta) && lt1(beta) && pos(gamma) && lt1(gamma)) {
         double pp[3], dd[3];
@@ -368,6 +386,7 @@ __device__ __forceinline__ void for_each_tet(const DevGrid& g, int i, int j, int
 // distance evaluations that cannot change a running minimum
 struct alignas(16) GeoTet {
     double tri[2][9];
+    TriGeo tg[2];
     float box[2][6];  // lo x y z, hi x y z
     double area, wv;
     int nis;
@@ -551,6 +570,7 @@ __global__ void k_geo_tets(DevGrid g, const double* __restrict__ phi, const doub
             for (int q = 0; q < 2; ++q) {
 #pragma unroll
                 for (int c = 0; c < 9; ++c) T.tri[q][c] = q < T.nis ? o.tri[q][c / 3][c % 3] : 0.0;
+                tri_geo(T.tri[q], T.tg[q]);
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     const double a = T.tri[q][c], b = T.tri[q][3 + c], e = T.tri[q][6 + c];
@@ -601,7 +621,7 @@ __device__ __forceinline__ double tet_min(const GeoTet* __restrict__ tets, int t
     if (nis > 0 && T.area > 0.0) {
         for (int q = 0; q < nis; ++q) {
             if (beyond_box(P.f, P.scale, T.box[q], T.box[q] + 3, (float)d)) continue;
-            d = run_min(d, dist_point_triangle(T.tri[q], P.d));
+            d = run_min(d, dist_point_triangle(T.tri[q], T.tg[q], P.d));
         }
     }
     return d;
