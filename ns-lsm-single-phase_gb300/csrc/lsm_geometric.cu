@@ -388,6 +388,7 @@ struct alignas(16) GeoTet {
     double tri[2][9];
     TriGeo tg[2];
     float box[2][6];  // lo x y z, hi x y z
+    float trf[2][9];  // the vertices rounded to FP32 (upper bounds of the distance)
     double area, wv;
     int nis;
     int v[4];
@@ -572,6 +573,8 @@ __global__ void k_geo_tets(DevGrid g, const double* __restrict__ phi, const doub
                 for (int c = 0; c < 9; ++c) T.tri[q][c] = q < T.nis ? o.tri[q][c / 3][c % 3] : 0.0;
                 tri_geo(T.tri[q], T.tg[q]);
 #pragma unroll
+                for (int c = 0; c < 9; ++c) T.trf[q][c] = (float)T.tri[q][c];
+#pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     const double a = T.tri[q][c], b = T.tri[q][3 + c], e = T.tri[q][6 + c];
                     T.box[q][c] = __double2float_rd(fmin(a, fmin(b, e)));
@@ -599,6 +602,11 @@ __global__ void k_geo_mark(DevGrid g, int npn, const long long* __restrict__ nod
     }
 }
 
+__device__ __forceinline__ float dist3f(const float* a, const float* b) {
+    const float dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
+    return sqrtf(dx * dx + dy * dy + dz * dz);
+}
+
 // a point in both precisions (the FP32 copy for the culling bounds)
 struct Pt {
     double d[3];
@@ -613,18 +621,27 @@ __device__ __forceinline__ Pt make_pt(double a, double b, double c) {
     return p;
 }
 
+// a running value with its FP32 copy for the culling tests, converted
+// only when the value changes (conversions run on the FP64 pipe)
+struct Run {
+    double d;
+    float f;
+};
+__device__ __forceinline__ void set_run(Run& r, double v) {
+    if (dbits(v) != dbits(r.d)) { r.d = v; r.f = (float)v; }
+}
+
 // the triangles of tetrahedron t against point P (running minimum d); a
 // triangle whose bounding box lies beyond d is not evaluated
-__device__ __forceinline__ double tet_min(const GeoTet* __restrict__ tets, int t, const Pt& P, double d) {
+__device__ __forceinline__ void tet_min(const GeoTet* __restrict__ tets, int t, const Pt& P, Run& d) {
     const GeoTet& T = tets[t];
     const int nis = T.nis;
     if (nis > 0 && T.area > 0.0) {
         for (int q = 0; q < nis; ++q) {
-            if (beyond_box(P.f, P.scale, T.box[q], T.box[q] + 3, (float)d)) continue;
-            d = run_min(d, dist_point_triangle(T.tri[q], T.tg[q], P.d));
+            if (beyond_box(P.f, P.scale, T.box[q], T.box[q] + 3, d.f)) continue;
+            set_run(d, run_min(d.d, dist_point_triangle(T.tri[q], T.tg[q], P.d)));
         }
     }
-    return d;
 }
 
 // per pnode: the bounding box of every triangle of its K tetrahedra
@@ -656,11 +673,11 @@ __global__ void k_geo_prad(DevGrid g, int npn, const long long* __restrict__ nod
 }
 
 // true when pnode m's triangles all lie beyond d from P
-__device__ __forceinline__ bool pnode_beyond(int m, const Pt& P, double d, const float4* __restrict__ pbox) {
+__device__ __forceinline__ bool pnode_beyond(int m, const Pt& P, float d, const float4* __restrict__ pbox) {
     const float4 a = pbox[2 * m], b = pbox[2 * m + 1];
     if (a.w == 0.0f) return true;
     const float lo[3] = {a.x, a.y, a.z}, hi[3] = {b.x, b.y, b.z};
-    return beyond_box(P.f, P.scale, lo, hi, (float)d);
+    return beyond_box(P.f, P.scale, lo, hi, d);
 }
 
 // the pnodes' signed distances (src/GetIsosurfaceAndDistances.F90:166-330)
@@ -675,10 +692,11 @@ __global__ void k_geo_sd(DevGrid g, int npn, const long long* __restrict__ node_
         node_ijk(g, l0, &i, &j, &k);
         const Pt P = make_pt(x[l0], y[l0], z[l0]);
         const double s = sgn1(phi[l0]);
-        double dp = 10.0, sd = 99.9;
+        Run dp{10.0, 10.0f};
+        double sd = 99.9;
         auto sd_step = [&]() {
             // sd = |sd| + exsign2 (dp - |sd|), then sign(one, phi) * sd
-            sd = copysign(mag_step(fabs(sd), dp), s);
+            sd = copysign(mag_step(fabs(sd), dp.d), s);
         };
         for (int ks = max(k - 4, 0); ks <= min(k + 4, g.nk - 1); ++ks)
             for (int js = max(j - 4, 0); js <= min(j + 4, g.nj - 1); ++js)
@@ -687,12 +705,12 @@ __global__ void k_geo_sd(DevGrid g, int npn, const long long* __restrict__ node_
                     if (m < 0) continue;
                     // every triangle of this pnode beyond dp: dp stays, the
                     // signed distance update still runs once per tetrahedron
-                    if (pnode_beyond(m, P, dp, prad)) {
+                    if (pnode_beyond(m, P, dp.f, prad)) {
                         for_each_tet(g, is, js, ks, cellbits, tetbase, [&](int) { sd_step(); });
                         continue;
                     }
                     for_each_tet(g, is, js, ks, cellbits, tetbase, [&](int t) {
-                        dp = tet_min(tets, t, P, dp);
+                        tet_min(tets, t, P, dp);
                         sd_step();
                     });
                 }
@@ -835,46 +853,146 @@ __global__ void k_geo_pnode_phi(int npn, const long long* __restrict__ node_of, 
     }
 }
 
-// NeighboursPhiCorrection on the -1 nodes (src/NeighboursPhiCorrection.F90:186-343)
-__global__ void k_geo_neigh(DevGrid g, const int* __restrict__ ids,
-                            const unsigned char* __restrict__ cellbits, const int* __restrict__ tetbase,
-                            const GeoTet* __restrict__ tets, const long long* __restrict__ node_of,
-                            const float4* __restrict__ prad, const double* __restrict__ x,
-                            const double* __restrict__ y, const double* __restrict__ z, double* __restrict__ pc,
-                            int nsec, const long long* __restrict__ second) {
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nsec; c += gridDim.x * blockDim.x) {
+// NeighboursPhiCorrection on the -1 nodes (src/NeighboursPhiCorrection.F90:186-343).
+//
+// One warp per node.  The node's result is a sequential chain over the
+// pnodes of its +-4 box, in the reference's order: per pnode a running
+// minimum dp over the triangles of its K tetrahedra (reset to 10), and
+// after each tetrahedron |v| <- |v| + exsign2 (dp - |v|).  Its last bits
+// depend on that order, so the chain itself runs in order, uniformly on
+// all lanes; what the lanes share out is the FP64 work inside it, the
+// point-triangle distances.  Pnodes that can still change v (the same tests
+// as the chain: the box of all their triangles, then the triangles' own
+// boxes, against the current |v|) are queued with their tetrahedra and
+// triangles; once the queue holds a lane-full of triangles, the lanes
+// evaluate all of them, and the chain is replayed over the queued pnodes,
+// each test made again with the v of that moment.  v only decreases, so a
+// pnode skipped when queued would be skipped in the chain too; one queued
+// but skipped in the replay, or a triangle culled there by the running
+// minimum, only cost a wasted evaluation.  Every value the replay uses is
+// the one the sequential chain computes.
+constexpr int kQN = 16;    // queued pnodes
+constexpr int kQT = 160;   // queued tetrahedra
+constexpr int kQP = 96;    // queued triangles
+constexpr int kQFlush = 32;
+
+struct NeighQueue {
+    int nn, nt, np;
+    int nm[kQN];           // pnode ids
+    int nstart[kQN + 1];   // first tetrahedron slot of each queued pnode
+    int tet[kQT];          // tetrahedron ids, in order
+    int tp[kQT + 1];       // first triangle slot of each tetrahedron slot
+    int ptet[kQP];         // triangle slot -> tetrahedron id
+    unsigned char pq[kQP]; // triangle slot -> triangle 0/1 of that tetrahedron
+    double da[kQP];        // the distances
+};
+
+constexpr int kNeighWarps = 4;
+
+__global__ void __launch_bounds__(32 * kNeighWarps) k_geo_neigh(
+        DevGrid g, const int* __restrict__ ids, const unsigned char* __restrict__ cellbits,
+        const int* __restrict__ tetbase, const GeoTet* __restrict__ tets, const float4* __restrict__ prad,
+        const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z,
+        double* __restrict__ pc, int nsec, const long long* __restrict__ second) {
+    __shared__ NeighQueue qs[kNeighWarps];
+    NeighQueue& Q = qs[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int nwarps = gridDim.x * kNeighWarps;
+    for (int c = blockIdx.x * kNeighWarps + (threadIdx.x >> 5); c < nsec; c += nwarps) {
         const long long l0 = second[c];
         int i, j, k;
         node_ijk(g, l0, &i, &j, &k);
         const Pt P = make_pt(x[l0], y[l0], z[l0]);
         double v = pc[l0];
+        float vf = (float)fabs(v);   // |v| in FP32 for the culling tests
+        int nn = 0, nt = 0, np = 0;  // uniform copies of the queue sizes
+
+        // the triangles of queued pnode slot n all beyond af (pnode box first)
+        auto all_beyond = [&](int n, float af) -> bool {
+            if (pnode_beyond(Q.nm[n], P, af, prad)) return true;
+            for (int s2 = Q.nstart[n]; s2 < Q.nstart[n + 1]; ++s2)
+                for (int p = Q.tp[s2]; p < Q.tp[s2 + 1]; ++p) {
+                    const GeoTet& T = tets[Q.ptet[p]];
+                    if (!beyond_box(P.f, P.scale, T.box[Q.pq[p]], T.box[Q.pq[p]] + 3, af)) return false;
+                }
+            return true;
+        };
+        auto flush = [&]() {
+            __syncwarp();
+            for (int p = lane; p < np; p += 32) {
+                const GeoTet& T = tets[Q.ptet[p]];
+                const int q = Q.pq[p];
+                Q.da[p] = dist_point_triangle(T.tri[q], T.tg[q], P.d);
+            }
+            __syncwarp();
+            for (int n = 0; n < nn; ++n) {
+                if (all_beyond(n, vf)) continue;
+                Run dp{10.0, 10.0f};
+                for (int s2 = Q.nstart[n]; s2 < Q.nstart[n + 1]; ++s2) {
+                    for (int p = Q.tp[s2]; p < Q.tp[s2 + 1]; ++p) {
+                        const GeoTet& T = tets[Q.ptet[p]];
+                        if (beyond_box(P.f, P.scale, T.box[Q.pq[p]], T.box[Q.pq[p]] + 3, dp.f)) continue;
+                        set_run(dp, run_min(dp.d, Q.da[p]));
+                    }
+                    // |v| + exsign2 (dp - |v|), with the sign of v
+                    const double av = fabs(v), nv2 = mag_step(av, dp.d);
+                    if (dbits(nv2) != dbits(av)) vf = (float)nv2;
+                    v = copysign(nv2, v);
+                }
+            }
+            __syncwarp();
+            nn = nt = np = 0;
+        };
+
         for (int ks = max(k - 4, 0); ks <= min(k + 4, g.nk - 1); ++ks)
             for (int js = max(j - 4, 0); js <= min(j + 4, g.nj - 1); ++js)
                 for (int is = max(i - 4, 0); is <= min(i + 4, g.ni - 1); ++is) {
                     const int m = ids[gid(g, is, js, ks)] - 1;
                     if (m < 0) continue;
-                    // every triangle of this pnode beyond |v|: each of its
-                    // running minima stays above |v|, so v cannot change
-                    // (first the box of all its triangles, then the
-                    // triangles' own boxes)
-                    const double av0 = fabs(v);
-                    if (pnode_beyond(m, P, av0, prad)) continue;
-                    const float avf = (float)av0;
-                    bool near = false;
+                    if (pnode_beyond(m, P, vf, prad)) continue;
+                    if (nn == kQN || nt > kQT - 24 || np > kQP - 48) flush();
+                    // queue the pnode's tetrahedra and triangles (every lane
+                    // writes the same values).  A triangle is left out when
+                    // the chain will cull it for sure: ub bounds the
+                    // running minimum from above (the reference's distance is
+                    // at most the distance to each vertex, here in FP32
+                    // with a margin, and whether an earlier triangle is
+                    // evaluated or culled the minimum stays below it), and
+                    // the cull test only gets stricter as the minimum falls.
+                    Q.nm[nn] = m;
+                    Q.nstart[nn] = nt;
+                    float ub = 10.0f;
                     for_each_tet(g, is, js, ks, cellbits, tetbase, [&](int t) {
                         const GeoTet& T = tets[t];
-                        if (near || !(T.nis > 0 && T.area > 0.0)) return;
-                        for (int q = 0; q < T.nis; ++q) near |= !beyond_box(P.f, P.scale, T.box[q], T.box[q] + 3, avf);
+                        const int ntri = (T.nis > 0 && T.area > 0.0) ? T.nis : 0;
+                        Q.tet[nt] = t;
+                        Q.tp[nt] = np;
+                        for (int q = 0; q < ntri; ++q) {
+                            if (!beyond_box(P.f, P.scale, T.box[q], T.box[q] + 3, ub)) {
+                                Q.ptet[np] = t;
+                                Q.pq[np] = (unsigned char)q;
+                                ++np;
+                            }
+                            float u = fminf(dist3f(P.f, T.trf[q]), fminf(dist3f(P.f, T.trf[q] + 3),
+                                                                           dist3f(P.f, T.trf[q] + 6)));
+                            u = u + 1.0e-5f * (u + P.scale) + 1.0e-30f;
+                            ub = fminf(ub, u);
+                        }
+                        ++nt;
                     });
-                    if (!near) continue;
-                    double dp = 10.0;
-                    for_each_tet(g, is, js, ks, cellbits, tetbase, [&](int t) {
-                        dp = tet_min(tets, t, P, dp);
-                        // |v| + exsign2 (dp - |v|), with the sign of v
-                        v = copysign(mag_step(fabs(v), dp), v);
-                    });
+                    Q.tp[nt] = np;
+                    Q.nstart[nn + 1] = nt;
+                    __syncwarp();
+                    if (all_beyond(nn, vf)) {  // not near: drop it again
+                        nt = Q.nstart[nn];
+                        np = Q.tp[nt];
+                        continue;
+                    }
+                    ++nn;
+                    if (np >= kQFlush) flush();
                 }
-        pc[l0] = v;
+        if (nn) flush();
+        if (lane == 0) pc[l0] = v;
     }
 }
 
@@ -1062,8 +1180,8 @@ cudaError_t geo_reinit(const DevGrid& g, const double* phi0, const double* x, co
     }
     {
         ProfScope ps("k_geo_neigh", s);
-        k_geo_neigh<<<grid_for(ns, 128), 128, 0, s>>>(g, ids, cellbits, tetbase, tets, node_of, prad, x, y, z, pc, ns,
-                                                 second);
+        k_geo_neigh<<<grid_for(ns, kNeighWarps), 32 * kNeighWarps, 0, s>>>(g, ids, cellbits, tetbase, tets, prad, x,
+                                                                            y, z, pc, ns, second);
         GEO_CU(cudaGetLastError());
     }
     GEO_CU(cudaStreamSynchronize(s));
