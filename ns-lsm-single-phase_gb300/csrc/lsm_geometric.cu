@@ -18,11 +18,10 @@
 // tetrahedron number, which is exactly the order GetTetrahedraList appends
 // them (src/GetTetrahedraList.F90:322-446).  The distance loops keep the
 // reference's sequential running-minimum updates per node (their rounding
-// depends on the order), one thread per node.
+// depends on the order): one thread per pnode in k_geo_sd, one warp per
+// -1 node in k_geo_neigh (the lanes share out the distances, the chain is
+// replayed in order).
 #include <cuda_runtime.h>
-
-#include <cstdio>
-#include <vector>
 
 #include "lsm_common.cuh"
 #include "lsm_geometric.h"
