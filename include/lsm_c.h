@@ -105,7 +105,11 @@ typedef struct lsm_params {
 } lsm_params;
 
 /* Fill a params struct with the values of the reference's example deck
-   (control.dat): WENO3, btype 1 everywhere, BigPhi 5, M_Sphi0 1, ... */
+   (control.dat): WENO3, btype 1 everywhere, BigPhi 5, M_Sphi0 1,
+   ConvergenceToleranceGeomReini 1e-9, ...  One exception: the deck sets
+   hybrid_reinitialisation = .true. (control.dat:200); the default here is
+   0 (the Sussman branch, which runs on decomposed subdomains too), and
+   read_ind3dmg_lsm / a caller copying global_lsm sets it from the deck. */
 void lsm_params_default(lsm_params* p);
 
 /* ---- handle -------------------------------------------------------------- */
