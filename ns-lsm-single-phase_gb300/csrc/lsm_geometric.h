@@ -110,7 +110,7 @@ double geo_newton(F funcv, double tol, int* its_out, bool* converged) {
         if (check) {
             const double den = std::fmax(f, 0.5 * 1);
             const double t2 = std::fabs(gr) * std::fmax(std::fabs(x), 1.0) / den;
-            check = !(t2 < TOLMIN);
+            check = t2 < TOLMIN;  // spurious convergence: check stays set
             return finish();
         }
         const double t3 = std::fabs(x - xold) / std::fmax(std::fabs(x), 1.0);

@@ -3,7 +3,10 @@
 Each translation unit is compiled by nvcc in parallel and linked into one
 shared library with a plain C ABI (include/lsm_c.h); PyTorch is not linked.
 The FP64 translation units that restate the reference arithmetic are built
-with --fmad=false so every multiply and add is rounded separately.
+with --fmad=false so every multiply and add is rounded separately (and the
+geometric reinitialisation's host-side Newton solve with the host compiler's
+-ffp-contract=off, which matters on Arm hosts, where contraction is the
+default).
 """
 from __future__ import annotations
 
@@ -31,7 +34,7 @@ UNITS = {
     "lsm_fp64.cu": ["--fmad=false"],
     "lsm_volume.cu": ["--fmad=false"],
     "lsm_sussman.cu": ["--fmad=false"],
-    "lsm_geometric.cu": ["--fmad=false"],
+    "lsm_geometric.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"],
     "lsm_capi.cu": ["-Xcompiler", "-fvisibility=default"],
     "lsm_batch.cu": ["--fmad=true"],
     "lsm_batch_capi.cu": ["-Xcompiler", "-fvisibility=default"],

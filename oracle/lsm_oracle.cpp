@@ -1423,7 +1423,8 @@ double geo_funcv(const Geo& G, double target, double C, int* err) {
    src/NewtonRaphsonSolver.F90 (Numerical Recipes' globally convergent
    Newton).  The PARAMETERs written as default-real literals (1.e-12, 1.e-7,
    1.e-4, .1) are single precision promoted to REAL(8).  Returns C. */
-double geo_newton(const Geo& G, double target, double tol, int* its_out, bool* converged, int* err) {
+template <class F>
+double newton_1d(F funcv, double tol, int* its_out, bool* converged) {
     const int MAXITS = 20;
     const double TOLF = (double)1.e-12f, TOLMIN = (double)1.e-12f, TOLX = (double)1.e-12f, STPMX = 100.0;
     const double ALF = (double)1.e-4f, TOLXL = (double)1.e-7f, P1 = (double)0.1f;
@@ -1431,7 +1432,7 @@ double geo_newton(const Geo& G, double target, double tol, int* its_out, bool* c
     double x = 0.0;            /* C_initial_guest */
     bool check = false;        /* not set by newt on its zero-Jacobian return */
     int its = 1;
-    double fvec = geo_funcv(G, target, x, err);
+    double fvec = funcv(x);
     double f = 0.5 * (0.0 + fvec * fvec);
     auto finish = [&](bool conv_path) {
         (void)conv_path;
@@ -1448,11 +1449,11 @@ double geo_newton(const Geo& G, double target, double tol, int* its_out, bool* c
         if (h < kEpsSims) h = EPS;
         x = temp + h;
         h = x - temp;
-        const double fh = geo_funcv(G, target, x, err);
+        const double fh = funcv(x);
         x = temp;
         double fjac = (fh - fvec) / h;
         if (std::fabs(0.0 + fjac) < tol) return finish(false); /* zero Jacobian */
-        fvec = geo_funcv(G, target, x, err);
+        fvec = funcv(x);
         const double gr = 0.0 + fjac * fvec;
         const double xold = x, fold = f;
         double p = -fvec;
@@ -1469,7 +1470,7 @@ double geo_newton(const Geo& G, double target, double tol, int* its_out, bool* c
         double alam = 1.0, alam2 = 2.0, f2 = 2.0, tmplam = 0.0;
         for (;;) {
             x = xold + alam * p;
-            fvec = geo_funcv(G, target, x, err);
+            fvec = funcv(x);
             f = 0.5 * (0.0 + fvec * fvec);
             if (alam < alamin) { x = xold; check = true; break; }
             if (f <= fold + ALF * alam * slope) break;
@@ -1496,7 +1497,7 @@ double geo_newton(const Geo& G, double target, double tol, int* its_out, bool* c
         if (check) {
             const double den = std::max(f, 0.5 * 1);
             const double t2 = std::fabs(gr) * std::max(std::fabs(x), 1.0) / den;
-            check = !(t2 < TOLMIN);
+            check = t2 < TOLMIN; /* spurious convergence: check stays set */
             return finish(false);
         }
         const double t3 = std::fabs(x - xold) / std::max(std::fabs(x), 1.0);
@@ -1505,9 +1506,22 @@ double geo_newton(const Geo& G, double target, double tol, int* its_out, bool* c
     return finish(false); /* its = MAXITS + 1 */
 }
 
+double geo_newton(const Geo& G, double target, double tol, int* its_out, bool* converged, int* err) {
+    return newton_1d([&](double c) { return geo_funcv(G, target, c, err); }, tol, its_out, converged);
+}
+
 } /* namespace */
 
 extern "C" {
+
+/* The Newton solve alone, on a caller's function f(ud, C) = target - volume(C)
+   (test entry: the product's solver is checked against this one). */
+int oracle_newton_1d(double (*f)(void*, double), void* ud, double tol, int* its, int* conv, double* C) {
+    bool c = false;
+    *C = newton_1d([&](double x) { return f(ud, x); }, tol, its, &c);
+    *conv = c ? 1 : 0;
+    return LSM_OK;
+}
 
 /* geometric_reinitialisation, src/geometric_reinitialisation.F90:1-94
    (TriangulationCase 1, one rank, no ghost planes, no blanking).
