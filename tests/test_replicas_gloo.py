@@ -5,7 +5,10 @@ runs its own copy of the workload, with no data-path collective).  What the
 N > 1 launch relies on is host logic: the process-group setup from the
 torchrun environment, the barrier around the timed region, the maximum of
 the ranks' times, and the reference arm printing from rank 0 only.  Each
-rank here is a spawned CPU process on 127.0.0.1.
+rank here is a spawned CPU process on 127.0.0.1 with every GPU hidden (so
+the process group is gloo even on a machine with one GPU, where two NCCL
+ranks would have to share it), and the ranks are killed if they do not
+finish in time.
 """
 import os
 import socket
@@ -25,7 +28,33 @@ def _free_port():
         return s.getsockname()[1]
 
 
+def _cpu_only():
+    # before anything initialises CUDA in this (spawned) process
+    os.environ["CUDA_VISIBLE_DEVICES"] = ""
+
+
+def _run_ranks(target, args_of, n):
+    """start n spawned ranks, collect one queue item each, always reap them"""
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=target, args=args_of(r, q), daemon=True) for r in range(n)]
+    for p in procs:
+        p.start()
+    try:
+        res = [q.get(timeout=120) for _ in procs]
+        for p in procs:
+            p.join(timeout=60)
+            assert p.exitcode == 0
+        return res
+    finally:
+        for p in procs:
+            if p.is_alive():
+                p.kill()
+                p.join(timeout=10)
+
+
 def _rank_main(rank, world, port, out):
+    _cpu_only()
     os.environ.update({"RANK": str(rank), "WORLD_SIZE": str(world), "LOCAL_RANK": str(rank),
                        "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
     sys.path.insert(0, REPO)
@@ -42,21 +71,14 @@ def _rank_main(rank, world, port, out):
 
 def test_two_replicas_barrier_and_max_time():
     port = _free_port()
-    ctx = mp.get_context("spawn")
-    q = ctx.Queue()
-    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
-    for p in procs:
-        p.start()
-    res = sorted(q.get(timeout=120) for _ in procs)
-    for p in procs:
-        p.join(timeout=60)
-        assert p.exitcode == 0
+    res = sorted(_run_ranks(_rank_main, lambda r, q: (r, 2, port, q), 2))
     assert [r for r, *_ in res] == [0, 1]
     for _, w, t, value in res:
         assert w == 2 and t == 1.5 and abs(value - 2000 / 1.5) < 1e-9
 
 
 def _ref_rank(rank, world, out):
+    _cpu_only()
     os.environ.update({"RANK": str(rank), "WORLD_SIZE": str(world)})
     sys.path.insert(0, REPO)
     import contextlib
@@ -74,13 +96,5 @@ def _ref_rank(rank, world, out):
 
 
 def test_reference_arm_prints_from_rank_zero_only():
-    ctx = mp.get_context("spawn")
-    q = ctx.Queue()
-    procs = [ctx.Process(target=_ref_rank, args=(r, 2, q)) for r in range(2)]
-    for p in procs:
-        p.start()
-    res = dict(q.get(timeout=120) for _ in procs)
-    for p in procs:
-        p.join(timeout=60)
-        assert p.exitcode == 0
+    res = dict(_run_ranks(_ref_rank, lambda r, q: (r, 2, q), 2))
     assert '"impl": "reference"' in res[0] and res[1] == ""
