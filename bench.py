@@ -901,13 +901,13 @@ def run_fp64(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = host_threads()
         if scheme == 2:
-            # the oracle's geometric reinitialisation is serial: an eighth of the grid
+            # an eighth of the grid keeps the oracle's step within the bench's minutes
             sg = (W["ni"] // 2, W["nj"] // 2, W["nk"] // 2)
             sample = make_case(sg[0], sg[1], sg[2], W["reinit_iters"], scheme)
             sec, used = cpu_oracle_time(sample, 1, threads)
             cpu = {"value": sample.grid.n / sec / 1e9, "unit": "Gcell-steps/s", "cores": used, "kind": "port",
-                   "sample": "1 physical step of the same case on %dx%dx%d nodes (FP64 oracle; advection on %d "
-                             "OpenMP threads, the geometric reinitialisation serial)" % (sg + (used,))}
+                   "sample": "1 physical step of the same case on %dx%dx%d nodes (FP64 oracle, OpenMP, %d "
+                             "threads; the Newton solve serial)" % (sg + (used,))}
         else:
             sample = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"], scheme)
             sec, used = cpu_oracle_time(sample, 1, threads)
@@ -952,7 +952,7 @@ def run_reference(args):
     W = workload(args)
     scheme = FP64_SCHEME[args.workload]
     if scheme == 2 and not args.grid:
-        # the oracle's geometric reinitialisation is serial: an eighth of the grid
+        # an eighth of the grid keeps the oracle's steps within the bench's minutes
         W["ni"], W["nj"], W["nk"] = W["ni"] // 2, W["nj"] // 2, W["nk"] // 2
     case = make_case(W["ni"], W["nj"], W["nk"], W["reinit_iters"], scheme)
     threads = host_threads()

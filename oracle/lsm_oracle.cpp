@@ -1584,7 +1584,10 @@ int oracle_geometric_reinitialisation(const lsm_grid* gg, const lsm_params* p, c
                 }
             }
     /* GetIsosurfaceAndDistances: marching tetrahedra on the K tetrahedra */
-    for (GKTet& t : G.tets) {
+    const long ntet = (long)G.tets.size(), npn = (long)G.nodes.size();
+#pragma omp parallel for schedule(static) reduction(| : err)
+    for (long it = 0; it < ntet; ++it) {
+        GKTet& t = G.tets[it];
         double V[4][3], ph[4];
         G.vertices(t, V);
         for (int q = 0; q < 4; ++q) ph[q] = G.nodes[t.v[q]].phi;
@@ -1594,8 +1597,13 @@ int oracle_geometric_reinitialisation(const lsm_grid* gg, const lsm_params* p, c
         t.nis = o.ntri > 0 ? o.ntri : 0;
         std::memcpy(t.tri, o.tri, sizeof(t.tri));
     }
-    /* ... and the pnodes' distances over the +-4 box, tagging non-pnodes -1 */
-    for (GPNode& n : G.nodes) {
+    /* ... the pnodes' distances over the +-4 box ... (the reference tags the
+       box's non-pnodes -1 inside the same loop; the tags change no test of
+       the loop, which only asks for ids > 0, so they are a pass of their
+       own here and the distance loop reads ids only) */
+#pragma omp parallel for schedule(dynamic, 16)
+    for (long ip = 0; ip < npn; ++ip) {
+        GPNode& n = G.nodes[ip];
         const double P[3] = {n.x, n.y, n.z};
         double dp = 10.0;
         for (int ks = std::max(n.k - 4, g.kl); ks <= std::min(n.k + 4, g.ku); ++ks)
@@ -1611,18 +1619,26 @@ int oracle_geometric_reinitialisation(const lsm_grid* gg, const lsm_params* p, c
                             n.sd = asd + ex2 * (dp - asd);
                             n.sd = fsign1(n.phi) * n.sd;
                         }
-                    } else {
-                        ids[l] = -1;
                     }
                 }
     }
+    /* ... and the -1 tags */
+    for (const GPNode& n : G.nodes)
+        for (int ks = std::max(n.k - 4, g.kl); ks <= std::min(n.k + 4, g.ku); ++ks)
+            for (int js = std::max(n.j - 4, g.jl); js <= std::min(n.j + 4, g.ju); ++js)
+                for (int is = std::max(n.i - 4, g.il); is <= std::min(n.i + 4, g.iu); ++is) {
+                    const long l = g.id(is, js, ks);
+                    if (ids[l] <= 0) ids[l] = -1;
+                }
     /* GlobalMassCorrection: per-tetrahedron eta (secant), xi, Newton's C */
     double Cc = 0.0;
     int its = 0;
     bool conv = false;
     if (p->GlobalMassCorrection) {
         const double tol = p->ConvergenceToleranceGeomReini / 1000.0;
-        for (GKTet& t : G.tets) {
+#pragma omp parallel for schedule(dynamic, 64) reduction(| : err)
+        for (long it = 0; it < ntet; ++it) {
+            GKTet& t = G.tets[it];
             double V[4][3], ph[4];
             G.vertices(t, V);
             for (int q = 0; q < 4; ++q) ph[q] = G.nodes[t.v[q]].sd;
@@ -1641,8 +1657,9 @@ int oracle_geometric_reinitialisation(const lsm_grid* gg, const lsm_params* p, c
         n.phi = n.sd + aux;
         pc[g.id(n.i, n.j, n.k)] = n.phi;
     }
-    /* ... and the -1 nodes */
+    /* ... and the -1 nodes (each reads and writes its own value only) */
     int nsecond = 0;
+#pragma omp parallel for collapse(2) schedule(dynamic, 4) reduction(+ : nsecond)
     for (int k = g.kl; k <= g.ku; ++k)
         for (int j = g.jl; j <= g.ju; ++j)
             for (int i = g.il; i <= g.iu; ++i) {
