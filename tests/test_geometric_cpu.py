@@ -217,3 +217,13 @@ def test_near_zero_values_run(oracle):
     # reference, so some distances come from farther triangles)
     m = ids != 0
     assert (np.abs(out[m]) - np.abs(0.5 - z[m])).min() >= -1e-12
+
+
+def test_openmp_oracle_is_bit_identical(oracle):
+    """the timing build (OpenMP) gives the checker's bits (no mass correction:
+    its Newton sums are serial in both)"""
+    omp = O.Oracle(omp=True)
+    g, x, y, z, phi, _ = cases.curvilinear(20, 14, 16, seed=3)
+    a = oracle.geometric_reinitialisation(g, O.make_params(), phi, x, y, z, 0.0, seed(phi))
+    b = omp.geometric_reinitialisation(g, O.make_params(), phi, x, y, z, 0.0, seed(phi))
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and a[2] == b[2]
