@@ -227,3 +227,13 @@ def test_openmp_oracle_is_bit_identical(oracle):
     a = oracle.geometric_reinitialisation(g, O.make_params(), phi, x, y, z, 0.0, seed(phi))
     b = omp.geometric_reinitialisation(g, O.make_params(), phi, x, y, z, 0.0, seed(phi))
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and a[2] == b[2]
+
+
+def test_no_interface_changes_nothing(oracle):
+    g, x, y, z, phi, _ = cases.curvilinear(12, 10, 9, seed=2)
+    phi = cases.F(np.abs(phi) + 0.5)          # all water: no phase-change cell
+    pc0 = seed(phi)
+    out, ids, info = oracle.geometric_reinitialisation(g, O.make_params(GlobalMassCorrection=1), phi, x, y, z,
+                                                       1.0, pc0)
+    assert info["nnodes"] == 0 and info["ntetrahedra"] == 0 and info["nsecond"] == 0
+    assert np.array_equal(out, pc0) and not ids.any()

@@ -143,3 +143,15 @@ def test_geometric_rejects_ghost_planes(ls):
     with pytest.raises(LsmError) as e:
         ls.geometric_reinitialisation(G(gg), P(O.make_params()), phi, x, y, z, 0.0, seed(phi))
     assert e.value.status == 4
+
+
+def test_geometric_without_interface(ls, oracle):
+    """no phase-change cell: no lists, phicorrected untouched, no Newton"""
+    g, x, y, z, phi, _ = cases.curvilinear(12, 10, 9, seed=2)
+    phi = cases.F(np.abs(phi) + 0.5)
+    pc0 = seed(phi)
+    p = O.make_params(GlobalMassCorrection=1)
+    out, ids, info = ls.geometric_reinitialisation(G(g), P(p), dev(phi), dev(x), dev(y), dev(z), 1.0, dev(pc0))
+    out, ids = host(out), host(ids)
+    assert info["nnodes"] == 0 and info["ntetrahedra"] == 0 and info["nsecond"] == 0 and info["C"] == 0.0
+    assert np.array_equal(out, pc0) and not ids.any()
