@@ -51,6 +51,17 @@ def test_reads_every_record():
     assert p.call_levelsetmethod and p.call_reinitialisation and not p.hybrid_reinitialisation
     assert p.TotalVolumeComputation and not p.GlobalMassCorrection
     assert p.epsReinitialisation == 1e-5 and p.BigPhi == 5.0
+    assert p.ConvergenceToleranceGeomReini == 1.0e-4
+
+
+def test_hybrid_deck_selects_the_geometric_branch():
+    deck = DECK.replace(".true.\n.true.\n.false.\n3\n2.5\n1.0e-4\nT\n.false.",
+                        ".true.\n.true.\n.true.\n3\n2.5\n1.0E-09\nT\n.true.")
+    p = read_ind3dmg_lsm(deck, delti=0.01)
+    assert p.hybrid_reinitialisation and p.GlobalMassCorrection
+    assert p.ConvergenceToleranceGeomReini == 1.0e-9
+    c = p.to_c()
+    assert c.hybrid_reinitialisation == 1 and c.GlobalMassCorrection == 1 and c.ConvergenceToleranceGeomReini == 1e-9
 
 
 def test_multi_zone_btype_and_repeat_counts():
