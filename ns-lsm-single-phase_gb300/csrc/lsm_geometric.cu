@@ -379,9 +379,10 @@ __device__ __forceinline__ void for_each_tet(const DevGrid& g, int i, int j, int
     }
 }
 
-// one K tetrahedron: its isosurface triangles (18 doubles), area and water
-// volume of the linear reconstruction, its four pnode ids (0-based) and a
-// bounding box per triangle (FP32, rounded outwards) used only to skip
+// one K tetrahedron: its isosurface triangles (18 doubles) with their
+// triangle-only distance terms (TriGeo), area and water volume of the
+// linear reconstruction, its four pnode ids (0-based), and per triangle an
+// FP32 bounding box (rounded outwards) and FP32 vertices, used only to skip
 // distance evaluations that cannot change a running minimum
 struct alignas(16) GeoTet {
     double tri[2][9];
