@@ -258,10 +258,14 @@ int lsm_total_water_volume(lsm_handle h, const lsm_grid* g, const double* phi,
    scratch is one file-scope device array of fixed size (about 6 MiB, held by
    every GPU that loads this library until the process exits), sized for at
    most LSM_NOALLOC_MAX_CELLS cells; larger grids return LSM_ERR_CAPACITY.
-   The first call on each device looks the array's address up, so make that
-   first call before any stream capture.  Every call shares the one array:
+   The first call on each device looks the array's address up and keeps it
+   for the life of the process, so make that first call before any stream
+   capture, and do not call this entry point again on a device after a
+   cudaDeviceReset of it (the array may then sit at another address).
+   Every call shares the one array:
    calls that overlap on the GPU (other streams or threads) race and must be
-   serialised by the caller.  The call returns after `stream` has drained. */
+   serialised by the caller.  `volumes` on another GPU returns
+   LSM_ERR_MIXED_MEMORY.  The call returns after `stream` has drained. */
 #define LSM_NOALLOC_MAX_CELLS (64LL * 1024 * 1024)
 int lsm_total_water_volume_noalloc(const lsm_grid* g, const double* phi, const double* x,
                                    const double* y, const double* z, double* volumes,

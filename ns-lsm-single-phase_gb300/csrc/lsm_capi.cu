@@ -1094,14 +1094,19 @@ int noalloc_scratch(int dev, unsigned char** out) {
     return LSM_OK;
 }
 
-bool is_device_ptr(const void* p, int dev) {
+// Where a pointer lives: 0 plain host memory (unregistered or page-locked),
+// 1 device or managed memory of GPU `dev`, -1 device or managed memory of
+// another GPU (or an address the runtime cannot classify).
+int classify_ptr(const void* p, int dev) {
     cudaPointerAttributes at;
     if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
         cudaGetLastError();
-        return false;
+        return -1;
     }
-    return (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) && at.device == dev;
+    if (at.type == cudaMemoryTypeUnregistered || at.type == cudaMemoryTypeHost) return 0;
+    return at.device == dev ? 1 : -1;
 }
+bool is_device_ptr(const void* p, int dev) { return classify_ptr(p, dev) == 1; }
 
 }  // namespace
 
@@ -1123,6 +1128,9 @@ extern "C" int lsm_total_water_volume_noalloc(const lsm_grid* g, const double* p
     for (const double* a : {phi, x, y, z})
         if (!is_device_ptr(a, dev))
             return set_err(nullptr, LSM_ERR_MIXED_MEMORY, "inputs must be device arrays of the current GPU");
+    const int vol_where = classify_ptr(volumes, dev);
+    if (vol_where < 0)
+        return set_err(nullptr, LSM_ERR_MIXED_MEMORY, "volumes must be host memory or device memory of the current GPU");
     unsigned char* base = nullptr;
     LSM_TRY(noalloc_scratch(dev, &base));
     cudaStream_t s = (cudaStream_t)stream;
@@ -1135,7 +1143,7 @@ extern "C" int lsm_total_water_volume_noalloc(const lsm_grid* g, const double* p
     LSM_TRY(after_launch(nullptr));
     double res[4];
     unsigned flags = 0;
-    const cudaMemcpyKind k = is_device_ptr(volumes, dev) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    const cudaMemcpyKind k = vol_where == 1 ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     LSM_CU(nullptr, cudaMemcpyAsync(k == cudaMemcpyDeviceToHost ? (void*)res : (void*)volumes, result,
                                     sizeof(res), k, s));
     LSM_CU(nullptr, cudaMemcpyAsync(&flags, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s));

@@ -64,3 +64,46 @@ def test_noalloc_rejects_grids_beyond_its_fixed_scratch(ls):
                                             dummy.ctypes.data, dummy.ctypes.data, None)
     assert st == _lib.LSM_ERR_CAPACITY
     assert b"LSM_NOALLOC_MAX_CELLS" in lib.lsm_last_error(None)
+
+
+def test_noalloc_leaves_free_device_memory_unchanged(ls):
+    """The property the entry point exists for: after one warm-up call (which
+    loads the kernels), repeated calls do not change the free device memory
+    the driver reports."""
+    from nslsm import Grid, _lib
+    lib = _lib.load()
+    g, x, y, z, phi, _ = cases.curvilinear(36, 24, 20, seed=5)
+    grid = Grid(36, 24, 20)
+    gc = grid.to_c()
+    dx, dy, dz, dphi = _dev(x), _dev(y), _dev(z), _dev(phi)
+    dres = torch.zeros(4, dtype=torch.float64, device="cuda")
+    got = np.zeros(4)
+    stream = torch.cuda.current_stream().cuda_stream
+    args = (C.byref(gc), dphi.data_ptr(), dx.data_ptr(), dy.data_ptr(), dz.data_ptr())
+    assert lib.lsm_total_water_volume_noalloc(*args, got.ctypes.data, stream) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for r in range(4):
+        out = got.ctypes.data if r % 2 == 0 else dres.data_ptr()
+        assert lib.lsm_total_water_volume_noalloc(*args, out, stream) == 0, lib.lsm_last_error(None)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+    assert cases.relerr(dres.cpu().numpy(), got) <= TOL
+
+
+def test_noalloc_rejects_host_inputs(ls):
+    """phi, x, y, z must be device arrays: host arrays are refused before any
+    kernel runs."""
+    from nslsm import Grid, _lib
+    lib = _lib.load()
+    g, x, y, z, phi, _ = cases.curvilinear(12, 10, 8, seed=6)
+    gc = Grid(12, 10, 8).to_c()
+    got = np.zeros(4)
+    st = lib.lsm_total_water_volume_noalloc(C.byref(gc), phi.ctypes.data, x.ctypes.data, y.ctypes.data,
+                                            z.ctypes.data, got.ctypes.data, None)
+    assert st == _lib.LSM_ERR_MIXED_MEMORY
+    dphi = _dev(phi)
+    st = lib.lsm_total_water_volume_noalloc(C.byref(gc), dphi.data_ptr(), x.ctypes.data, y.ctypes.data,
+                                            z.ctypes.data, got.ctypes.data, None)
+    assert st == _lib.LSM_ERR_MIXED_MEMORY
