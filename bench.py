@@ -7,15 +7,17 @@ Default workload ("fwdadj"): the large free-surface case, 512 x 256 x 256
 curvilinear nodes (x = 16 xi + 0.05 sin(2 pi eta), y = 4 eta, z = 2 zeta^1.3),
 phi0 = z - 1 - 0.08 sech^2(k(x-4)) (1 + 0.2 cos(2 pi y / 4)), solitary-wave
 velocity, CFL 0.4, 10 reinitialisation pseudo-steps per step, FP64 water
-volume every step.  One benchmark step = one 20-step checkpoint segment of
-the FP32 batched path forward (autotuned tile shape), keeping every step's
-internals (the segment is the run's last, so its reverse needs no
-recompute), followed by its hand-written adjoint, seeded with dL/dphi_T of
-a linear loss with seeded weights; successive benchmark steps continue the
-trajectory (10 steps = the 200-step run).  Beside it: the plain FP64 GPU path
-(lsm_levelsetmethod, the reference's arithmetic) on the same grid, timed,
-and used as the FP64 reference for the FP32 path's narrow-band phi error
-and volume difference after 20 steps.
+volume and mass correction (towards the initial volume) every step.  One
+benchmark step = the whole 200-step run of the FP32 batched path (autotuned
+tile shape) from phi0 with a checkpoint every 20 steps, followed by the
+hand-written adjoint's reverse sweep, seeded with dL/dphi_T of a linear loss
+with seeded weights: the sweep reverses the last segment from the internals
+the forward kept and recomputes each of the 9 earlier segments from its
+checkpoint before reversing it.  Beside it: the plain FP64 GPU path
+(lsm_levelsetmethod, the reference's arithmetic) on the same grid, timed;
+and the narrow-band phi error and volume drift of the FP32 run after 200
+steps against the same 200 steps in FP64 (the batch's FP64 instantiation,
+which matches the FP64 oracle to 1e-12, with the same mass correction).
 
 "batched" workload: 64 independent instances with per-axis sizes drawn from
 {32..96} (numpy seed 0), identity-plus-random-shear grids, Fourier phi0,
@@ -537,7 +539,12 @@ def run_ours(args):
 
 
 # ------------------------------------------------- FP32 forward + adjoint arm
-FWDADJ = dict(ni=512, nj=256, nk=256, reinit_iters=10, segment=20, compare_steps=20)
+FWDADJ = dict(ni=512, nj=256, nk=256, reinit_iters=10, nsteps=200, ckpt=20, compare_steps=20)
+FWDADJ_METRIC = ("Gcell-steps/s (batched FP32 level-set forward + adjoint: WENO3-RK3 + %d reinit pseudo-steps + "
+                 "FP64 volume and mass correction; vs the plain FP64 GPU path)")
+FWDADJ_WORKLOAD = ("large_free_surface %dx%dx%d curvilinear, CFL 0.4, %d RK3 steps, %d reinit pseudo-steps/step, "
+                   "FP64 volume reduction and mass correction every step; adjoint with a checkpoint every %d steps "
+                   "(one step = the whole run: forward from phi0, then the reverse sweep recomputing %d segments)")
 
 # algorithmic HBM bytes per node for one launch of the FP32 batched kernels
 # (each distinct array read once and written once; halos not counted)
@@ -558,6 +565,11 @@ FWDADJ_BYTES = {
     "k_adj_contra": 18 * 4,        # lamW(3), metrics(9), lam_u(3, rmw)
     "k_cvt_in": 8 + 4,
     "k_cvt_out": 4 + 8,
+    "k_volume_slope": 4 + 8,       # as k_volume; the slope dV/dC adds arithmetic on interface cells only
+    "k_mass_shift": 2 * 4,         # phi in, phi out
+    "k_mass_weights": 4,           # phi (interface cells' coordinates and weight atomics not counted)
+    "k_tile_sum": 4,               # lam
+    "k_mass_apply": 8,             # fixed-point weights (lam read and written on interface nodes only)
 }
 
 
@@ -590,8 +602,10 @@ def run_fwdadj(args):
     if args.grid:
         W["ni"], W["nj"], W["nk"] = (int(v) for v in args.grid.lower().split("x"))
     if args.segment:
-        W["segment"] = args.segment
-    R, S = W["reinit_iters"], W["segment"]
+        W["ckpt"] = args.segment
+    if args.nsteps:
+        W["nsteps"] = args.nsteps
+    R, NS, CK = W["reinit_iters"], W["nsteps"], min(W["ckpt"], W["nsteps"])
     case = configs.large_free_surface(W["ni"], W["nj"], W["nk"], reinit_iters=R)
     g = case.grid
     n = g.n
@@ -609,51 +623,82 @@ def run_fwdadj(args):
     dt = case.cfl / smax
     cp = case.params
     eps, dtau = cp.epslsm, cp.RNtimestep
+    inst = [(g.ni, g.nj, g.nk, dt, dtau, eps)]
 
-    # ---- plain FP64 GPU path on the same grid: timed, and the FP64 reference
-    # for the FP32 path's accuracy after `compare_steps` steps
+    def make_batch(**kw):
+        b = LevelSetBatch(inst, RNitermax=R, btype=(1,) * 6, BigPhi=5.0, stream=stream.cuda_stream,
+                          mass_correction=True, **kw)
+        b.set_geometry(0, x, y, z, csi, eta, zet)
+        b.set_velocity(0, q)
+        b.set_phi(0, phi0)
+        return b
+
+    # ---- plain FP64 GPU path on the same grid (lsm_levelsetmethod, the
+    # reference's arithmetic; no mass correction in its Sussman branch), timed
     p64 = LsmParams(epslsm=eps, delti_lsm=dt, RNitermax=R, RNtimestep=dtau, isnarrow=1, narrowcoef=4.0, BigPhi=5.0)
     ls.set_stream(torch.cuda.current_stream().cuda_stream)
     phi64, phin64 = phi0.clone(), phi0.clone()
     nc = W["compare_steps"]
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    vol64 = None
     for it in range(1, nc + 1):
         if it == 2:
             e0.record()
         phin64.copy_(phi64)
-        vol64 = ls.levelsetmethod(g, p64, q, csi, eta, zet, aj, phi64, phin64, x, y, z, it)
+        ls.levelsetmethod(g, p64, q, csi, eta, zet, aj, phi64, phin64, x, y, z, it)
     e1.record()
     torch.cuda.synchronize()
     v64 = n * (nc - 1) / (e0.elapsed_time(e1) / 1e3) / 1e9
     ls.set_stream(None)
     ls.close()
-    del phin64
+    del phi64, phin64
     torch.cuda.empty_cache()
 
-    # ---- the FP32 batch (one instance of the whole grid); the recorded
-    # segment keeps the pseudo-steps' adjoint coefficients when they fit in
-    # device memory (else the reverse sweep recomputes them)
-    need = LevelSetBatch.adjoint_bytes(n, R, S, S, "fp32", "store")
+    # ---- accuracy after the whole run: FP32 and FP64 (the same algorithm in
+    # the reference's FP64 arithmetic) batches, both mass-corrected towards
+    # the initial volume, NS steps each
+    acc = None
+    if not args.no_fp64_compare:
+        b64 = make_batch(precision="fp64")
+        target = float(b64.water_volume()[0, 3])
+        b64.set_mass_target(0, target)
+        b64.step(NS, volumes=False)
+        phi64 = b64.get_phi(0, like=phi0)
+        vol64 = float(b64.water_volume()[0, 3])
+        b64.close()
+        torch.cuda.empty_cache()
+        b32 = make_batch()
+        b32.set_mass_target(0, target)
+        b32.step(NS, volumes=False)
+        phi32 = b32.get_phi(0, like=phi0)
+        vol32 = float(b32.water_volume()[0, 3])
+        b32.close()
+        band = phi64.abs() < 4.0 * eps
+        acc = {"steps": NS, "band_linf_phi_err": float((phi32 - phi64).abs()[band].max()),
+               "band": "|phi64| < 4 epslsm (6 cells)",
+               "volume_rel_diff": abs(vol32 - vol64) / abs(vol64),
+               "volume_drift_fp32": abs(vol32 - target) / target, "volume_drift_fp64": abs(vol64 - target) / target,
+               "reference": "FP64 batch (the same algorithm in FP64, matching the FP64 oracle to 1e-12) with the same "
+                            "mass correction; drift = |V(phi_T) - V(phi_0)| / V(phi_0)"}
+        del phi32, phi64, band
+        torch.cuda.empty_cache()
+
+    # ---- the timed FP32 batch; the recorded segments keep the pseudo-steps'
+    # adjoint coefficients when they fit in device memory (else the reverse
+    # sweep recomputes them)
+    need = LevelSetBatch.adjoint_bytes(n, R, NS, CK, "fp32", "store", True)
     mode = "store" if need + (8 << 30) < torch.cuda.mem_get_info()[0] else "recompute"
-    b = LevelSetBatch([(g.ni, g.nj, g.nk, dt, dtau, eps)], RNitermax=R, btype=(1,) * 6, BigPhi=5.0,
-                      stream=stream.cuda_stream, adjoint_mode=mode)
-    b.set_geometry(0, x, y, z, csi, eta, zet)
-    b.set_velocity(0, q)
-    b.set_phi(0, phi0)
-    vols32 = b.step(nc)
-    phi32 = b.get_phi(0, like=phi0)
-    band = phi64.abs() < 4.0 * eps
-    band_err = float((phi32 - phi64).abs()[band].max())
-    vol_err = abs(float(vols32[0, 3]) - float(vol64[3])) / abs(float(vol64[3]))
-    del phi32, band
-    b.set_phi(0, phi0)
+    b = make_batch(adjoint_mode=mode)
+    target = float(b.water_volume()[0, 3])
+    b.set_mass_target(0, target)
     gen = torch.Generator(device="cuda").manual_seed(0)
     wts = torch.randn(phi0.shape, generator=gen, dtype=torch.float64, device="cuda")
 
     def bench_step():
-        b.forward_record(S, S)
+        # the whole run from phi0: NS steps forward with a checkpoint every CK
+        # steps, then the reverse sweep (recomputing every segment but the last)
+        b.set_phi(0, phi0)
+        b.forward_record(NS, CK)
         b.set_grad_phi(0, wts)
         b.backward()
 
@@ -683,8 +728,9 @@ def run_fwdadj(args):
     dist_barrier(world)
     ms = ev0.elapsed_time(ev1)
     ms_max = dist_max(ms, world)
-    value = world * n * S * args.steps / (ms_max / 1e3) / 1e9
+    value = world * n * NS * args.steps / (ms_max / 1e3) / 1e9
     shape = b.shape
+    mstate = b.mass_state()[0]
 
     # ---- end to end through the C-ABI with host (pinned) arrays
     def pinned(a):
@@ -701,7 +747,7 @@ def run_fwdadj(args):
     h_gphi, t5 = pinned(np.zeros(g.shape))
     h_gq, t6 = pinned(np.zeros((4,) + g.shape))
     keep = (t1, t2, t3, t4, t5, t6)
-    e2e_steps = 3
+    e2e_steps = max(1, min(args.steps, 2))
     parts = {}
 
     def part(name, fn):
@@ -714,7 +760,8 @@ def run_fwdadj(args):
     for _ in range(e2e_steps):
         part("set_phi", lambda: b.set_phi(0, h_phi))
         part("set_velocity", lambda: b.set_velocity(0, h_q))
-        part("forward_record", lambda: b.forward_record(S, S))
+        part("set_mass_target", lambda: b.set_mass_target(0, target))
+        part("forward_record", lambda: b.forward_record(NS, CK))
         part("get_phi", lambda: b._chk(b.lib.lsm_batch_get_phi(b.h, 0, h_phiT.ctypes.data), "get_phi"))
         part("set_grad_phi", lambda: b.set_grad_phi(0, h_w))
         part("backward", lambda: b.backward())
@@ -724,25 +771,25 @@ def run_fwdadj(args):
                                                  "get_grad_velocity"))
     torch.cuda.synchronize()
     e2e_s = dist_max(time.perf_counter() - t0, world)
-    e2e_value = world * n * S * e2e_steps / e2e_s / 1e9
+    e2e_value = world * n * NS * e2e_steps / e2e_s / 1e9
     del keep
-
     b.close()
+    torch.cuda.empty_cache()
 
-    # ---- per-kernel attribution: a batch without the graph, one shorter
-    # segment (4 steps) forward + adjoint under the library's event timer
-    b2 = LevelSetBatch([(g.ni, g.nj, g.nk, dt, dtau, eps)], RNitermax=R, btype=(1,) * 6, BigPhi=5.0,
-                       stream=stream.cuda_stream, use_graph=False, autotune=False, shape=shape[0], adjoint_mode=mode)
-    b2.set_geometry(0, x, y, z, csi, eta, zet)
-    b2.set_velocity(0, q)
-    b2.set_phi(0, phi0)
-    SA = min(4, S)   # physical steps of the attributed segment
-    b2.forward_record(min(2, S), min(2, S))
+    # ---- per-kernel attribution: a batch without the graph, the same schedule
+    # in miniature (10 steps, a checkpoint every step: 9 plain steps, 1
+    # recorded, 9 recomputed, 10 reversed -- the 0.9 : 1 : 1 proportions of
+    # the full run) under the library's event timer
+    b2 = make_batch(use_graph=False, autotune=False, shape=shape[0], adjoint_mode=mode)
+    b2.set_mass_target(0, target)
+    SA = 10
+    b2.forward_record(2, 1)
     b2.set_grad_phi(0, wts)
     b2.backward()
     torch.cuda.synchronize()
     with KernelTimer() as kt:
-        b2.forward_record(SA, SA)
+        b2.set_phi(0, phi0)
+        b2.forward_record(SA, 1)
         b2.set_grad_phi(0, wts)
         b2.backward()
         torch.cuda.synchronize()
@@ -751,22 +798,22 @@ def run_fwdadj(args):
     peaks = load_peaks()
     roof = _roofline(prof, n, peaks, FWDADJ_BYTES, "FP32 words x 4 B per node (FP64 cell volume 8 B)")
     # whole-step roofline: algorithmic bytes of every launch of the profiled
-    # 4-step segment, per cell-step, at the measured throughput
+    # schedule, per cell-step, at the measured throughput
     seg_bytes = sum(FWDADJ_BYTES[k] * n * v[0] for k, v in prof.items() if k in FWDADJ_BYTES)
     per_cell_step = seg_bytes / (float(SA) * n)
     # the same step counted by the passes of the reference's formulation
     # (each distinct array read and written once per pass): forward
-    # 53 + 14R words, adjoint 131 + 32R words of which 53 + 14R are the
-    # forward recompute, which this schedule (one segment, internals kept
-    # by the forward) does not run; FP32
-    pass_bytes = (131 + 32 * R) * 4.0
+    # 53 + 14R words and adjoint 131 + 32R words (which include the forward
+    # recompute this schedule runs for every segment but the last), FP32
+    pass_bytes = (184 + 46 * R) * 4.0
     step_roof = {"algorithmic_bytes_per_cell_step": per_cell_step,
                  "achieved_gbs": per_cell_step * value,
                  "frac": per_cell_step * value / roof["peak"],
                  "per_pass_accounting": {"bytes_per_cell_step": pass_bytes,
                                          "frac": pass_bytes * value / roof["peak"]},
-                 "note": "bytes: the launches of a profiled 4-step segment, each kernel's own algorithmic bytes; "
-                         "the 20-step segment's checkpoint and segment-state copies add 0.8 B/cell-step"}
+                 "kernel_share_ms": {k: round(v[1], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
+                 "note": "bytes: the launches of the profiled 10-step schedule (checkpoint every step), each "
+                         "kernel's own algorithmic bytes, per cell-step"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -776,18 +823,16 @@ def run_fwdadj(args):
                          "the reference has no adjoint)" % (g.ni, g.nj, g.nk, used)}
     if rank == 0:
         line = {
-            "metric": "Gcell-steps/s (batched FP32 level-set forward + adjoint: WENO3-RK3 + %d reinit pseudo-steps + "
-                      "FP64 volume; vs the plain FP64 GPU path)" % R,
+            "metric": FWDADJ_METRIC % R,
             "value": value, "unit": "Gcell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (analytic 3-D free surface and solitary-wave velocity; the reference "
                                     "ships no decks)",
-            "config": {"workload": "large_free_surface %dx%dx%d curvilinear, CFL 0.4, %d reinit pseudo-steps/step, "
-                                   "volume each step; one step = %d-step segment forward keeping its internals + "
-                                   "adjoint (checkpoint every %d steps: no recompute)" % (g.ni, g.nj, g.nk, R, S, S),
-                       "nodes": n, "physical_steps_per_step": S, "tile_shape": shape[1],
-                       "adjoint_mode": mode, "adjoint_state_gb": round(LevelSetBatch.adjoint_bytes(
-                           n, R, S, S, "fp32", mode) / 1e9, 1),
+            "config": {"workload": FWDADJ_WORKLOAD % (g.ni, g.nj, g.nk, NS, R, CK, -(-NS // CK) - 1),
+                       "nodes": n, "physical_steps_per_step": NS, "checkpoint_every": CK, "tile_shape": shape[1],
+                       "adjoint_mode": mode, "adjoint_state_gb": round(need / 1e9, 1),
+                       "mass_correction": {"target": target, "last_step": {"V": mstate[0], "dV_dC": mstate[1],
+                                                                           "C": mstate[2]}},
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "loss": "linear, seeded N(0,1) weights on phi_T",
                        "l2": "inputs larger than L2 (phi alone %.2f GB > 129 MB)" % (n * 4 / 1e9)},
@@ -797,9 +842,8 @@ def run_fwdadj(args):
             "fp64_gpu_path": {"value": v64, "unit": "Gcell-steps/s", "sample": "%d forward steps of the same grid, "
                               "lsm_levelsetmethod (reference FP64 arithmetic)" % (nc - 1),
                               "speedup_fp32_fwd_adj": value / v64},
-            "accuracy_vs_fp64": {"steps": nc, "band_linf_phi_err": band_err, "band": "|phi64| < 4 epslsm (6 cells)",
-                                 "volume_rel_diff": vol_err},
-            "e2e": {"value": e2e_value, "unit": "Gcell-steps/s", "h2d_bytes_per_step": 8 * n * (1 + 4 + 1),
+            "accuracy_vs_fp64": acc,
+            "e2e": {"value": e2e_value, "unit": "Gcell-steps/s", "h2d_bytes_per_step": 8 * n * (1 + 4 + 1) + 8,
                     "d2h_bytes_per_step": 8 * n * (1 + 1 + 4), "steps": e2e_steps,
                     "ms_per_call": {k: round(v, 1) for k, v in parts.items()}},
             "clocks": clocks.summary(),
@@ -1189,19 +1233,17 @@ def run_reference_fwdadj(args, world):
     warm = max(0, min(args.warmup, 3))
     sec, used = cpu_oracle_time(case, steps, threads, warm)
     v = case.grid.n / sec / 1e9
-    S = args.segment or W["segment"]
+    NS, CK = W["nsteps"], min(W["ckpt"], W["nsteps"])
     line = {
         "impl": "reference",
-        "metric": "Gcell-steps/s (batched FP32 level-set forward + adjoint: WENO3-RK3 + %d reinit pseudo-steps + "
-                  "FP64 volume; vs the plain FP64 GPU path)" % R,
+        "metric": FWDADJ_METRIC % R,
         "value": v, "unit": "Gcell-steps/s", "n_gpus": world, "steps": steps, "warmup": warm,
         "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": "large_free_surface %dx%dx%d curvilinear, CFL 0.4, %d reinit pseudo-steps/step, "
-                               "volume each step; one step = %d-step segment forward keeping its internals + "
-                               "adjoint (checkpoint every %d steps: no recompute)" % (W["ni"], W["nj"], W["nk"], R, S, S),
+        "config": {"workload": FWDADJ_WORKLOAD % (W["ni"], W["nj"], W["nk"], NS, R, CK, -(-NS // CK) - 1),
                    "nodes": case.grid.n,
-                   "timed": "one physical forward step of the whole grid per step (the reference has no adjoint)"},
+                   "timed": "one physical forward step of the whole grid per step (the reference has no adjoint "
+                            "and no mass correction in its Sussman branch)"},
         "cpu_baseline": {"value": v, "unit": "Gcell-steps/s", "cores": used, "kind": "port",
                          "sample": "%d physical forward steps of the whole grid; CPU FP64 restatement of the "
                                    "reference (the Fortran/MPI original cannot be built here: no Fortran compiler); "
@@ -1221,7 +1263,7 @@ def workload(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=None, help="timed steps (default 10 for fwdadj, else 30)")
+    ap.add_argument("--steps", type=int, default=None, help="timed steps (default 3 for fwdadj, else 30)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -1231,10 +1273,12 @@ def main():
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--n-inst", type=int, default=None, help="instances of the batched workload (profiling runs)")
     ap.add_argument("--segment", type=int, default=None,
-                    help="physical steps per benchmark step of the fwdadj workload (profiling runs)")
+                    help="checkpoint interval of the fwdadj workload (profiling runs)")
+    ap.add_argument("--nsteps", type=int, default=None,
+                    help="physical steps of the fwdadj workload's run (profiling runs)")
     args = ap.parse_args()
     if args.steps is None:
-        args.steps = 10 if args.workload == "fwdadj" else 30
+        args.steps = 3 if args.workload == "fwdadj" else 30
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":

@@ -29,6 +29,15 @@
  * frozen), giving dL/dphi^0 and dL/dq(2:4) (the velocity is held fixed over
  * the recorded steps).
  *
+ * Mass correction (config.mass_correction = 1; no counterpart in the
+ * reference's Sussman branch, whose GlobalMassCorrection, src/levelsetmethod.
+ * F90:245-266, feeds the geometric reinitialisation instead): after each
+ * step's final bcond_lsm, the FP64 water volume V of the result and its
+ * derivative A = dV/dC under a uniform shift phi + C are formed, and phi +=
+ * C with C = (target - V) / A (one Newton step towards the instance's
+ * target volume; instances without a target are not corrected).  The
+ * adjoint differentiates C exactly, including dA/dphi.
+ *
  * No counterpart exists in the reference, which advances one subdomain per
  * MPI rank and has no adjoint.
  */
@@ -60,6 +69,9 @@ typedef struct lsm_batch_config {
     int adjoint_mode;   /* 0: recorded pseudo-steps store their adjoint coefficients (6 arrays
                            each; the reverse sweep is a stencil), 1: the reverse sweep
                            recomputes them from the stored pseudo-step inputs (1 array each) */
+    int mass_correction;  /* 1: FP64 mass correction after every step towards the targets of
+                             lsm_batch_set_mass_target (the step's volume pass then measures the
+                             step's result instead of its input) */
 } lsm_batch_config;
 
 typedef struct lsm_batch* lsm_batch_handle;
@@ -81,8 +93,21 @@ int lsm_batch_get_phi(lsm_batch_handle h, int inst, double* phi);
 
 /* Advance every instance by `nsteps` physical steps.  `volumes` (nullable,
    host, 4*ninst doubles) receives each instance's pre-advection volumes of
-   the last step (K-tetrahedra, second tetrahedra, bulk, total). */
+   the last step (K-tetrahedra, second tetrahedra, bulk, total); with the
+   mass correction, the volumes of the last step's result before its
+   correction. */
 int lsm_batch_step(lsm_batch_handle h, int nsteps, double* volumes);
+
+/* Water volumes (K, S, bulk, total; host, 4*ninst doubles) of the current
+   phi of every instance. */
+int lsm_batch_water_volume(lsm_batch_handle h, double* volumes);
+/* Target water volume of one instance for the mass correction (NaN: no
+   correction of that instance; the default).  The adjoint treats it as a
+   constant.  LSM_ERR_BAD_PARAM when the batch has no mass correction. */
+int lsm_batch_set_mass_target(lsm_batch_handle h, int inst, double volume);
+/* The last step's mass correction per instance (host, 4*ninst doubles):
+   volume before the correction V, slope A = dV/dC, shift C, target. */
+int lsm_batch_mass_state(lsm_batch_handle h, double* out);
 
 /* Adjoint.  Run `nsteps` steps from the current phi (which becomes phi^0),
    keeping a checkpoint every `checkpoint_every` steps; the last segment
@@ -90,8 +115,9 @@ int lsm_batch_step(lsm_batch_handle h, int nsteps, double* volumes);
    last segment from those and each earlier one after recomputing it once
    from its checkpoint (keeping its internals); with nsteps <=
    checkpoint_every nothing is recomputed.  Device memory: N (ceil(nsteps /
-   k) + k (5 + c RNitermax) + 9) elements of the batch precision, k =
-   checkpoint_every, c = 6 (adjoint_mode 0) or 1 (adjoint_mode 1). */
+   k) + k (5 + m + c RNitermax) + 9) elements of the batch precision, k =
+   checkpoint_every, c = 6 (adjoint_mode 0) or 1 (adjoint_mode 1), m = 1
+   with the mass correction (which adds N 8-byte words of scratch) else 0. */
 int lsm_batch_forward_record(lsm_batch_handle h, int nsteps, int checkpoint_every);
 /* Seed dL/dphi at the end of the recorded steps for one instance (FP64, host
    or device; instances not seeded get zero). */

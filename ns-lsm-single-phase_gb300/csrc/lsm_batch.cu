@@ -35,6 +35,7 @@
 // and the sign field frozen (a 7-point stencil on lam with coefficients the
 // recorded forward step stored, or recomputed from its input); the
 // contravariant-velocity chain rule.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -178,12 +179,17 @@ __global__ void __launch_bounds__(TX * TY * TZ) k_contra(const Inst* __restrict_
 // their faces from bcond_lsm afterwards.  Halo slots: threads 0..127 hold the y-halo rows
 // -2, -1, 8, 9 of the tile, threads 128..159 the x-halo columns -2, -1, 32,
 // 33 (the cross stencil needs no corners).
+// The z face k-1/2 of a node is the z face k+1/2 of the node below it with
+// the same stencil whenever their upwind choices agree (M at k equals P at
+// k - 1): that reconstruction is carried from the previous plane, and a
+// warp skips the recomputation when all its lanes can reuse it.
 constexpr int kStSX = 36, kStSY = 12;
 template <typename T>
 __global__ void __launch_bounds__(256) k_stage_z(const Inst* __restrict__ inst, const Brick* __restrict__ bmap,
         int nb, FieldsT<T> f, const T* __restrict__ phin, const T* __restrict__ phi1, T* __restrict__ out, T c1, T c2,
         T c3) {
     __shared__ T pl[2][kStSY][kStSX];
+    const unsigned FM = 0xffffffffu;
     const int t = threadIdx.x, tx = t & 31, ty = t >> 5;
     int hx = 0, hy = 0;
     if (t < 128) {
@@ -221,6 +227,9 @@ __global__ void __launch_bounds__(256) k_stage_z(const Inst* __restrict__ inst, 
             W2 = __ldg(f.W[2] + l);
             pn = __ldg(phin + l);
         }
+        // the z face k - 1/2 carried from the previous plane (Pz: its stencil choice)
+        T fpz = T(0);
+        bool Pz = false, have = false;
         for (int k = k0; k < k1; ++k) {
             // loads of plane k + 1 (window plane k + 3) go out first
             const bool nx = k + 1 < k1;
@@ -239,19 +248,35 @@ __global__ void __launch_bounds__(256) k_stage_z(const Inst* __restrict__ inst, 
             P[ty + 2][tx + 2] = w2;
             if (has_h) P[hy + 2][hx + 2] = hv;
             __syncthreads();
+            const bool interior = col && ij_int && k > 0 && k < nk - 1;
+            // z stencil choices (weno_diff's P and M)
+            const bool upz = W2 > T(0);
+            const bool Pk = upz || k == nk - 2, Mk = upz && k != 1;
+            const bool reuse = !interior || (have && Mk == Pz);
+            const bool all_reuse = __all_sync(FM, reuse);
             if (col) {
                 T R = T(0);
-                if (ij_int && k > 0 && k < nk - 1) {
+                if (interior) {
                     const int x = tx + 2, y = ty + 2;
                     R = W0 * weno_diff(i > 1 ? P[y][x - 2] : T(0), P[y][x - 1], w2, P[y][x + 1],
                                        i < ni - 2 ? P[y][x + 2] : T(0), W0, i == 1, i == ni - 2);
                     R = vfma(W1, weno_diff(j > 1 ? P[y - 2][x] : T(0), P[y - 1][x], w2, P[y + 1][x],
                                            j < nj - 2 ? P[y + 2][x] : T(0), W1, j == 1, j == nj - 2), R);
-                    R = vfma(W2, weno_diff(k > 1 ? w0 : T(0), w1, w2, w3, k < nk - 2 ? w4 : T(0), W2, k == 1,
-                                           k == nk - 2), R);
+                    const T p2 = k < nk - 2 ? w4 : T(0);
+                    const T fp = rec3(Pk ? w1 : p2, Pk ? w2 : w3, Pk ? w3 : w2);
+                    T fm = fpz;
+                    if (!all_reuse) {
+                        const T m2 = k > 1 ? w0 : T(0);
+                        const T g = rec3(Mk ? m2 : w3, Mk ? w1 : w2, Mk ? w2 : w1);
+                        if (!reuse) fm = g;
+                    }
+                    R = vfma(W2, fp - fm, R);
+                    fpz = fp;
+                    Pz = Pk;
                 }
                 out[cb + sk * k] = c1 * pn + c2 * w2 - c3 * R;
             }
+            have = interior;
             w0 = w1;
             w1 = w2;
             w2 = w3;
@@ -262,6 +287,182 @@ __global__ void __launch_bounds__(256) k_stage_z(const Inst* __restrict__ inst, 
             W1 = W1n;
             W2 = W2n;
             pn = pnn;
+        }
+    }
+}
+
+// ------------------------------------------------------------ TMA staging
+// Tensor-memory-accelerator copies of one tile per plane into shared memory
+// (cp.async.bulk.tensor), completion tracked by an mbarrier whose phase the
+// threads wait on, each wait bounded (kErrTimeout after kTmaSpins polls).
+constexpr int kTmaSpins = 1 << 20;
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait for phase `parity` of `bar`; false when it gave up
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+    for (int it = 0; it < kTmaSpins; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// 4-D tiled load (x, y, z, array) of the map's box into dst, completing on bar
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int x, int y, int z, int a,
+                                            unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(a), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// RK stage (FP32) with the plane tiles staged by TMA: the same arithmetic,
+// tiles and z window as k_stage_z, for a batch of one instance whose rows
+// are whole 16-byte units (ni a multiple of 4).  The stage input phi1 is
+// array `a_in` of the 4-D tensor map `tm` ((ni, nj, nk, arrays), the
+// arena's arrays ld apart).  Per plane one thread issues the copy of a 40 x
+// 12 box starting at (i0 - 4, j0 - 2): x rounded down to a 16-byte boundary,
+// a two-node halo on every side, the out-of-range part zero-filled by the
+// copy engine.  Three buffers; the copy of plane k + 2 is issued (after the
+// plane barrier that frees its buffer) while plane k is computed.
+constexpr int kTmaBX = 40, kTmaBY = 12, kTmaBuf = 3;
+__global__ void __launch_bounds__(256) k_stage_tma(const __grid_constant__ CUtensorMap tm, int a_in,
+        const Inst* __restrict__ inst, const Brick* __restrict__ bmap, int nb, FieldsT<float> f,
+        const float* __restrict__ phin, const float* __restrict__ phi1, float* __restrict__ out, float c1, float c2,
+        float c3, unsigned* __restrict__ err) {
+    __shared__ __align__(128) float pl[kTmaBuf][kTmaBY][kTmaBX];
+    __shared__ __align__(8) unsigned long long bar[kTmaBuf];
+    __shared__ int abort_flag;
+    const unsigned FM = 0xffffffffu;
+    const int t = threadIdx.x, tx = t & 31, ty = t >> 5;
+    constexpr unsigned kBytes = kTmaBX * kTmaBY * sizeof(float);
+    if (t == 0) {
+        for (int b = 0; b < kTmaBuf; ++b) mbar_init(&bar[b], 1);
+        abort_flag = 0;
+        mbar_fence_init();
+    }
+    __syncthreads();
+    unsigned issued = 0, used = 0;   // copies issued / planes consumed by this CTA (same on every thread)
+    const Inst& I = inst[0];
+    const int ni = I.ni, nj = I.nj, nk = I.nk;
+    const long long sk = (long long)ni * nj;
+    auto issue = [&](int i0, int j0, int k) {
+        if (t == 0) {
+            unsigned long long* b = &bar[issued % kTmaBuf];
+            mbar_expect_tx(b, kBytes);
+            tma_load_4d(&pl[issued % kTmaBuf][0][0], &tm, i0 - 4, j0 - 2, k, a_in, b);
+        }
+        ++issued;
+    };
+    bool aborted = false;
+    for (int blk = blockIdx.x; blk < nb && !aborted; blk += gridDim.x) {
+        const ABrick ab = adj_brick(bmap, 2, blk);
+        const int i = ab.i0 + tx, j = ab.j0 + ty;
+        const int k0 = ab.k0, k1 = min(k0 + adj_shape(2).oz, nk);
+        const bool col = i < ni && j < nj;
+        const long long cb = i + (long long)ni * j;
+        const bool ij_int = i > 0 && i < ni - 1 && j > 0 && j < nj - 1;
+        // the first two planes of the tile
+        issue(ab.i0, ab.j0, k0);
+        if (k0 + 1 < k1) issue(ab.i0, ab.j0, k0 + 1);
+        auto own = [&](int k) { return col && k >= 0 && k < nk ? __ldg(phi1 + cb + sk * k) : 0.f; };
+        float w0 = own(k0 - 2), w1 = own(k0 - 1), w2 = own(k0), w3 = own(k0 + 1), w4 = own(k0 + 2);
+        float W0 = 0.f, W1 = 0.f, W2 = 0.f, pn = 0.f;
+        if (col) {
+            const long long l = cb + sk * k0;
+            W0 = __ldg(f.W[0] + l);
+            W1 = __ldg(f.W[1] + l);
+            W2 = __ldg(f.W[2] + l);
+            pn = __ldg(phin + l);
+        }
+        float fpz = 0.f;
+        bool Pz = false, have = false;
+        for (int k = k0; k < k1; ++k) {
+            const bool nx = k + 1 < k1;
+            const float w5 = nx ? own(k + 3) : 0.f;
+            float W0n = 0.f, W1n = 0.f, W2n = 0.f, pnn = 0.f;
+            if (col && nx) {
+                const long long l = cb + sk * (k + 1);
+                W0n = __ldg(f.W[0] + l);
+                W1n = __ldg(f.W[1] + l);
+                W2n = __ldg(f.W[2] + l);
+                pnn = __ldg(phin + l);
+            }
+            const unsigned slot = used % kTmaBuf, par = (used / kTmaBuf) & 1u;
+            ++used;
+            if (!mbar_wait(&bar[slot], par)) abort_flag = 1;
+            const float (*P)[kTmaBX] = pl[slot];
+            const bool interior = col && ij_int && k > 0 && k < nk - 1;
+            const bool upz = W2 > 0.f;
+            const bool Pk = upz || k == nk - 2, Mk = upz && k != 1;
+            const bool reuse = !interior || (have && Mk == Pz);
+            const bool all_reuse = __all_sync(FM, reuse);
+            if (col) {
+                float R = 0.f;
+                if (interior) {
+                    const int x = tx + 4, y = ty + 2;
+                    R = W0 * weno_diff(i > 1 ? P[y][x - 2] : 0.f, P[y][x - 1], w2, P[y][x + 1],
+                                       i < ni - 2 ? P[y][x + 2] : 0.f, W0, i == 1, i == ni - 2);
+                    R = vfma(W1, weno_diff(j > 1 ? P[y - 2][x] : 0.f, P[y - 1][x], w2, P[y + 1][x],
+                                           j < nj - 2 ? P[y + 2][x] : 0.f, W1, j == 1, j == nj - 2), R);
+                    const float p2 = k < nk - 2 ? w4 : 0.f;
+                    const float fp = rec3(Pk ? w1 : p2, Pk ? w2 : w3, Pk ? w3 : w2);
+                    float fm = fpz;
+                    if (!all_reuse) {
+                        const float m2 = k > 1 ? w0 : 0.f;
+                        const float g = rec3(Mk ? m2 : w3, Mk ? w1 : w2, Mk ? w2 : w1);
+                        if (!reuse) fm = g;
+                    }
+                    R = vfma(W2, fp - fm, R);
+                    fpz = fp;
+                    Pz = Pk;
+                }
+                out[cb + sk * k] = c1 * pn + c2 * w2 - c3 * R;
+            }
+            have = interior;
+            // every thread is done with this plane's buffer: it takes plane k + 2
+            __syncthreads();
+            if (abort_flag) {
+                aborted = true;
+                break;
+            }
+            if (k + 2 < k1) issue(ab.i0, ab.j0, k + 2);
+            w0 = w1;
+            w1 = w2;
+            w2 = w3;
+            w3 = w4;
+            w4 = w5;
+            W0 = W0n;
+            W1 = W1n;
+            W2 = W2n;
+            pn = pnn;
+        }
+    }
+    if (aborted && t == 0) {
+        atomicOr(err, (unsigned)kErrTimeout);
+        // let the copies still in flight land before the CTA's shared memory goes away
+        while (used < issued) {
+            mbar_wait(&bar[used % kTmaBuf], (used / kTmaBuf) & 1u);
+            ++used;
         }
     }
 }
@@ -753,21 +954,108 @@ __device__ __forceinline__ X sel4(const X (&a)[4], int i) {
     return i == 0 ? a[0] : (i == 1 ? a[1] : (i == 2 ? a[2] : a[3]));
 }
 
-template <typename G>
-__device__ __forceinline__ G tet_water(const G (&V)[4][3], const G (&ph)[4]) {
+// ------------------------------------------------------------ dual numbers
+// Forward-mode derivatives of the tetrahedron water volume with respect to
+// its vertex values (the mass correction and its adjoint): a value and K
+// partials; S is a scalar or itself a Dual (second derivatives).
+template <typename S, int K>
+struct Dual {
+    S v;
+    S d[K];
+};
+template <typename X> struct DualTraits { using Base = X; };
+template <typename S, int K> struct DualTraits<Dual<S, K>> { using Base = typename DualTraits<S>::Base; };
+template <typename X> __device__ __forceinline__ typename DualTraits<X>::Base dval(const X& x) { return x; }
+template <typename S, int K> __device__ __forceinline__ typename DualTraits<S>::Base dval(const Dual<S, K>& x) {
+    return dval(x.v);
+}
+// constant (all partials zero)
+template <typename X> struct Lift { __device__ static X of(typename DualTraits<X>::Base c) { return X(c); } };
+template <typename S, int K> struct Lift<Dual<S, K>> {
+    __device__ static Dual<S, K> of(typename DualTraits<S>::Base c) {
+        Dual<S, K> r;
+        r.v = Lift<S>::of(c);
+#pragma unroll
+        for (int k = 0; k < K; ++k) r.d[k] = Lift<S>::of(typename DualTraits<S>::Base(0));
+        return r;
+    }
+};
+template <typename S, int K>
+__device__ __forceinline__ Dual<S, K> operator+(const Dual<S, K>& a, const Dual<S, K>& b) {
+    Dual<S, K> r;
+    r.v = a.v + b.v;
+#pragma unroll
+    for (int k = 0; k < K; ++k) r.d[k] = a.d[k] + b.d[k];
+    return r;
+}
+template <typename S, int K>
+__device__ __forceinline__ Dual<S, K> operator-(const Dual<S, K>& a, const Dual<S, K>& b) {
+    Dual<S, K> r;
+    r.v = a.v - b.v;
+#pragma unroll
+    for (int k = 0; k < K; ++k) r.d[k] = a.d[k] - b.d[k];
+    return r;
+}
+template <typename S, int K>
+__device__ __forceinline__ Dual<S, K> operator-(const Dual<S, K>& a) {
+    Dual<S, K> r;
+    r.v = -a.v;
+#pragma unroll
+    for (int k = 0; k < K; ++k) r.d[k] = -a.d[k];
+    return r;
+}
+template <typename S, int K>
+__device__ __forceinline__ Dual<S, K> operator*(const Dual<S, K>& a, const Dual<S, K>& b) {
+    Dual<S, K> r;
+    r.v = a.v * b.v;
+#pragma unroll
+    for (int k = 0; k < K; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
+    return r;
+}
+template <typename S, int K>
+__device__ __forceinline__ Dual<S, K> operator/(const Dual<S, K>& a, const Dual<S, K>& b) {
+    Dual<S, K> r;
+    r.v = a.v / b.v;
+#pragma unroll
+    for (int k = 0; k < K; ++k) r.d[k] = (a.d[k] - r.v * b.d[k]) / b.v;
+    return r;
+}
+// scalar (geometry) factor times a dual
+template <typename S, int K>
+__device__ __forceinline__ Dual<S, K> operator*(typename DualTraits<S>::Base c, const Dual<S, K>& a) {
+    Dual<S, K> r;
+    r.v = c * a.v;
+#pragma unroll
+    for (int k = 0; k < K; ++k) r.d[k] = c * a.d[k];
+    return r;
+}
+template <typename S, int K>
+__device__ __forceinline__ Dual<S, K> operator-(typename DualTraits<S>::Base c, const Dual<S, K>& a) {
+    return Lift<Dual<S, K>>::of(c) - a;
+}
+
+// Water (phi > 0) volume of one tetrahedron with vertices V and vertex
+// values ph (the reference's MarchingTetrahedron + GetWaterVolume cases,
+// src/TetrahedronMethods.F90:586-954, in closed form).  X is the vertex
+// value type: the geometry type G, or a Dual of it for the derivatives with
+// respect to the vertex values (the case chosen by the values themselves).
+template <typename G, typename X>
+__device__ __forceinline__ X tet_water_x(const G (&V)[4][3], const X (&ph)[4]) {
     const G TV = tetvol_g(V[0], V[1], V[2], V[3]);
     const G tiny = G(sizeof(G) == 8 ? kTinyD : 0.0);   // tiny(1d0); in FP32 every nonzero value exceeds it
+    const X zero = Lift<X>::of(G(0)), one = Lift<X>::of(G(1)), full = Lift<X>::of(TV);
     int s[4], nz = 0, fi = 0;
     bool allp = true, alln = true, allge = true, allle = true;
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-        s[v] = ph[v] > tiny ? 1 : (ph[v] < -tiny ? -1 : 0);
+        const G pv = dval(ph[v]);
+        s[v] = pv > tiny ? 1 : (pv < -tiny ? -1 : 0);
         allp &= s[v] == 1; alln &= s[v] == -1; nz += s[v] == 0;
         allge &= s[v] >= 0; allle &= s[v] <= 0;
         if (s[v] == -1) fi |= 1 << v;
     }
-    if (allp) return TV;
-    if (alln) return G(0);
+    if (allp) return full;
+    if (alln) return zero;
     if (nz > 0 && (allge || allle)) {
         // the reference's zero-vertex cases: full or empty tetrahedron
         int water = -1;
@@ -786,7 +1074,7 @@ __device__ __forceinline__ G tet_water(const G (&V)[4][3], const G (&ph)[4]) {
             for (int v = 0; v < 4; ++v)
                 if (water < 0 && s[v] != 0) water = s[v] == 1;   // the non-zero vertex
         }
-        return water == 0 ? G(0) : TV;   // four zero vertices: full (FlagIndex 0)
+        return water == 0 ? zero : full;   // four zero vertices: full (FlagIndex 0)
     }
     // one vertex isolated from the other three (cases 2/15, 3/14, 5/12, 9/8)
     int iso = -1;
@@ -796,14 +1084,14 @@ __device__ __forceinline__ G tet_water(const G (&V)[4][3], const G (&ph)[4]) {
         // prod_k p_iso / (p_iso - p_k) over one division (the differences
         // all carry the sign of p_iso: no cancellation); the factor of k =
         // iso is an exact 1
-        const G pI = sel4(ph, iso);
-        G num = G(1), den = G(1);
+        const X pI = sel4(ph, iso);
+        X num = one, den = one;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            num *= k != iso ? pI : G(1);
-            den *= k != iso ? pI - ph[k] : G(1);
+            num = num * (k != iso ? pI : one);
+            den = den * (k != iso ? pI - ph[k] : one);
         }
-        const G AV = TV * (num / den);
+        const X AV = TV * (num / den);
         return (sel4(s, iso) == -1) ? TV - AV : AV;   // isolated vertex negative: the rest is water
     }
     // two against two (cases 4/13, 6/11, 7/10): pair (A, B) as listed by the
@@ -815,14 +1103,19 @@ __device__ __forceinline__ G tet_water(const G (&V)[4][3], const G (&ph)[4]) {
     // denominator (pA - pC)(pA - pD)(pB - pC)(pB - pD), using 1 - bX =
     // -pX / (pB - pX), it needs one division, and its three numerator terms
     // share one sign (A, B on one side of the interface, C, D on the other)
-    const G pA = cs == 2 ? ph[1] : ph[0];
-    const G pB = cs == 0 ? ph[1] : ph[2];
-    const G pC = cs == 0 ? ph[2] : (cs == 1 ? ph[1] : ph[0]);
-    const G pD = ph[3];
-    const G dAC = pA - pC, dAD = pA - pD, dBC = pB - pC, dBD = pB - pD;
-    const G num = pB * pB * dAC * dAD - pA * pA * pD * dBC - pA * pB * pC * dAD;
-    const G AV = TV * (num / (dAC * dAD * dBC * dBD));
+    const X pA = cs == 2 ? ph[1] : ph[0];
+    const X pB = cs == 0 ? ph[1] : ph[2];
+    const X pC = cs == 0 ? ph[2] : (cs == 1 ? ph[1] : ph[0]);
+    const X pD = ph[3];
+    const X dAC = pA - pC, dAD = pA - pD, dBC = pB - pC, dBD = pB - pD;
+    const X num = pB * pB * dAC * dAD - pA * pA * pD * dBC - pA * pB * pC * dAD;
+    const X AV = TV * (num / (dAC * dAD * dBC * dBD));
     return ((cs == 2 ? s[1] : s[0]) == -1) ? TV - AV : AV;
+}
+
+template <typename G>
+__device__ __forceinline__ G tet_water(const G (&V)[4][3], const G (&ph)[4]) {
+    return tet_water_x<G, G>(V, ph);
 }
 
 // vertex v of tetrahedron t of CellAnalysis's split (the c_tets table
@@ -835,17 +1128,33 @@ __host__ __device__ constexpr int cell_tet(int t, int v) {
                                     : (t == 0 ? 1 : t == 1 ? 2 : t == 2 ? 3 : t == 3 ? 7 : t == 4 ? 4 : 5);
 }
 
-// CellAnalysis's split of an interface cell (src/TetrahedronMethods.F90:
-// 1823-2121): phase-change tetrahedra -> K, all-water tetrahedra -> S.
-// The classification runs in the phi type P (eps_sims = 2^-52 and +-1 are
-// exact in FP32, so its compares equal the FP64 ones on the same values),
-// the geometry in P as well, on vertex coordinates relative to the cell's
-// first vertex (C, formed in FP64 by the caller).  Fully unrolled: every
-// array index is a constant (no local memory).
+// CellAnalysis's tetrahedron classes: pct (phase change, a K tetrahedron)
+// or second (all water); the phi-type compares equal the FP64 ones.
 template <typename P>
-__device__ void cell_water_fast(const P (&ph8)[8], const P (&C)[8][3], double* K, double* S) {
+__device__ __forceinline__ void tet_class(const P (&ph8)[8], int t, bool* pct_out, bool* second_out) {
     const P es = P(kEpsSims);
-    P k = P(0), s2 = P(0);
+    bool pct = false, second = true;
+    const P pa = ph8[cell_tet(t, 0)];
+    if (pa <= es) second = false;
+    if (fabs(pa) < es) pct = true;
+    const P sg = signbit(pa) ? P(-1) : P(1);
+#pragma unroll
+    for (int v = 1; v < 4; ++v) {
+        const P pb = ph8[cell_tet(t, v)];
+        if (sg * pb < P(0) || fabs(pb) < es) {
+            if (pb <= es) second = false;
+            pct = true;
+        }
+    }
+    *pct_out = pct;
+    *second_out = second;
+}
+
+// whether CellAnalysis splits the cell (a vertex within eps_sims of zero or
+// a sign change)
+template <typename P>
+__device__ __forceinline__ bool cell_is_interface(const P (&ph8)[8]) {
+    const P es = P(kEpsSims);
     bool pcc = false;
 #pragma unroll
     for (int v = 0; v < 8; ++v) pcc |= fabs(ph8[v]) < es;
@@ -854,22 +1163,26 @@ __device__ void cell_water_fast(const P (&ph8)[8], const P (&C)[8][3], double* K
 #pragma unroll
         for (int v = 1; v < 8; ++v) pcc |= sg * ph8[v] < P(0);
     }
-    if (pcc) {
+    return pcc;
+}
+
+// CellAnalysis's split of an interface cell (src/TetrahedronMethods.F90:
+// 1823-2121): phase-change tetrahedra -> K, all-water tetrahedra -> S.
+// The classification runs in the phi type P (eps_sims = 2^-52 and +-1 are
+// exact in FP32, so its compares equal the FP64 ones on the same values),
+// the geometry in P as well, on vertex coordinates relative to the cell's
+// first vertex (C, formed in FP64 by the caller).  Fully unrolled: every
+// array index is a constant (no local memory).  With SLOPE, *A also gets
+// dK/dC, the derivative of the K volume under a uniform shift phi + C
+// (forward-mode dual numbers through the same case formulas).
+template <typename P, bool SLOPE = false>
+__device__ void cell_water_fast(const P (&ph8)[8], const P (&C)[8][3], double* K, double* S, double* A = nullptr) {
+    P k = P(0), s2 = P(0), a = P(0);
+    if (cell_is_interface(ph8)) {
 #pragma unroll
         for (int t = 0; t < 6; ++t) {
-            bool pct = false, second = true;
-            const P pa = ph8[cell_tet(t, 0)];
-            if (pa <= es) second = false;
-            if (fabs(pa) < es) pct = true;
-            const P sg = signbit(pa) ? P(-1) : P(1);
-#pragma unroll
-            for (int v = 1; v < 4; ++v) {
-                const P pb = ph8[cell_tet(t, v)];
-                if (sg * pb < P(0) || fabs(pb) < es) {
-                    if (pb <= es) second = false;
-                    pct = true;
-                }
-            }
+            bool pct, second;
+            tet_class(ph8, t, &pct, &second);
             if (pct || second) {
                 P V[4][3], ph[4];
 #pragma unroll
@@ -879,12 +1192,66 @@ __device__ void cell_water_fast(const P (&ph8)[8], const P (&C)[8][3], double* K
                     V[v][2] = C[cell_tet(t, v)][2];
                     ph[v] = ph8[cell_tet(t, v)];
                 }
-                if (pct) k += tet_water(V, ph);
-                else s2 += tetvol_g(V[0], V[1], V[2], V[3]);
+                if (pct) {
+                    if constexpr (SLOPE) {
+                        Dual<P, 1> pd[4];
+#pragma unroll
+                        for (int v = 0; v < 4; ++v) {
+                            pd[v].v = ph[v];
+                            pd[v].d[0] = P(1);
+                        }
+                        const Dual<P, 1> w = tet_water_x<P, Dual<P, 1>>(V, pd);
+                        k += w.v;
+                        a += w.d[0];
+                    } else {
+                        k += tet_water(V, ph);
+                    }
+                } else {
+                    s2 += tetvol_g(V[0], V[1], V[2], V[3]);
+                }
             }
         }
     }
     *K = (double)k; *S = (double)s2;
+    if (A) *A = (double)a;
+}
+
+// Mass-correction adjoint weights of one interface cell: for each vertex v
+// the derivative of the cell's K volume g_v = dK/dphi_v plus Cs h_v with
+// h_v = d(dK/dC)/dphi_v (second-order dual numbers), so that the shift
+// C = (target - V) / A has dC/dphi_v = -(g_v + C h_v) / A summed over the
+// cells around the node.
+template <typename P>
+__device__ void cell_mass_weights(const P (&ph8)[8], const P (&C)[8][3], P Cs, P (&w8)[8]) {
+#pragma unroll
+    for (int v = 0; v < 8; ++v) w8[v] = P(0);
+    if (!cell_is_interface(ph8)) return;
+    using D1 = Dual<P, 1>;
+    using D2 = Dual<D1, 4>;
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+        bool pct, second;
+        tet_class(ph8, t, &pct, &second);
+        if (!pct) continue;
+        P V[4][3];
+        D2 pd[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            V[v][0] = C[cell_tet(t, v)][0];
+            V[v][1] = C[cell_tet(t, v)][1];
+            V[v][2] = C[cell_tet(t, v)][2];
+            pd[v].v.v = ph8[cell_tet(t, v)];
+            pd[v].v.d[0] = P(1);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                pd[v].d[u].v = u == v ? P(1) : P(0);
+                pd[v].d[u].d[0] = P(0);
+            }
+        }
+        const D2 r = tet_water_x<P, D2>(V, pd);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) w8[cell_tet(t, u)] += r.d[u].v + Cs * r.d[u].d[0];
+    }
 }
 
 // Cells are classified against eps_sims = 2^-52 in the phi type.  Bulk
@@ -909,23 +1276,25 @@ __device__ __forceinline__ long long warp_sum_nn(long long v) {
     return (long long)(s0 + (s1 << 22) + (s2 << 44));
 }
 
-template <typename T, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(TX * TY * TZ) k_volume(const Inst* __restrict__ inst,
-        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phi,
-        unsigned long long* __restrict__ acc) {
+// Each instance has four accumulators: K, S, bulk and (SLOPE) the slope
+// A = dK/dC of the mass correction, all in the same fixed point.
+template <typename T, int TX, int TY, int TZ, bool SLOPE>
+__device__ __forceinline__ void volume_body(const Inst* __restrict__ inst, const Brick* __restrict__ bricks,
+                                            int nbricks, const FieldsT<T>& f, const T* __restrict__ phi,
+                                            unsigned long long* __restrict__ acc) {
     constexpr int NW = TX * TY * TZ / 32;
     const T eps = T(kEpsSims);
     __shared__ long long slot[NW][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    long long Kq = 0, Sq = 0, Bq = 0;
+    long long Kq = 0, Sq = 0, Bq = 0, Aq = 0;
     int cur = -1;
     // warp-uniform (every thread of the CTA walks the same bricks)
     auto flush = [&]() {
-        const long long v[3] = {warp_sum_nn(Kq), warp_sum_nn(Sq), warp_sum_nn(Bq)};
+        const long long v[4] = {warp_sum_nn(Kq), warp_sum_nn(Sq), warp_sum_nn(Bq), SLOPE ? warp_sum_nn(Aq) : 0};
         if (lane == 0)
-            for (int c = 0; c < 3; ++c)
-                if (v[c] != 0) atomicAdd(acc + 3 * (long long)cur + c, (unsigned long long)v[c]);
-        Kq = Sq = Bq = 0;
+            for (int c = 0; c < 4; ++c)
+                if (v[c] != 0) atomicAdd(acc + 4 * (long long)cur + c, (unsigned long long)v[c]);
+        Kq = Sq = Bq = Aq = 0;
     };
     for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
         const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
@@ -973,10 +1342,11 @@ __global__ void __launch_bounds__(TX * TY * TZ) k_volume(const Inst* __restrict_
 #pragma unroll
                     for (int a = 0; a < 3; ++a) C[v][a] = (T)(__ldg(f.xyz[a] + o[v]) - X0[a]);
                 }
-                double K = 0.0, S = 0.0;
-                cell_water_fast(P8, C, &K, &S);
+                double K = 0.0, S = 0.0, A = 0.0;
+                cell_water_fast<T, SLOPE>(P8, C, &K, &S, &A);
                 Kq += __double2ll_rn(K * kVolScale);
                 Sq += __double2ll_rn(S * kVolScale);
+                if (SLOPE) Aq += __double2ll_rn(A * kVolScale);
             }
             __syncwarp();
         }
@@ -984,20 +1354,188 @@ __global__ void __launch_bounds__(TX * TY * TZ) k_volume(const Inst* __restrict_
     if (cur >= 0) flush();
 }
 
-// converts each instance's accumulators (K, S, bulk) to volumes and clears
-// them for the next launch of k_volume
-__global__ void k_volume_final(int ninst, unsigned long long* __restrict__ acc, double* __restrict__ vols) {
+template <typename T, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(TX * TY * TZ) k_volume(const Inst* __restrict__ inst,
+        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phi,
+        unsigned long long* __restrict__ acc) {
+    volume_body<T, TX, TY, TZ, false>(inst, bricks, nbricks, f, phi, acc);
+}
+// the same with the mass correction's slope dK/dC
+template <typename T, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(TX * TY * TZ) k_volume_slope(const Inst* __restrict__ inst,
+        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phi,
+        unsigned long long* __restrict__ acc) {
+    volume_body<T, TX, TY, TZ, true>(inst, bricks, nbricks, f, phi, acc);
+}
+
+// converts each instance's accumulators (K, S, bulk, slope) to volumes and
+// clears them for the next launch of k_volume; with `mass` it also forms the
+// mass correction C = (target - V) / A of the total V (C = 0 without a
+// finite target or without interface), into mass[q] and, when recording,
+// mrec[q]
+__global__ void k_volume_final(int ninst, unsigned long long* __restrict__ acc, double* __restrict__ vols,
+                               const double* __restrict__ target, Mass* __restrict__ mass, Mass* __restrict__ mrec) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= ninst) return;
-    long long v[3];
-    for (int c = 0; c < 3; ++c) {
-        v[c] = (long long)acc[3 * q + c];
-        acc[3 * q + c] = 0ull;
+    long long v[4];
+    for (int c = 0; c < 4; ++c) {
+        v[c] = (long long)acc[4 * q + c];
+        acc[4 * q + c] = 0ull;
     }
+    const double tot = (double)(v[0] + v[1] + v[2]) * kVolUnit;
     vols[4 * q] = (double)v[0] * kVolUnit;
     vols[4 * q + 1] = (double)v[1] * kVolUnit;
     vols[4 * q + 2] = (double)v[2] * kVolUnit;
-    vols[4 * q + 3] = (double)(v[0] + v[1] + v[2]) * kVolUnit;
+    vols[4 * q + 3] = tot;
+    if (mass) {
+        Mass m;
+        m.V = tot;
+        m.A = (double)v[3] * kVolUnit;
+        m.target = target[q];
+        const double c = (target[q] - tot) / m.A;
+        m.C = mass_on(m) ? c : 0.0;
+        mass[q] = m;
+        if (mrec) mrec[q] = m;
+    }
+}
+
+// dst = src + C of the node's instance (the mass correction's uniform shift)
+template <typename T>
+__global__ void k_mass_shift(Flat fl, const Mass* __restrict__ mass, const T* __restrict__ src, T* __restrict__ dst) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < fl.n;
+         t += (long long)gridDim.x * blockDim.x) {
+        Node nd;
+        flat_node(fl, t, &nd);
+        dst[t] = src[t] + (T)mass[nd.inst].C;
+    }
+}
+
+// Adjoint of the shift, part 1: every interface cell of the step's
+// pre-correction field adds its vertices' weights g_v + C h_v
+// (cell_mass_weights) to wfix in fixed point (integer atomics: exact and
+// order-independent).  Same brick walk and warp packing as k_volume.
+template <typename T, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(TX * TY * TZ) k_mass_weights(const Inst* __restrict__ inst,
+        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phi,
+        const Mass* __restrict__ mass, unsigned long long* __restrict__ wfix) {
+    constexpr int NW = TX * TY * TZ / 32;
+    const T eps = T(kEpsSims);
+    __shared__ long long slot[NW][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
+        const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
+        const Inst& I = inst[b.inst];
+        const Mass M = mass[b.inst];
+        const long long sj = I.ni, sk = (long long)I.ni * I.nj;
+        bool mix = false;
+        long long l = 0;
+        if (mass_on(M) && b.i < I.ni - 1 && b.j < I.nj - 1 && b.k < I.nk - 1) {
+            l = I.off + b.i + sj * b.j + sk * b.k;
+            const long long o[8] = {l, l + 1, l + 1 + sj, l + sj, l + sk, l + 1 + sk, l + 1 + sj + sk, l + sj + sk};
+            bool allw = true, alla = true;
+#pragma unroll
+            for (int v = 0; v < 8; ++v) {
+                const T p = __ldg(phi + o[v]);
+                allw &= p > eps; alla &= p < -eps;
+            }
+            mix = !allw && !alla;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, mix);
+        if (m) {
+            if (mix) slot[w][__popc(m & ((1u << lane) - 1u))] = l;
+            __syncwarp();
+            if (lane < __popc(m)) {
+                const long long c = slot[w][lane];
+                const long long o[8] = {c, c + 1, c + 1 + sj, c + sj, c + sk, c + 1 + sk, c + 1 + sj + sk,
+                                        c + sj + sk};
+                T P8[8], C[8][3], W8[8];
+                double X0[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) X0[a] = __ldg(f.xyz[a] + c);
+#pragma unroll
+                for (int v = 0; v < 8; ++v) {
+                    P8[v] = __ldg(phi + o[v]);
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) C[v][a] = (T)(__ldg(f.xyz[a] + o[v]) - X0[a]);
+                }
+                cell_mass_weights<T>(P8, C, (T)M.C, W8);
+#pragma unroll
+                for (int v = 0; v < 8; ++v) {
+                    const long long q = __double2ll_rn((double)W8[v] * kVolScale);
+                    if (q != 0) atomicAdd(wfix + o[v], (unsigned long long)q);
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// Adjoint of the shift, part 2: per tile of adjoint map 2 (32 x 8 columns
+// x 32 planes, inside one instance) the FP64 sum of lam over the tile, in a
+// fixed order (each thread its column, then a fixed tree)
+template <typename T>
+__global__ void __launch_bounds__(256) k_tile_sum(const Inst* __restrict__ inst, const Brick* __restrict__ bmap,
+                                                   int nb, const T* __restrict__ lam, double* __restrict__ part) {
+    __shared__ double red[8];
+    const int t = threadIdx.x, tx = t & 31, ty = t >> 5;
+    for (int blk = blockIdx.x; blk < nb; blk += gridDim.x) {
+        const ABrick ab = adj_brick(bmap, 2, blk);
+        const Inst& I = inst[ab.inst];
+        const int i = ab.i0 + tx, j = ab.j0 + ty, k1 = min(ab.k0 + adj_shape(2).oz, I.nk);
+        double sacc = 0.0;
+        if (i < I.ni && j < I.nj) {
+            const long long sk = (long long)I.ni * I.nj;
+            const T* p = lam + I.off + i + (long long)I.ni * j;
+            for (int k = ab.k0; k < k1; ++k) sacc += (double)__ldg(p + sk * k);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
+        if (tx == 0) red[ty] = sacc;
+        __syncthreads();
+        if (t == 0) {
+            double r = 0.0;
+            for (int u = 0; u < 8; ++u) r += red[u];
+            part[blk] = r;
+        }
+        __syncthreads();
+    }
+}
+
+// part 3: one block per instance sums its tiles' partials in a fixed order
+__global__ void __launch_bounds__(256) k_inst_sum(const Inst* __restrict__ inst, const double* __restrict__ part,
+                                                  double* __restrict__ out) {
+    __shared__ double red[8];
+    const Inst& I = inst[blockIdx.x];
+    const int t0 = I.am[2][0];
+    const int nt = I.am[2][1] * I.am[2][2] * ((I.nk + adj_shape(2).oz - 1) / adj_shape(2).oz);
+    double s = 0.0;
+    for (int u = threadIdx.x; u < nt; u += blockDim.x) s += part[t0 + u];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = 0.0;
+        for (int u = 0; u < 8; ++u) r += red[u];
+        out[blockIdx.x] = r;
+    }
+}
+
+// part 4: lam_pre = lam - (S / A) w with S = sum(lam) of the instance, w =
+// wfix in fixed point; clears wfix for the next step
+template <typename T>
+__global__ void k_mass_apply(Flat fl, const Mass* __restrict__ mass, const double* __restrict__ ssum,
+                             T* __restrict__ lam, unsigned long long* __restrict__ wfix) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < fl.n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long q = (long long)wfix[t];
+        if (q == 0) continue;
+        wfix[t] = 0ull;
+        Node nd;
+        flat_node(fl, t, &nd);
+        const Mass M = mass[nd.inst];
+        lam[t] = (T)((double)lam[t] - ssum[nd.inst] / M.A * ((double)q * kVolUnit));
+    }
 }
 
 // fixed-point Davies-Salmond volume of every cell of one instance
@@ -1504,6 +2042,14 @@ LSM_BATCH_RUNNER(RunVolume, k_volume,
                  (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi,
                   unsigned long long* part, cudaStream_t s),
                  (inst, bi, nb, f, phi, part))
+LSM_BATCH_RUNNER(RunVolumeSlope, k_volume_slope,
+                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi,
+                  unsigned long long* part, cudaStream_t s),
+                 (inst, bi, nb, f, phi, part))
+LSM_BATCH_RUNNER(RunMassWeights, k_mass_weights,
+                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi, const Mass* m,
+                  unsigned long long* wfix, cudaStream_t s),
+                 (inst, bi, nb, f, phi, m, wfix))
 
 template <typename T, int TX, int TY, int TZ>
 struct Occupancy {
@@ -1530,6 +2076,18 @@ void stage(int grid, const Inst* inst, const Brick* bmap2, int nb, FieldsT<T> f,
            double c1, double c2, double c3, cudaStream_t s) {
     ProfScope ps_("k_stage_z", s);
     k_stage_z<T><<<grid, 256, 0, s>>>(inst, bmap2, nb, f, phin, phi1, out, T(c1), T(c2), T(c3));
+}
+void stage_tma(int grid, const CUtensorMap* tm, int a_in, const Inst* inst, const Brick* bmap2, int nb,
+               FieldsT<float> f, const float* phin, const float* phi1, float* out, double c1, double c2, double c3,
+               unsigned* err, cudaStream_t s) {
+    ProfScope ps_("k_stage_tma", s);
+    k_stage_tma<<<grid, 256, 0, s>>>(*tm, a_in, inst, bmap2, nb, f, phin, phi1, out, (float)c1, (float)c2, (float)c3,
+                                     err);
+}
+int stage_tma_blocks_per_sm() {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_stage_tma, 256, 0);
+    return n;
 }
 template <typename T>
 int stage_blocks_per_sm() {
@@ -1616,12 +2174,36 @@ void bc_reinit(const Inst* inst, int ninst, long long nface, FieldsT<T> f, BC bc
 }
 template <typename T>
 void volume(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi,
-            unsigned long long* acc, cudaStream_t s) {
-    dispatch<RunVolume, T>(shape, grid, inst, bi, nb, f, phi, acc, s);
+            unsigned long long* acc, bool slope, cudaStream_t s) {
+    if (slope) dispatch<RunVolumeSlope, T>(shape, grid, inst, bi, nb, f, phi, acc, s);
+    else dispatch<RunVolume, T>(shape, grid, inst, bi, nb, f, phi, acc, s);
 }
-void volume_final(int ninst, unsigned long long* acc, double* vols, cudaStream_t s) {
+void volume_final(int ninst, unsigned long long* acc, double* vols, const double* target, Mass* mass, Mass* mrec,
+                  cudaStream_t s) {
     ProfScope ps_("k_volume_final", s);
-    k_volume_final<<<(ninst + 127) / 128, 128, 0, s>>>(ninst, acc, vols);
+    k_volume_final<<<(ninst + 127) / 128, 128, 0, s>>>(ninst, acc, vols, target, mass, mrec);
+}
+template <typename T>
+void mass_shift(const Flat& fl, const Mass* mass, const T* src, T* dst, cudaStream_t s) {
+    ProfScope ps_("k_mass_shift", s);
+    k_mass_shift<T><<<(unsigned)std::min<long long>((fl.n + 255) / 256, 152 * 16), 256, 0, s>>>(fl, mass, src, dst);
+}
+template <typename T>
+void mass_adjoint(int shape, int grid, const Inst* inst, const Brick* bi, int nb, const Brick* bmap2, int nb2,
+                  const Flat& fl, FieldsT<T> f, const T* phi_pre, const Mass* mass, T* lam, unsigned long long* wfix,
+                  double* part, double* ssum, cudaStream_t s) {
+    dispatch<RunMassWeights, T>(shape, grid, inst, bi, nb, f, phi_pre, mass, wfix, s);
+    {
+        ProfScope ps_("k_tile_sum", s);
+        k_tile_sum<T><<<std::min(nb2, 152 * 8), 256, 0, s>>>(inst, bmap2, nb2, lam, part);
+    }
+    {
+        ProfScope ps_("k_inst_sum", s);
+        k_inst_sum<<<fl.ninst, 256, 0, s>>>(inst, part, ssum);
+    }
+    ProfScope ps_("k_mass_apply", s);
+    k_mass_apply<T><<<(unsigned)std::min<long long>((fl.n + 255) / 256, 152 * 16), 256, 0, s>>>(fl, mass, ssum, lam,
+                                                                                                 wfix);
 }
 void cell_hex(long long off, int ni, int nj, int nk, const double* x, const double* y, const double* z,
               long long* cellfix, cudaStream_t s) {
@@ -1702,7 +2284,10 @@ void adj_contra(const Flat& fl, FieldsT<T> f, const T* w0, const T* w1, const T*
                                   cudaStream_t);                                                                \
     template int adj_reinit_c_blocks_per_sm<T>();                                                               \
     template void volume<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, unsigned long long*,   \
-                             cudaStream_t);                                                                          \
+                             bool, cudaStream_t);                                                                    \
+    template void mass_shift<T>(const Flat&, const Mass*, const T*, T*, cudaStream_t);                                 \
+    template void mass_adjoint<T>(int, int, const Inst*, const Brick*, int, const Brick*, int, const Flat&, FieldsT<T>, \
+                                  const T*, const Mass*, T*, unsigned long long*, double*, double*, cudaStream_t);     \
     template void adj_face<T>(const Flat&, int, long long, BC, int, const T*, const T*, const T*, double, double, T*, \
                               cudaStream_t);                                                                          \
     template void adj_stage<T>(const int*, const Inst*, const Brick* const*, const int*, FieldsT<T>, const T*,      \

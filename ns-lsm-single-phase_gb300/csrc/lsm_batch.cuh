@@ -10,6 +10,7 @@
 // instance are physical boundaries (one rank per instance, no ghosts).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace lsm {
@@ -52,6 +53,19 @@ using Fields = FieldsT<float>;
 constexpr double kVolScale = 281474976710656.0;       // 2^48
 constexpr double kVolUnit = 1.0 / 281474976710656.0;  // 2^-48
 
+// Mass correction of one instance for one step (FP64): the water volume V
+// of the step's result before the correction, A = dK/dC, the derivative of
+// that volume under a uniform shift phi + C (only the interface cells'
+// K tetrahedra depend on it), the shift C = (target - V) / A that was
+// applied, and the instance's target volume (NaN: no correction).
+struct Mass {
+    double V, A, C, target;
+};
+__host__ __device__ inline bool mass_on(const Mass& m) {
+    const double c = (m.target - m.V) / m.A;
+    return m.target == m.target && m.A > 0.0 && c - c == 0.0;   // finite target, slope and shift
+}
+
 struct BC {
     int type[6];
     float BigPhi;
@@ -80,6 +94,14 @@ void stage(int grid, const Inst* inst, const Brick* bmap2, int nb, FieldsT<T> f,
            T* out, double c1, double c2, double c3, cudaStream_t s);
 template <typename T>
 int stage_blocks_per_sm();
+// The same stage (FP32) with each plane's tile + two-node halo staged in
+// shared memory by TMA copies: a batch of one instance with ni a multiple
+// of 4; phi1 is array a_in of the 4-D tensor map tm (ni, nj, nk, arrays);
+// err gets kErrTimeout if a copy's completion never arrived
+void stage_tma(int grid, const CUtensorMap* tm, int a_in, const Inst* inst, const Brick* bmap2, int nb,
+               FieldsT<float> f, const float* phin, const float* phi1, float* out, double c1, double c2, double c3,
+               unsigned* err, cudaStream_t s);
+int stage_tma_blocks_per_sm();
 template <typename T>
 void bc_stage(const Inst* inst, int ninst, long long nface, BC bc, const T* phin, const T* phi1, T* out, double c1,
               double c2, cudaStream_t s);
@@ -115,12 +137,16 @@ void reinit_z(int kind, int grid, const Inst* inst, const Brick* bmap2, int nb, 
 template <typename T>
 int reinit_z_blocks_per_sm();
 // water volume of every instance: k_volume adds 64-bit fixed-point sums
-// (K, S, bulk) to acc[3 * inst + c] (zero on entry); volume_final writes
-// vols[4 * inst + 0..3] = (K, S, bulk, total) and clears acc
+// (K, S, bulk and, with `slope`, dK/dC) to acc[4 * inst + c] (zero on
+// entry); volume_final writes vols[4 * inst + 0..3] = (K, S, bulk, total)
+// and clears acc; with `mass` (target volumes `target`, NaN = none) it also
+// forms each instance's mass correction into mass[inst] and, when mrec is
+// not null, mrec[inst]
 template <typename T>
 void volume(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f, const T* phi,
-            unsigned long long* acc, cudaStream_t s);
-void volume_final(int ninst, unsigned long long* acc, double* vols, cudaStream_t s);
+            unsigned long long* acc, bool slope, cudaStream_t s);
+void volume_final(int ninst, unsigned long long* acc, double* vols, const double* target, Mass* mass, Mass* mrec,
+                  cudaStream_t s);
 // fixed-point hexahedron volume of every cell of one instance (static
 // geometry); x, y, z and cellfix are the packed base arrays, `off` the
 // instance's first node
@@ -185,6 +211,18 @@ int adj_reinit_c_blocks_per_sm();
 // resident blocks per SM of the kernel of adjoint map `map`
 template <typename T>
 int adj_blocks_per_sm(int map);
+// Mass correction: dst = src + mass[inst].C on every node (dst may alias src)
+template <typename T>
+void mass_shift(const Flat& fl, const Mass* mass, const T* src, T* dst, cudaStream_t s);
+// Reverse of the shift phi' = phi + C(phi) in place on lam (the adjoint of
+// phi'): lam -= (sum(lam) / A) (dK/dphi + C d(dK/dC)/dphi), evaluated on
+// the step's pre-correction field phi_pre; wfix (N 64-bit words, zero on
+// entry and on exit) and part (one double per tile of adjoint map 2), ssum
+// (one per instance) are scratch
+template <typename T>
+void mass_adjoint(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, const Brick* bmap2,
+                  int nb2, const Flat& fl, FieldsT<T> f, const T* phi_pre, const Mass* mass, T* lam,
+                  unsigned long long* wfix, double* part, double* ssum, cudaStream_t s);
 // lam_u_c += sum_m M[m][c] dt lamW_m  (the W = dt M u chain rule)
 template <typename T>
 void adj_contra(const Flat& fl, FieldsT<T> f, const T* lamW0, const T* lamW1, const T* lamW2, T* lu0, T* lu1,

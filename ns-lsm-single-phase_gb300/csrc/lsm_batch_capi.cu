@@ -1,8 +1,9 @@
 // lsm_batch_capi.cu -- host side of include/lsm_batch.h: packed device
 // buffers of a batch of instances, the brick and tile tables of the
 // persistent kernels, the autotuner (tile shape; brick or marching
-// pseudo-steps), the CUDA graph of one physical step and the checkpointed
-// adjoint (forward_record keeping the last segment's internals / backward).
+// pseudo-steps), the CUDA graph of one physical step, the FP64 mass
+// correction and the checkpointed adjoint (forward_record keeping the last
+// segment's internals / backward).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -20,6 +21,7 @@
 
 using lsm::batch::Flat;
 using lsm::batch::Inst;
+using lsm::batch::Mass;
 template <typename T>
 using FieldsT = lsm::batch::FieldsT<T>;
 
@@ -56,8 +58,16 @@ struct lsm_batch {
     int namap[4] = {0, 0, 0, 0}, agrid[4] = {1, 1, 1, 1};
     int sgrid = 1, acgrid = 1, rzgrid = 1;   // CTAs of the map-2 kernels: stage, k_adj_reinit_c, reinit_z
     bool reinit_march = true;   // plain pseudo-steps march in k (reinit_z) rather than walk the brick table
-    unsigned long long* d_vacc = nullptr;   // volume accumulators, 3 per instance (k_volume)
+    unsigned long long* d_vacc = nullptr;   // volume accumulators, 4 per instance (k_volume)
     double* d_vols = nullptr;
+    // mass correction: per-instance target volumes (NaN: none) and the last
+    // step's correction; adjoint scratch (N fixed-point weights, one partial
+    // per tile of adjoint map 2, one sum per instance)
+    double* d_target = nullptr;
+    Mass* d_mass = nullptr;
+    unsigned long long* wfix = nullptr;
+    double* d_tpart = nullptr;
+    double* d_ssum = nullptr;
     double* h_vols = nullptr;    // pinned
     unsigned* d_err = nullptr;
     int shape = 0, grid = 0;
@@ -227,8 +237,8 @@ int build_bricks(lsm_batch* b, int shape) {
     BCU(b, cudaMemcpyAsync(b->d_brick, brick.data(), sizeof(Brick) * brick.size(), cudaMemcpyHostToDevice, b->stream));
     BCU(b, cudaMemcpyAsync(b->d_inst, hi.data(), sizeof(Inst) * hi.size(), cudaMemcpyHostToDevice, b->stream));
     if (!b->d_vacc) {
-        BCU(b, cudaMalloc(&b->d_vacc, sizeof(unsigned long long) * 3 * (size_t)b->ninst));
-        BCU(b, cudaMemsetAsync(b->d_vacc, 0, sizeof(unsigned long long) * 3 * (size_t)b->ninst, b->stream));
+        BCU(b, cudaMalloc(&b->d_vacc, sizeof(unsigned long long) * 4 * (size_t)b->ninst));
+        BCU(b, cudaMemsetAsync(b->d_vacc, 0, sizeof(unsigned long long) * 4 * (size_t)b->ninst, b->stream));
     }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
@@ -277,12 +287,14 @@ FieldsT<double>& fields<double>(lsm_batch* b) { return b->f64; }
 //                   pseudo-step's adjoint coefficients (C + 6 k ld);
 //   adjoint_mode 1: the RNitermax raw pseudo-step outputs (D + k ld) and
 //                   the sign field.
+//   with the mass correction, P: the step's result before the correction.
 template <typename T>
 struct Rec {
     T* A[3];
     T* D;
     T* sgn;   // mode 1 only
     T* C;     // mode 0 only
+    T* P;     // mass correction only
 };
 
 // raw output of pseudo-step k of a recorded step (mode 1: every k; mode 0:
@@ -297,18 +309,26 @@ T* rec_d(const lsm_batch* b, const Rec<T>& r, int k) {
 // outputs (before the final bcond_lsm) and the sign field are kept; `vol`
 // adds the pre-advection water volume; a recorded step checks phi_out for
 // non-finite values when `check` (plain steps always do).
+// With the mass correction the volume pass moves after the final bcond_lsm:
+// it measures the step's result (the slot's P in a recorded step, which is
+// then kept even when phi_out is nullptr), forms the correction (into mrec
+// too when given) and phi_out = result + C.
 template <typename T>
-void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec, bool vol, bool check = false) {
+void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec, bool vol, bool check = false,
+                     Mass* mrec = nullptr) {
     namespace B = lsm::batch;
     const int sh = b->shape, gr = b->grid, nb = b->nbricks;
     const B::BC bc = make_bc(b);
     FieldsT<T> f = fields<T>(b);
+    const bool mc = b->cfg.mass_correction != 0;
     const bool coef = rec && b->cfg.adjoint_mode == 0;   // recorded step storing adjoint coefficients
     if (rec && !coef) f.sgn = rec->sgn;
-    if (vol) {
-        B::volume<T>(sh, gr, b->d_inst, b->d_brick, nb, f, phin, b->d_vacc, b->stream);
-        B::volume_final(b->ninst, b->d_vacc, b->d_vols, b->stream);
+    if (vol && !mc) {
+        B::volume<T>(sh, gr, b->d_inst, b->d_brick, nb, f, phin, b->d_vacc, false, b->stream);
+        B::volume_final(b->ninst, b->d_vacc, b->d_vols, nullptr, nullptr, nullptr, b->stream);
     }
+    // the field the final bcond_lsm writes
+    T* res = mc && rec ? rec->P : phi_out;
     B::contra<T>(sh, gr, b->d_inst, b->d_brick, nb, f, b->stream);
     T* S[3] = {rec ? rec->A[0] : f.stage[0], rec ? rec->A[1] : f.stage[1], rec ? rec->A[2] : f.stage[0]};
     const T* in[3] = {phin, S[0], S[1]};
@@ -328,11 +348,11 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
         bool twice = false;
         for (int it = 0; it < R; ++it) {
             const bool last = it == R - 1;
-            T* o = coef ? (last ? rec->D : f.d[it & 1]) : rec ? rec_d(b, *rec, it) : (last ? phi_out : f.d[it & 1]);
+            T* o = coef ? (last ? rec->D : f.d[it & 1]) : rec ? rec_d(b, *rec, it) : (last ? res : f.d[it & 1]);
             const bool march = coef || b->reinit_march;
             // a recorded step's last pseudo-step also writes phi^{n+1} (its
             // faces are then redone from the raw output)
-            T* o2 = rec && last && phi_out && march ? phi_out : nullptr;
+            T* o2 = rec && last && res && march ? res : nullptr;
             twice = twice || o2 != nullptr;
             unsigned* err = (last && !rec) || (o2 && check) ? b->d_err : nullptr;
             T* cf = coef ? rec->C + 6LL * it * (long long)b->ld : nullptr;
@@ -343,17 +363,24 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
                 B::sign_reinit<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, err, b->stream);
             else
                 B::reinit<T>(sh, gr, b->d_inst, b->d_brick, nb, f, cur, o, err, b->stream);
-            if (last && !rec) B::bc_reinit<T>(b->d_inst, b->ninst, b->nface, f, bc, cur, phi_out, b->stream);
+            if (last && !rec) B::bc_reinit<T>(b->d_inst, b->ninst, b->nface, f, bc, cur, res, b->stream);
             cur = o;
         }
         // recorded steps keep the raw last pseudo-step and write phi^{n+1} apart
-        if (rec && phi_out && twice)
-            B::bc_faces<T>(b->d_inst, b->ninst, b->nface, bc, cur, phi_out, check ? b->d_err : nullptr, b->stream);
-        else if (rec && phi_out)
-            B::bc_full<T>(sh, gr, b->d_inst, b->d_brick, nb, bc, cur, phi_out, check ? b->d_err : nullptr, b->stream);
-    } else if (phi_out) {
-        B::bc_full<T>(sh, gr, b->d_inst, b->d_brick, nb, bc, S[2], phi_out, rec && !check ? nullptr : b->d_err,
+        if (rec && res && twice)
+            B::bc_faces<T>(b->d_inst, b->ninst, b->nface, bc, cur, res, check ? b->d_err : nullptr, b->stream);
+        else if (rec && res)
+            B::bc_full<T>(sh, gr, b->d_inst, b->d_brick, nb, bc, cur, res, check ? b->d_err : nullptr, b->stream);
+    } else if (res) {
+        B::bc_full<T>(sh, gr, b->d_inst, b->d_brick, nb, bc, S[2], res, rec && !check ? nullptr : b->d_err,
                       b->stream);
+    }
+    if (mc) {
+        // FP64 water volume of the result, the correction C = (target - V) / A
+        // and phi_out = result + C
+        B::volume<T>(sh, gr, b->d_inst, b->d_brick, nb, f, res, b->d_vacc, true, b->stream);
+        B::volume_final(b->ninst, b->d_vacc, b->d_vols, b->d_target, b->d_mass, mrec, b->stream);
+        if (phi_out) B::mass_shift<T>(Flat{b->d_inst, b->d_offs, b->ninst, b->N}, b->d_mass, res, phi_out, b->stream);
     }
 }
 
@@ -397,8 +424,9 @@ int autotune(lsm_batch* b) {
             &a[s], &br[s],
             [&]() {
                 B::contra<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, b->stream);
-                B::volume<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, f.phi, b->d_vacc, b->stream);
-                B::volume_final(b->ninst, b->d_vacc, b->d_vols, b->stream);
+                B::volume<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, f.phi, b->d_vacc, false,
+                                 b->stream);
+                B::volume_final(b->ninst, b->d_vacc, b->d_vols, nullptr, nullptr, nullptr, b->stream);
             },
             [&]() {
                 B::sign_reinit<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, f.phi, f.d[0], nullptr,
@@ -476,17 +504,19 @@ int check_inst(lsm_batch* b, int q) {
 template <typename T>
 struct AdjView {
     T *ckpt, *seg, *slots, *lam, *lam2, *lamPhin, *lamW[3], *lamU[3];
+    Mass* mrec;   // mass correction of every step of the segment, ninst per step
 };
 
 int n_ckpt(int nsteps, int ck) { return (nsteps + ck - 1) / ck; }
 // arrays of one recorded step, each b->ld elements apart
 long long slot_elems(const lsm_batch* b) {
     const long long R = b->cfg.RNitermax;
-    return (b->cfg.adjoint_mode == 0 ? 4 + 6 * R : 4 + R) * (long long)b->ld;
+    return ((b->cfg.adjoint_mode == 0 ? 4 + 6 * R : 4 + R) + (b->cfg.mass_correction ? 1 : 0)) * (long long)b->ld;
 }
 
 size_t adj_elems(const lsm_batch* b, int nsteps, int ck) {
-    return b->ld * (size_t)(n_ckpt(nsteps, ck) + ck + 3 + 3 + 3) + (size_t)ck * (size_t)slot_elems(b);
+    const size_t mrec = ((size_t)ck * (size_t)b->ninst * sizeof(Mass) + b->esz - 1) / b->esz;
+    return b->ld * (size_t)(n_ckpt(nsteps, ck) + ck + 3 + 3 + 3) + (size_t)ck * (size_t)slot_elems(b) + mrec;
 }
 
 template <typename T>
@@ -503,6 +533,7 @@ Rec<T> slot(lsm_batch* b, const AdjView<T>& v, int q) {
         r.C = nullptr;
         r.sgn = p + (3 + b->cfg.RNitermax) * L;
     }
+    r.P = b->cfg.mass_correction ? p + slot_elems(b) - L : nullptr;
     return r;
 }
 
@@ -531,6 +562,7 @@ AdjView<T> adj_view(lsm_batch* b) {
         v.lamU[c] = p;
         p += N;
     }
+    v.mrec = (Mass*)p;   // arrays are multiples of 256 bytes apart
     return v;
 }
 
@@ -547,6 +579,14 @@ int forward_record_t(lsm_batch* b, int nsteps, int ck) {
         }
         BCU(b, cudaMalloc(&b->adj, bytes));
         b->adj_bytes = bytes;
+    }
+    if (b->cfg.mass_correction && !b->wfix) {
+        // adjoint scratch of the mass correction (the weights start at zero
+        // and every reverse step leaves them at zero)
+        BCU(b, cudaMalloc(&b->wfix, sizeof(unsigned long long) * (size_t)b->N));
+        BCU(b, cudaMemsetAsync(b->wfix, 0, sizeof(unsigned long long) * (size_t)b->N, b->stream));
+        BCU(b, cudaMalloc(&b->d_tpart, sizeof(double) * (size_t)std::max(1, b->namap[2])));
+        BCU(b, cudaMalloc(&b->d_ssum, sizeof(double) * (size_t)b->ninst));
     }
     b->rec_steps = nsteps;
     b->rec_ck = ck;
@@ -573,7 +613,7 @@ int forward_record_t(lsm_batch* b, int nsteps, int ck) {
     for (int q = 0; q < L; ++q) {
         const Rec<T> r = slot<T>(b, v, q);
         enqueue_step_io<T>(b, v.seg + (long long)q * LD, q + 1 < L ? v.seg + (long long)(q + 1) * LD : f.phi, &r,
-                           true, true);
+                           true, true, v.mrec + (long long)q * b->ninst);
     }
     BCU(b, cudaGetLastError());
     unsigned flags = 0;
@@ -588,7 +628,7 @@ int forward_record_t(lsm_batch* b, int nsteps, int ck) {
 // lam holds the adjoint of phi^{n+1}, on exit the adjoint of phi^n (the
 // pointers of `v` swap along the way).
 template <typename T>
-void adj_step(lsm_batch* b, AdjView<T>& v, const Rec<T>& r, const T* phin) {
+void adj_step(lsm_batch* b, AdjView<T>& v, const Rec<T>& r, const T* phin, const Mass* m) {
     namespace B = lsm::batch;
     FieldsT<T> f = fields<T>(b);
     if (r.sgn) f.sgn = r.sgn;
@@ -596,6 +636,10 @@ void adj_step(lsm_batch* b, AdjView<T>& v, const Rec<T>& r, const T* phin) {
     const long long N = b->N;
     const Flat fl{b->d_inst, b->d_offs, b->ninst, N};
     const int R = b->cfg.RNitermax;
+    // reverse of the mass correction phi^{n+1} = P + C(P), in place on lam
+    if (b->cfg.mass_correction)
+        B::mass_adjoint<T>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, b->d_amap[2], b->namap[2], fl, f,
+                           r.P, m, v.lam, b->wfix, b->d_tpart, b->d_ssum, b->stream);
     auto faces = [&](int kind, const T* pn, const T* in, const T* out, double c1, double c2) {
         for (int face = 5; face >= 0; --face)
             B::adj_face<T>(fl, face, b->nplane[face >> 1], bc, kind, pn, in, out, c1, c2, v.lam, b->stream);
@@ -649,10 +693,11 @@ int backward_t(lsm_batch* b) {
             for (int q = 0; q < L; ++q) {
                 const Rec<T> r = slot<T>(b, v, q);
                 enqueue_step_io<T>(b, v.seg + (long long)q * LD, q + 1 < L ? v.seg + (long long)(q + 1) * LD : nullptr,
-                                   &r, false);
+                                   &r, false, false, v.mrec + (long long)q * b->ninst);
             }
         }
-        for (int q = L - 1; q >= 0; --q) adj_step<T>(b, v, slot<T>(b, v, q), v.seg + (long long)q * LD);
+        for (int q = L - 1; q >= 0; --q)
+            adj_step<T>(b, v, slot<T>(b, v, q), v.seg + (long long)q * LD, v.mrec + (long long)q * b->ninst);
     }
     const Flat fl{b->d_inst, b->d_offs, b->ninst, N};
     lsm::batch::adj_contra<T>(fl, fields<T>(b), v.lamW[0], v.lamW[1], v.lamW[2], v.lamU[0], v.lamU[1], v.lamU[2],
@@ -687,7 +732,7 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
     for (int f = 0; f < 6; ++f)
         if (cfg->btype_lsm[f] < 0 || cfg->btype_lsm[f] > 2) return LSM_ERR_BAD_PARAM;
     if (cfg->RNitermax < 0 || (cfg->precision != 0 && cfg->precision != 1) ||
-        (cfg->adjoint_mode != 0 && cfg->adjoint_mode != 1))
+        (cfg->adjoint_mode != 0 && cfg->adjoint_mode != 1) || (cfg->mass_correction != 0 && cfg->mass_correction != 1))
         return LSM_ERR_BAD_PARAM;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
@@ -734,6 +779,16 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
     if (cudaMalloc(&b->d_vols, sizeof(double) * 4 * ninst) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMallocHost(&b->h_vols, sizeof(double) * 4 * ninst) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->d_err, sizeof(unsigned)) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
+    if (cudaMalloc(&b->d_target, sizeof(double) * ninst) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
+    if (cudaMalloc(&b->d_mass, sizeof(Mass) * ninst) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
+    {
+        // no target volume (no correction) until lsm_batch_set_mass_target
+        std::vector<double> nan((size_t)ninst, std::nan(""));
+        std::vector<Mass> zero((size_t)ninst, Mass{0.0, 0.0, 0.0, std::nan("")});
+        if (cudaMemcpy(b->d_target, nan.data(), sizeof(double) * ninst, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(b->d_mass, zero.data(), sizeof(Mass) * ninst, cudaMemcpyHostToDevice) != cudaSuccess)
+            return cleanup(LSM_ERR_CUDA);
+    }
     cudaMemcpyAsync(b->d_offs, b->off.data(), sizeof(long long) * (ninst + 1), cudaMemcpyHostToDevice, b->stream);
     cudaMemsetAsync(b->d_err, 0, sizeof(unsigned), b->stream);
     cudaMemsetAsync(b->d_vols, 0, sizeof(double) * 4 * ninst, b->stream);
@@ -769,7 +824,8 @@ int lsm_batch_destroy(lsm_batch_handle b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     for (void* p : {b->field_arena, (void*)b->xyz, (void*)b->staging, (void*)b->d_inst, (void*)b->d_offs,
                     (void*)b->d_brick, (void*)b->d_amap[0], (void*)b->d_amap[1], (void*)b->d_amap[2],
-                    (void*)b->d_amap[3], (void*)b->d_vacc, (void*)b->d_vols, (void*)b->d_err, b->adj})
+                    (void*)b->d_amap[3], (void*)b->d_vacc, (void*)b->d_vols, (void*)b->d_err, b->adj,
+                    (void*)b->d_target, (void*)b->d_mass, (void*)b->wfix, (void*)b->d_tpart, (void*)b->d_ssum})
         if (p) cudaFree(p);
     if (b->h_vols) cudaFreeHost(b->h_vols);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
@@ -910,6 +966,51 @@ int lsm_batch_get_grad_velocity(lsm_batch_handle b, int q, double* gq) {
     return copy_out(b, gq, 4 * n);
 }
 
+int lsm_batch_set_mass_target(lsm_batch_handle b, int q, double volume) {
+    if (!b) return LSM_ERR_NULL;
+    BTRY(check_inst(b, q));
+    if (!b->cfg.mass_correction) return fail(b, LSM_ERR_BAD_PARAM, "the batch was created without mass correction");
+    Dev guard(b->device);
+    const double v = volume;   // copied before the call returns (synchronised below)
+    BCU(b, cudaMemcpyAsync(b->d_target + q, &v, sizeof(double), cudaMemcpyHostToDevice, b->stream));
+    BCU(b, cudaStreamSynchronize(b->stream));
+    return LSM_OK;
+}
+
+int lsm_batch_water_volume(lsm_batch_handle b, double* volumes) {
+    if (!b || !volumes) return LSM_ERR_NULL;
+    Dev guard(b->device);
+    BTRY(prepare(b));
+    namespace B = lsm::batch;
+    if (b->prec)
+        B::volume<double>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, b->f64, b->f64.phi, b->d_vacc, false,
+                          b->stream);
+    else
+        B::volume<float>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, b->f32, b->f32.phi, b->d_vacc, false,
+                         b->stream);
+    B::volume_final(b->ninst, b->d_vacc, b->d_vols, nullptr, nullptr, nullptr, b->stream);
+    BCU(b, cudaGetLastError());
+    BCU(b, cudaMemcpyAsync(b->h_vols, b->d_vols, sizeof(double) * 4 * b->ninst, cudaMemcpyDeviceToHost, b->stream));
+    BCU(b, cudaStreamSynchronize(b->stream));
+    std::memcpy(volumes, b->h_vols, sizeof(double) * 4 * b->ninst);
+    return LSM_OK;
+}
+
+int lsm_batch_mass_state(lsm_batch_handle b, double* out) {
+    if (!b || !out) return LSM_ERR_NULL;
+    Dev guard(b->device);
+    std::vector<Mass> m((size_t)b->ninst);
+    BCU(b, cudaMemcpyAsync(m.data(), b->d_mass, sizeof(Mass) * b->ninst, cudaMemcpyDeviceToHost, b->stream));
+    BCU(b, cudaStreamSynchronize(b->stream));
+    for (int q = 0; q < b->ninst; ++q) {
+        out[4 * q] = m[q].V;
+        out[4 * q + 1] = m[q].A;
+        out[4 * q + 2] = m[q].C;
+        out[4 * q + 3] = m[q].target;
+    }
+    return LSM_OK;
+}
+
 int lsm_batch_shape(lsm_batch_handle b, int* index, int* tx, int* ty, int* tz) {
     if (!b) return LSM_ERR_NULL;
     const auto sh = lsm::batch::kShapes[b->shape];
@@ -926,9 +1027,9 @@ int lsm_batch_launches_per_step(lsm_batch_handle b) {
     if (!b) return 0;
     // volume 2, contra 1, three stages x (stencil + faces) 6, then
     // RNitermax pseudo-steps (the first with the sign field) + final faces,
-    // or one full bcond pass
+    // or one full bcond pass; the mass correction's shift 1
     const int R = b->cfg.RNitermax;
-    return 2 + 1 + 6 + (R > 0 ? R + 1 : 1);
+    return 2 + 1 + 6 + (R > 0 ? R + 1 : 1) + (b->cfg.mass_correction ? 1 : 0);
 }
 
 const char* lsm_batch_last_error(lsm_batch_handle b) { return b ? b->err.c_str() : ""; }

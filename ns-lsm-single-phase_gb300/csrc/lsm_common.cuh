@@ -36,6 +36,7 @@ struct DevBC {
 enum : unsigned {
     kErrNegativeVolume = 1u,
     kErrNonFinite = 2u,
+    kErrTimeout = 4u,   // a bounded wait on an asynchronous copy gave up
 };
 
 constexpr double kPi = 3.141592653589793;     // src/precision.F90:51

@@ -56,7 +56,7 @@ module lsm_iso_c
    type, bind(C) :: lsm_batch_config
       integer(c_int) :: RNitermax, btype_lsm(6)
       real(c_double) :: BigPhi
-      integer(c_int) :: use_graph, autotune, shape, precision, adjoint_mode
+      integer(c_int) :: use_graph, autotune, shape, precision, adjoint_mode, mass_correction
    end type lsm_batch_config
 
    interface
@@ -283,6 +283,22 @@ module lsm_iso_c
          type(c_ptr), value :: h
          integer(c_int), value :: nsteps
          real(c_double), intent(out) :: vols(*)
+      end function
+      integer(c_int) function lsm_batch_water_volume(h, vols) bind(C, name="lsm_batch_water_volume")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         real(c_double), intent(out) :: vols(*)
+      end function
+      integer(c_int) function lsm_batch_set_mass_target(h, inst, volume) bind(C, name="lsm_batch_set_mass_target")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         integer(c_int), value :: inst
+         real(c_double), value :: volume
+      end function
+      integer(c_int) function lsm_batch_mass_state(h, state) bind(C, name="lsm_batch_mass_state")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         real(c_double), intent(out) :: state(*)
       end function
    end interface
 

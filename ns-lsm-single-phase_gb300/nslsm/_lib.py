@@ -62,7 +62,7 @@ class LsmBatchConfig(C.Structure):
     """struct lsm_batch_config"""
     _fields_ = [("RNitermax", C.c_int), ("btype_lsm", C.c_int * 6), ("BigPhi", C.c_double),
                 ("use_graph", C.c_int), ("autotune", C.c_int), ("shape", C.c_int),
-                ("precision", C.c_int), ("adjoint_mode", C.c_int)]
+                ("precision", C.c_int), ("adjoint_mode", C.c_int), ("mass_correction", C.c_int)]
 
 
 EXCHANGE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.POINTER(LsmGrid))
@@ -112,6 +112,9 @@ SIGNATURES = {
     "lsm_batch_set_phi": (_i, [_vp, _i, _vp]),
     "lsm_batch_get_phi": (_i, [_vp, _i, _vp]),
     "lsm_batch_step": (_i, [_vp, _i, _vp]),
+    "lsm_batch_water_volume": (_i, [_vp, _vp]),
+    "lsm_batch_set_mass_target": (_i, [_vp, _i, _d]),
+    "lsm_batch_mass_state": (_i, [_vp, _vp]),
     "lsm_batch_forward_record": (_i, [_vp, _i, _i]),
     "lsm_batch_set_grad_phi": (_i, [_vp, _i, _vp]),
     "lsm_batch_backward": (_i, [_vp]),

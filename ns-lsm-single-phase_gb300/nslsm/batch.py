@@ -13,6 +13,10 @@
     # the same through torch.autograd
     outs = transport(b, nsteps, phi0_list, q_list)
 
+    # FP64 mass correction towards each instance's target volume
+    b = LevelSetBatch(instances, mass_correction=True)
+    ...; b.set_mass_target(k, b.water_volume()[k, 3])
+
 Arrays follow the same conventions as nslsm.api: numpy in the reference's
 Fortran layout or CUDA tensors with the reversed shape.
 """
@@ -42,10 +46,11 @@ class LevelSetBatch:
     def __init__(self, instances: Sequence[Tuple[int, int, int, float, float, float]], RNitermax: int = 5,
                  btype: Sequence[int] = (1, 1, 1, 1, 1, 1), BigPhi: float = 5.0, device: int = 0, stream=None,
                  use_graph: bool = True, autotune: bool = True, shape: int = 0, precision: str = "fp32",
-                 adjoint_mode: str = "store"):
+                 adjoint_mode: str = "store", mass_correction: bool = False):
         """instances: (ni, nj, nk, dt, dtau, eps) per instance; precision "fp32" or "fp64";
         adjoint_mode "store" (recorded pseudo-steps keep their adjoint coefficients: 6 arrays each)
-        or "recompute" (the reverse sweep re-derives them: 1 array each)."""
+        or "recompute" (the reverse sweep re-derives them: 1 array each); mass_correction: after
+        every step shift phi by C = (target - V) / (dV/dC) towards the targets of set_mass_target."""
         if precision not in ("fp32", "fp64"):
             raise ValueError("precision must be 'fp32' or 'fp64'")
         if adjoint_mode not in ("store", "recompute"):
@@ -64,6 +69,8 @@ class LevelSetBatch:
         cfg.use_graph, cfg.autotune, cfg.shape = int(use_graph), int(autotune), int(shape)
         cfg.precision = 1 if precision == "fp64" else 0
         cfg.adjoint_mode = 0 if adjoint_mode == "store" else 1
+        cfg.mass_correction = int(bool(mass_correction))
+        self.mass_correction = bool(mass_correction)
         self.precision = precision
         self.adjoint_mode = adjoint_mode
         h = C.c_void_p()
@@ -124,16 +131,34 @@ class LevelSetBatch:
                   "lsm_batch_step")
         return v
 
+    def water_volume(self):
+        """(ninst, 4) water volumes (K, S, bulk, total) of the current phi."""
+        v = np.zeros((self.ninst, 4))
+        self._chk(self.lib.lsm_batch_water_volume(self.h, v.ctypes.data), "lsm_batch_water_volume")
+        return v
+
+    def set_mass_target(self, k, volume: float):
+        """Target water volume of instance k for the mass correction (nan: none)."""
+        self._chk(self.lib.lsm_batch_set_mass_target(self.h, int(k), float(volume)), "lsm_batch_set_mass_target")
+
+    def mass_state(self):
+        """(ninst, 4): the last step's volume before the correction V, slope dV/dC, shift C, target."""
+        v = np.zeros((self.ninst, 4))
+        self._chk(self.lib.lsm_batch_mass_state(self.h, v.ctypes.data), "lsm_batch_mass_state")
+        return v
+
     # ------------------------------------------------------------ adjoint
     @staticmethod
     def adjoint_bytes(nodes: int, RNitermax: int, nsteps: int, checkpoint_every: int, precision: str = "fp32",
-                      adjoint_mode: str = "store") -> int:
+                      adjoint_mode: str = "store", mass_correction: bool = False) -> int:
         """Device bytes forward_record allocates for the adjoint state (padding ignored):
-        N (ceil(nsteps / k) + k (5 + c R) + 9) elements, c = 6 (store) or 1 (recompute)."""
+        N (ceil(nsteps / k) + k (5 + m + c R) + 9) elements, c = 6 (store) or 1 (recompute), m = 1
+        with the mass correction (plus N 8-byte words of scratch)."""
         c = 6 if adjoint_mode == "store" else 1
+        m = 1 if mass_correction else 0
         k = min(int(checkpoint_every), int(nsteps))
-        arrays = -(-int(nsteps) // k) + k * (5 + c * int(RNitermax)) + 9
-        return int(nodes) * arrays * (8 if precision == "fp64" else 4)
+        arrays = -(-int(nsteps) // k) + k * (5 + m + c * int(RNitermax)) + 9
+        return int(nodes) * arrays * (8 if precision == "fp64" else 4) + (8 * int(nodes) if m else 0)
 
     def forward_record(self, nsteps: int, checkpoint_every: int = 4):
         self._chk(self.lib.lsm_batch_forward_record(self.h, int(nsteps), int(checkpoint_every)),
