@@ -320,7 +320,7 @@ BATCH_ALGO_BYTES = {
     "k_reinit_z": 12.0 * 4,      # d, s, metrics(9); d
     "k_sign_reinit_z": 12.0 * 4, # phi0, metrics(9); s, d
     "k_contra": 15.0 * 4,        # u(3), metrics(9); W(3)
-    "k_volume": 4.0 + 8.0,       # phi (FP32) + FP64 cell volume (+ coordinates of interface cells only)
+    "k_vol_scan": 4.0 + 8.0,     # phi (FP32) + FP64 cell volume (interface cells listed for k_vol_iface)
     "k_bc_full": 8.0,
 }
 
@@ -556,7 +556,7 @@ FWDADJ_BYTES = {
     "k_reinit_rec_z": 18 * 4,      # d, s, metrics(9); d, adjoint coefficients(6)
     "k_sign_reinit_rec_z": 18 * 4, # phi0, metrics(9); s, d, adjoint coefficients(6)
     "k_adj_reinit_c": 8 * 4,       # lam, coefficients(6); lam_out
-    "k_volume": 4 + 8,             # phi (FP32) + fixed-point cell volume (interface-cell coordinates not counted)
+    "k_vol_scan": 4 + 8,           # phi (FP32) + fixed-point cell volume; interface cells listed
     "k_bc_full": 2 * 4,            # phi in, phi out
     "k_adj_stage_x": 8 * 4,        # in, W_x, lamP0, lamPhin (rmw), lamW_x (rmw); lam_in
     "k_adj_stage_y": 7 * 4,        # in, W_y, lamP0, lam_in (rmw), lamW_y (rmw)
@@ -565,7 +565,7 @@ FWDADJ_BYTES = {
     "k_adj_contra": 18 * 4,        # lamW(3), metrics(9), lam_u(3, rmw)
     "k_cvt_in": 8 + 4,
     "k_cvt_out": 4 + 8,
-    "k_volume_slope": 4 + 8,       # as k_volume; the slope dV/dC adds arithmetic on interface cells only
+    "k_iface_scan": 4,             # phi; interface cells listed (the mass correction's adjoint)
     "k_mass_shift": 2 * 4,         # phi in, phi out
     "k_mass_weights": 4,           # phi (interface cells' coordinates and weight atomics not counted)
     "k_tile_sum": 4,               # lam

@@ -132,6 +132,11 @@ int lsm_batch_get_grad_velocity(lsm_batch_handle h, int inst, double* grad_q);
 /* Tile shape in use (index 0..5 as lsm_batch_config.shape, and the brick
    table's TX, TY, TZ). */
 int lsm_batch_shape(lsm_batch_handle h, int* index, int* tx, int* ty, int* tz);
+/* RK stage kernel in use after the first step: 1 plane tiles staged by TMA
+   copies (FP32 batches of one instance with ni a multiple of 4, when the
+   autotuner finds it faster; the environment variable LSM_BATCH_STAGE=tma
+   or =smem forces the choice), 0 staged by the threads, -1 no handle. */
+int lsm_batch_stage_kernel(lsm_batch_handle h);
 /* Total nodes of the batch and kernels launched per physical step. */
 long long lsm_batch_nodes(lsm_batch_handle h);
 int lsm_batch_launches_per_step(lsm_batch_handle h);

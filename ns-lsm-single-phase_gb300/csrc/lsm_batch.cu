@@ -408,8 +408,9 @@ __global__ void __launch_bounds__(256) k_stage_tma(const __grid_constant__ CUten
                 pnn = __ldg(phin + l);
             }
             const unsigned slot = used % kTmaBuf, par = (used / kTmaBuf) & 1u;
-            ++used;
-            if (!mbar_wait(&bar[slot], par)) abort_flag = 1;
+            // a wait that gave up leaves `used` at the copy still owed
+            if (mbar_wait(&bar[slot], par)) ++used;
+            else abort_flag = 1;
             const float (*P)[kTmaBX] = pl[slot];
             const bool interior = col && ij_int && k > 0 && k < nk - 1;
             const bool upz = W2 > 0.f;
@@ -459,7 +460,8 @@ __global__ void __launch_bounds__(256) k_stage_tma(const __grid_constant__ CUten
     }
     if (aborted && t == 0) {
         atomicOr(err, (unsigned)kErrTimeout);
-        // let the copies still in flight land before the CTA's shared memory goes away
+        // let the copies still in flight land before the CTA's shared memory
+        // goes away (each wait bounded again)
         while (used < issued) {
             mbar_wait(&bar[used % kTmaBuf], (used / kTmaBuf) & 1u);
             ++used;
@@ -938,7 +940,7 @@ __global__ void k_bc_reinit(const Inst* __restrict__ inst, int ninst, long long 
 // closed form: one determinant per tetrahedron instead of up to four
 // (equal in exact arithmetic, rounding differs).  G is the geometry type:
 // FP64 for the FP64 stencils, FP32 for the FP32 ones (vertices relative to
-// the cell's first vertex, see k_volume).
+// the cell's first vertex, see k_vol_iface).
 template <typename G>
 __device__ __forceinline__ G tetvol_g(const G (&a)[3], const G (&b)[3], const G (&c)[3], const G (&d)[3]) {
     const G u0 = b[0] - a[0], u1 = b[1] - a[1], u2 = b[2] - a[2];
@@ -1254,16 +1256,19 @@ __device__ void cell_mass_weights(const P (&ph8)[8], const P (&C)[8][3], P Cs, P
     }
 }
 
-// Cells are classified against eps_sims = 2^-52 in the phi type.  Bulk
-// water cells add their precomputed FP64 fixed-point hexahedron volume;
-// each warp packs its interface cells into its first lanes (ballot + rank,
-// in cell order) so their geometry runs on dense lanes, in the stencil
-// precision T (FP32: each interface cell's share carries a relative
-// rounding error of about 1e-7 of that cell's volume).  Every thread keeps
-// 64-bit integer sums over the bricks of one instance; each warp adds them
-// to the instance's accumulators with integer atomics when its CTA moves to
-// another instance and at the end (exact and order-independent: the result
-// does not depend on the schedule; no block-wide barrier).
+// The volume pass runs in two kernels.  k_vol_scan streams every cell of
+// every instance (one thread per cell on the brick table): cells whose
+// eight vertices are water (phi > eps_sims, in the phi type) add their
+// precomputed FP64 hexahedron volume in 64-bit fixed point; interface cells
+// (any other mix) are appended to a list, each warp reserving its slots with
+// one atomic (list order is not fixed; every sum below is an integer sum, so
+// the result does not depend on it).  k_vol_iface then runs the reference's
+// six-tetrahedra split on the listed cells with every lane busy, in the
+// stencil precision on coordinates relative to each cell's first vertex
+// (differences formed in FP64), optionally with the mass correction's slope
+// dK/dC.  Each cell's shares are rounded to multiples of 2^-48 and added to
+// the instance's accumulators with integer atomics after a warp sum: exact
+// and order-independent.
 // exact warp sum of 64-bit integers (two's complement, modulo 2^64): three
 // limbs of 22, 22 and 20 bits, each summed by the warp's integer reduction
 // (32 x 2^22 < 2^32), recombined; every lane gets the sum
@@ -1276,29 +1281,25 @@ __device__ __forceinline__ long long warp_sum_nn(long long v) {
     return (long long)(s0 + (s1 << 22) + (s2 << 44));
 }
 
-// Each instance has four accumulators: K, S, bulk and (SLOPE) the slope
-// A = dK/dC of the mass correction, all in the same fixed point.
-template <typename T, int TX, int TY, int TZ, bool SLOPE>
-__device__ __forceinline__ void volume_body(const Inst* __restrict__ inst, const Brick* __restrict__ bricks,
-                                            int nbricks, const FieldsT<T>& f, const T* __restrict__ phi,
-                                            unsigned long long* __restrict__ acc) {
-    constexpr int NW = TX * TY * TZ / 32;
+// bulk water volumes of the cells and the interface-cell list (SUMS: also
+// add the bulk cells' fixed-point volumes to acc[4 inst + 2])
+template <typename T, int TX, int TY, int TZ, bool SUMS>
+__device__ __forceinline__ void vol_scan_body(const Inst* __restrict__ inst, const Brick* __restrict__ bricks,
+                                              int nbricks, const FieldsT<T>& f, const T* __restrict__ phi,
+                                              unsigned long long* __restrict__ acc, unsigned* __restrict__ list,
+                                              unsigned* __restrict__ count) {
     const T eps = T(kEpsSims);
-    __shared__ long long slot[NW][32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    long long Kq = 0, Sq = 0, Bq = 0, Aq = 0;
+    const int lane = threadIdx.x & 31;
+    long long Bq = 0;
     int cur = -1;
-    // warp-uniform (every thread of the CTA walks the same bricks)
     auto flush = [&]() {
-        const long long v[4] = {warp_sum_nn(Kq), warp_sum_nn(Sq), warp_sum_nn(Bq), SLOPE ? warp_sum_nn(Aq) : 0};
-        if (lane == 0)
-            for (int c = 0; c < 4; ++c)
-                if (v[c] != 0) atomicAdd(acc + 4 * (long long)cur + c, (unsigned long long)v[c]);
-        Kq = Sq = Bq = Aq = 0;
+        const long long v = warp_sum_nn(Bq);
+        if (lane == 0 && v != 0) atomicAdd(acc + 4 * (long long)cur + 2, (unsigned long long)v);
+        Bq = 0;
     };
     for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
         const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
-        if (b.inst != cur) {
+        if (SUMS && b.inst != cur) {
             if (cur >= 0) flush();
             cur = b.inst;
         }
@@ -1309,67 +1310,117 @@ __device__ __forceinline__ void volume_body(const Inst* __restrict__ inst, const
         if (b.i < I.ni - 1 && b.j < I.nj - 1 && b.k < I.nk - 1) {
             l = I.off + b.i + sj * b.j + sk * b.k;
             const long long o[8] = {l, l + 1, l + 1 + sj, l + sj, l + sk, l + 1 + sk, l + 1 + sj + sk, l + sj + sk};
-            // the cell volume is fetched with the corners (one memory round
-            // trip per brick; it is used for water cells only)
-            const long long cv = __ldg(f.cellfix + l);
+            long long cv = 0;
+            if (SUMS) cv = __ldg(f.cellfix + l);
             bool allw = true, alla = true;
 #pragma unroll
             for (int v = 0; v < 8; ++v) {
                 const T p = __ldg(phi + o[v]);
                 allw &= p > eps; alla &= p < -eps;
             }
-            if (allw) Bq += cv;
+            if (SUMS && allw) Bq += cv;
             mix = !allw && !alla;
         }
         const unsigned m = __ballot_sync(0xffffffffu, mix);
         if (m) {
-            if (mix) slot[w][__popc(m & ((1u << lane) - 1u))] = l;
-            __syncwarp();
-            if (lane < __popc(m)) {
-                const long long c = slot[w][lane];
-                const long long o[8] = {c, c + 1, c + 1 + sj, c + sj, c + sk, c + 1 + sk, c + 1 + sj + sk,
-                                        c + sj + sk};
-                // vertex coordinates relative to vertex 0 (differences in FP64,
-                // then rounded to T: the FP32 geometry keeps the cell's own
-                // size as its scale, not the domain's)
-                T P8[8], C[8][3];
-                double X0[3];
-#pragma unroll
-                for (int a = 0; a < 3; ++a) X0[a] = __ldg(f.xyz[a] + c);
-#pragma unroll
-                for (int v = 0; v < 8; ++v) {
-                    P8[v] = __ldg(phi + o[v]);
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) C[v][a] = (T)(__ldg(f.xyz[a] + o[v]) - X0[a]);
-                }
-                double K = 0.0, S = 0.0, A = 0.0;
-                cell_water_fast<T, SLOPE>(P8, C, &K, &S, &A);
-                Kq += __double2ll_rn(K * kVolScale);
-                Sq += __double2ll_rn(S * kVolScale);
-                if (SLOPE) Aq += __double2ll_rn(A * kVolScale);
-            }
-            __syncwarp();
+            unsigned base = 0;
+            if (lane == 0) base = atomicAdd(count, (unsigned)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (mix) list[base + __popc(m & ((1u << lane) - 1u))] = (unsigned)l;
         }
     }
-    if (cur >= 0) flush();
+    if (SUMS && cur >= 0) flush();
 }
 
 template <typename T, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(TX * TY * TZ) k_volume(const Inst* __restrict__ inst,
+__global__ void __launch_bounds__(TX * TY * TZ) k_vol_scan(const Inst* __restrict__ inst,
         const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phi,
-        unsigned long long* __restrict__ acc) {
-    volume_body<T, TX, TY, TZ, false>(inst, bricks, nbricks, f, phi, acc);
+        unsigned long long* __restrict__ acc, unsigned* __restrict__ list, unsigned* __restrict__ count) {
+    vol_scan_body<T, TX, TY, TZ, true>(inst, bricks, nbricks, f, phi, acc, list, count);
 }
-// the same with the mass correction's slope dK/dC
+// the interface-cell list alone (the mass correction's adjoint)
 template <typename T, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(TX * TY * TZ) k_volume_slope(const Inst* __restrict__ inst,
+__global__ void __launch_bounds__(TX * TY * TZ) k_iface_scan(const Inst* __restrict__ inst,
         const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phi,
-        unsigned long long* __restrict__ acc) {
-    volume_body<T, TX, TY, TZ, true>(inst, bricks, nbricks, f, phi, acc);
+        unsigned* __restrict__ list, unsigned* __restrict__ count) {
+    vol_scan_body<T, TX, TY, TZ, false>(inst, bricks, nbricks, f, phi, nullptr, list, count);
+}
+
+// the eight vertex values and the coordinates relative to vertex 0 of the
+// listed cell whose first node is l (instance I)
+template <typename T>
+__device__ __forceinline__ void cell_gather(const Inst& I, const FieldsT<T>& f, const T* __restrict__ phi,
+                                            long long l, long long (&o)[8], T (&P8)[8], T (&C)[8][3]) {
+    const long long sj = I.ni, sk = (long long)I.ni * I.nj;
+    o[0] = l; o[1] = l + 1; o[2] = l + 1 + sj; o[3] = l + sj;
+    o[4] = l + sk; o[5] = l + 1 + sk; o[6] = l + 1 + sj + sk; o[7] = l + sj + sk;
+    double X0[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) X0[a] = __ldg(f.xyz[a] + l);
+#pragma unroll
+    for (int v = 0; v < 8; ++v) {
+        P8[v] = __ldg(phi + o[v]);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) C[v][a] = (T)(__ldg(f.xyz[a] + o[v]) - X0[a]);
+    }
+}
+
+// instance of packed node t (binary search over the node offsets)
+__device__ __forceinline__ int node_instance(const Flat& fl, long long t) {
+    int lo = 0, hi = fl.ninst - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (fl.offs[mid] <= t) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// K and S volumes (and with SLOPE dK/dC) of the listed interface cells into
+// acc[4 inst + 0, 1, 3]: lanes of a warp that all hold one instance add a
+// warp sum, otherwise each lane adds its own
+template <typename T, bool SLOPE>
+__global__ void __launch_bounds__(128) k_vol_iface(Flat fl, FieldsT<T> f, const T* __restrict__ phi,
+                                                   const unsigned* __restrict__ list, const unsigned* __restrict__ count,
+                                                   unsigned long long* __restrict__ acc) {
+    const unsigned FM = 0xffffffffu;
+    const unsigned n = *count;
+    const int lane = threadIdx.x & 31;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long e0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); e0 < n; e0 += stride) {
+        const long long e = e0 + lane;
+        const bool valid = e < n;
+        long long Kq = 0, Sq = 0, Aq = 0;
+        int q = -1;
+        if (valid) {
+            const long long l = list[e];
+            q = node_instance(fl, l);
+            long long o[8];
+            T P8[8], C[8][3];
+            cell_gather(fl.inst[q], f, phi, l, o, P8, C);
+            double K = 0.0, S = 0.0, A = 0.0;
+            cell_water_fast<T, SLOPE>(P8, C, &K, &S, &A);
+            Kq = __double2ll_rn(K * kVolScale);
+            Sq = __double2ll_rn(S * kVolScale);
+            if (SLOPE) Aq = __double2ll_rn(A * kVolScale);
+        }
+        const int q0 = __shfl_sync(FM, q, 0);
+        if (__all_sync(FM, q == q0)) {
+            const long long v[3] = {warp_sum_nn(Kq), warp_sum_nn(Sq), SLOPE ? warp_sum_nn(Aq) : 0};
+            if (lane == 0 && q0 >= 0) {
+                if (v[0]) atomicAdd(acc + 4 * (long long)q0, (unsigned long long)v[0]);
+                if (v[1]) atomicAdd(acc + 4 * (long long)q0 + 1, (unsigned long long)v[1]);
+                if (v[2]) atomicAdd(acc + 4 * (long long)q0 + 3, (unsigned long long)v[2]);
+            }
+        } else if (valid) {
+            if (Kq) atomicAdd(acc + 4 * (long long)q, (unsigned long long)Kq);
+            if (Sq) atomicAdd(acc + 4 * (long long)q + 1, (unsigned long long)Sq);
+            if (SLOPE && Aq) atomicAdd(acc + 4 * (long long)q + 3, (unsigned long long)Aq);
+        }
+    }
 }
 
 // converts each instance's accumulators (K, S, bulk, slope) to volumes and
-// clears them for the next launch of k_volume; with `mass` it also forms the
+// clears them for the next volume pass; with `mass` it also forms the
 // mass correction C = (target - V) / A of the total V (C = 0 without a
 // finite target or without interface), into mass[q] and, when recording,
 // mrec[q]
@@ -1410,62 +1461,30 @@ __global__ void k_mass_shift(Flat fl, const Mass* __restrict__ mass, const T* __
     }
 }
 
-// Adjoint of the shift, part 1: every interface cell of the step's
+// Adjoint of the shift, part 1: every listed interface cell of the step's
 // pre-correction field adds its vertices' weights g_v + C h_v
 // (cell_mass_weights) to wfix in fixed point (integer atomics: exact and
-// order-independent).  Same brick walk and warp packing as k_volume.
-template <typename T, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(TX * TY * TZ) k_mass_weights(const Inst* __restrict__ inst,
-        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phi,
-        const Mass* __restrict__ mass, unsigned long long* __restrict__ wfix) {
-    constexpr int NW = TX * TY * TZ / 32;
-    const T eps = T(kEpsSims);
-    __shared__ long long slot[NW][32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
-        const Inst& I = inst[b.inst];
-        const Mass M = mass[b.inst];
-        const long long sj = I.ni, sk = (long long)I.ni * I.nj;
-        bool mix = false;
-        long long l = 0;
-        if (mass_on(M) && b.i < I.ni - 1 && b.j < I.nj - 1 && b.k < I.nk - 1) {
-            l = I.off + b.i + sj * b.j + sk * b.k;
-            const long long o[8] = {l, l + 1, l + 1 + sj, l + sj, l + sk, l + 1 + sk, l + 1 + sj + sk, l + sj + sk};
-            bool allw = true, alla = true;
+// order-independent).
+template <typename T>
+__global__ void __launch_bounds__(128) k_mass_weights(Flat fl, FieldsT<T> f, const T* __restrict__ phi,
+                                                      const unsigned* __restrict__ list,
+                                                      const unsigned* __restrict__ count, const Mass* __restrict__ mass,
+                                                      unsigned long long* __restrict__ wfix) {
+    const unsigned n = *count;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long l = list[e];
+        const int q = node_instance(fl, l);
+        const Mass M = mass[q];
+        if (!mass_on(M)) continue;
+        long long o[8];
+        T P8[8], C[8][3], W8[8];
+        cell_gather(fl.inst[q], f, phi, l, o, P8, C);
+        cell_mass_weights<T>(P8, C, (T)M.C, W8);
 #pragma unroll
-            for (int v = 0; v < 8; ++v) {
-                const T p = __ldg(phi + o[v]);
-                allw &= p > eps; alla &= p < -eps;
-            }
-            mix = !allw && !alla;
-        }
-        const unsigned m = __ballot_sync(0xffffffffu, mix);
-        if (m) {
-            if (mix) slot[w][__popc(m & ((1u << lane) - 1u))] = l;
-            __syncwarp();
-            if (lane < __popc(m)) {
-                const long long c = slot[w][lane];
-                const long long o[8] = {c, c + 1, c + 1 + sj, c + sj, c + sk, c + 1 + sk, c + 1 + sj + sk,
-                                        c + sj + sk};
-                T P8[8], C[8][3], W8[8];
-                double X0[3];
-#pragma unroll
-                for (int a = 0; a < 3; ++a) X0[a] = __ldg(f.xyz[a] + c);
-#pragma unroll
-                for (int v = 0; v < 8; ++v) {
-                    P8[v] = __ldg(phi + o[v]);
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) C[v][a] = (T)(__ldg(f.xyz[a] + o[v]) - X0[a]);
-                }
-                cell_mass_weights<T>(P8, C, (T)M.C, W8);
-#pragma unroll
-                for (int v = 0; v < 8; ++v) {
-                    const long long q = __double2ll_rn((double)W8[v] * kVolScale);
-                    if (q != 0) atomicAdd(wfix + o[v], (unsigned long long)q);
-                }
-            }
-            __syncwarp();
+        for (int v = 0; v < 8; ++v) {
+            const long long w = __double2ll_rn((double)W8[v] * kVolScale);
+            if (w != 0) atomicAdd(wfix + o[v], (unsigned long long)w);
         }
     }
 }
@@ -1630,22 +1649,41 @@ __device__ __forceinline__ T rec3_vg(T fL, T fC, T fR, T* dL, T* dC, T* dR) {
     return vfma(w0, g, T(1.5) * fC - T(0.5) * fL);
 }
 
-// D = Phi+ - Phi- of a node (stencil s, orientation frozen by w) and the
-// gradient G = lp w dD/ds of lp w D, branch-free
+// One face's reconstruction and its gradient with respect to its three
+// stencil values (rec3_vg).
 template <typename T>
-__device__ __forceinline__ T stage_node_grad(const T (&s)[5], T w, T lp, bool lo, bool hi, T (&G)[5]) {
+struct FaceVG {
+    T v, a, b, c;
+};
+
+// D = Phi+ - Phi- of a node (stencil s, orientation frozen by w) and the
+// gradient G = lp w dD/ds of lp w D, branch-free, with the face - 1/2 of
+// the node shared with the previous node along the axis: that face is the
+// previous node's face + 1/2 with the same stencil whenever the node's M
+// choice equals the previous node's P choice.  `use_prev` takes `prev` for it; `skip_m` (the whole warp
+// takes it) skips its own evaluation.  fp receives the node's face + 1/2,
+// *Pout its P choice.
+template <typename T>
+__device__ __forceinline__ T stage_node_grad_c(const T (&s)[5], T w, T lp, bool lo, bool hi, bool use_prev,
+                                               bool skip_m, const FaceVG<T>& prev, T (&G)[5], FaceVG<T>& fp,
+                                               bool* Pout) {
     const bool up = w > T(0);
     const bool P = up || hi, M = up && !lo;
-    T a, b, c, a2, b2, c2;
-    const T vp = rec3_vg(P ? s[1] : s[4], P ? s[2] : s[3], P ? s[3] : s[2], &a, &b, &c);
-    const T vm = rec3_vg(M ? s[0] : s[3], M ? s[1] : s[2], M ? s[2] : s[1], &a2, &b2, &c2);
+    fp.v = rec3_vg(P ? s[1] : s[4], P ? s[2] : s[3], P ? s[3] : s[2], &fp.a, &fp.b, &fp.c);
+    FaceVG<T> fm = prev;
+    if (!skip_m) {
+        FaceVG<T> g;
+        g.v = rec3_vg(M ? s[0] : s[3], M ? s[1] : s[2], M ? s[2] : s[1], &g.a, &g.b, &g.c);
+        if (!use_prev) fm = g;
+    }
     const T k = lp * w;
-    G[0] = -k * (M ? a2 : T(0));
-    G[1] = k * ((P ? a : T(0)) - (M ? b2 : c2));
-    G[2] = k * ((P ? b : c) - (M ? c2 : b2));
-    G[3] = k * ((P ? c : b) - (M ? T(0) : a2));
-    G[4] = k * (P ? T(0) : a);
-    return vp - vm;
+    G[0] = -k * (M ? fm.a : T(0));
+    G[1] = k * ((P ? fp.a : T(0)) - (M ? fm.b : fm.c));
+    G[2] = k * ((P ? fp.b : fp.c) - (M ? fm.c : fm.b));
+    G[3] = k * ((P ? fp.c : fp.b) - (M ? T(0) : fm.a));
+    G[4] = k * (P ? T(0) : fp.a);
+    *Pout = P;
+    return fp.v - fm.v;
 }
 
 // Stage adjoint, x part (adjoint map 0: bricks of 8 whole rows of one
@@ -1671,21 +1709,73 @@ __global__ void __launch_bounds__(256) k_adj_stage_x(const Inst* __restrict__ in
         const bool jk_int = j >= 1 && j <= nj - 2 && k >= 1 && k <= nk - 2;
         const long long rowbase = I.off + (long long)ni * (j + (long long)nj * k);
         const int nc = (ni + 31) >> 5;
-        // G_x of chunk c (zero outside the row and at non-interior nodes)
+        // face + 1/2 of lane 31 of the last evaluated chunk (last_c), its P
+        // choice and whether it was evaluated
+        FaceVG<T> fpl{T(0), T(0), T(0), T(0)};
+        bool Pl = false, hl = false;
+        int last_c = -2;
+        // G_x of chunk c (zero outside the row and at non-interior nodes).
+        // Each node evaluates its face + 1/2; its face - 1/2 is the previous
+        // node's face + 1/2 (lane - 1, or lane 31 of the previous chunk) when
+        // their stencil choices agree, and is evaluated only when a lane of
+        // the warp needs it.
         auto eval = [&](int c, T (&G)[5], T& D, T& lp) {
+            const unsigned FM = 0xffffffffu;
 #pragma unroll
             for (int p = 0; p < 5; ++p) G[p] = T(0);
             D = lp = T(0);
             const int ii = (c << 5) + lane;
-            if (c >= 0 && c < nc && ii < ni) {
-                const long long l = rowbase + ii;
-                lp = __ldg(lamP0 + l);
-                if (jk_int && ii >= 1 && ii <= ni - 2) {
-                    const T sv[5] = {ii >= 2 ? __ldg(in + l - 2) : T(0), __ldg(in + l - 1), __ldg(in + l),
-                                     __ldg(in + l + 1), ii <= ni - 3 ? __ldg(in + l + 2) : T(0)};
-                    D = stage_node_grad(sv, __ldg(f.W[0] + l), lp, ii == 1, ii == ni - 2, G);
-                }
+            const bool inr = c >= 0 && c < nc && ii < ni;
+            const bool nint = inr && jk_int && ii >= 1 && ii <= ni - 2;
+            const long long l = rowbase + ii;
+            T wv = T(0), sv[5] = {T(0), T(0), T(0), T(0), T(0)};
+            if (inr) lp = __ldg(lamP0 + l);
+            if (nint) {
+                wv = __ldg(f.W[0] + l);
+                sv[0] = ii >= 2 ? __ldg(in + l - 2) : T(0);
+                sv[1] = __ldg(in + l - 1);
+                sv[2] = __ldg(in + l);
+                sv[3] = __ldg(in + l + 1);
+                sv[4] = ii <= ni - 3 ? __ldg(in + l + 2) : T(0);
             }
+            const bool up = wv > T(0);
+            const bool P = up || ii == ni - 2, M = up && ii != 1;
+            FaceVG<T> fp{T(0), T(0), T(0), T(0)};
+            if (nint) fp.v = rec3_vg(P ? sv[1] : sv[4], P ? sv[2] : sv[3], P ? sv[3] : sv[2], &fp.a, &fp.b, &fp.c);
+            FaceVG<T> pv;
+            pv.v = __shfl_up_sync(FM, fp.v, 1);
+            pv.a = __shfl_up_sync(FM, fp.a, 1);
+            pv.b = __shfl_up_sync(FM, fp.b, 1);
+            pv.c = __shfl_up_sync(FM, fp.c, 1);
+            bool Pv = __shfl_up_sync(FM, (int)P, 1) != 0, hv = __shfl_up_sync(FM, (int)nint, 1) != 0;
+            if (lane == 0) {
+                pv = fpl;
+                Pv = Pl;
+                hv = hl && last_c == c - 1;
+            }
+            const bool reuse = !nint || (hv && M == Pv);
+            FaceVG<T> fm = pv;
+            if (!__all_sync(FM, reuse)) {
+                FaceVG<T> g;
+                g.v = rec3_vg(M ? sv[0] : sv[3], M ? sv[1] : sv[2], M ? sv[2] : sv[1], &g.a, &g.b, &g.c);
+                if (!reuse) fm = g;
+            }
+            if (nint) {
+                const T k = lp * wv;
+                G[0] = -k * (M ? fm.a : T(0));
+                G[1] = k * ((P ? fp.a : T(0)) - (M ? fm.b : fm.c));
+                G[2] = k * ((P ? fp.b : fp.c) - (M ? fm.c : fm.b));
+                G[3] = k * ((P ? fp.c : fp.b) - (M ? T(0) : fm.a));
+                G[4] = k * (P ? T(0) : fp.a);
+                D = fp.v - fm.v;
+            }
+            fpl.v = __shfl_sync(FM, fp.v, 31);
+            fpl.a = __shfl_sync(FM, fp.a, 31);
+            fpl.b = __shfl_sync(FM, fp.b, 31);
+            fpl.c = __shfl_sync(FM, fp.c, 31);
+            Pl = __shfl_sync(FM, (int)P, 31) != 0;
+            hl = __shfl_sync(FM, (int)nint, 31) != 0;
+            last_c = c;
         };
         // march chunks a .. b-1 (outputs), with chunk a-1 primed
         auto segment = [&](int a, int b) {
@@ -1745,7 +1835,10 @@ __global__ void __launch_bounds__(256) k_adj_stage_x(const Inst* __restrict__ in
 // Stage adjoint, y (AX = 1, adjoint map 1) or z (AX = 2, map 2) part: each
 // thread marches one line along AX over adj_shape(map) outputs, keeping
 // windows of five G, lamP0 and D values in registers; lam_in -= c3 acc,
-// lamW_AX -= c3 lamP0 D.
+// lamW_AX -= c3 lamP0 D.  The face - 1/2 of a node is carried from the
+// previous node of the line when their stencil choices agree
+// (stage_node_grad_c); a warp evaluates it only when one of its lanes needs
+// it.
 template <typename T, int AX>
 __global__ void __launch_bounds__(256) k_adj_stage_m(const Inst* __restrict__ inst, const Brick* __restrict__ bmap,
         int nb, FieldsT<T> f, const T* __restrict__ in, const T* __restrict__ lamP0, T* __restrict__ lam_in,
@@ -1775,6 +1868,8 @@ __global__ void __launch_bounds__(256) k_adj_stage_m(const Inst* __restrict__ in
 #pragma unroll
             for (int p = 0; p < 5; ++p) g[a][p] = T(0);
         }
+        FaceVG<T> fpp{T(0), T(0), T(0), T(0)};   // face + 1/2 of the previous node and its P choice
+        bool Pp = false, hp = false;
         for (int q = m0 - 2; q < m1 + 2; ++q) {
             const int jo = q - 2;   // output position: window index 2 after the shift
             const bool wo = col && jo >= m0 && jo < m1;
@@ -1792,16 +1887,23 @@ __global__ void __launch_bounds__(256) k_adj_stage_m(const Inst* __restrict__ in
                 for (int p = 0; p < 5; ++p) g[a][p] = g[a + 1][p];
             }
             T G[5] = {T(0), T(0), T(0), T(0), T(0)};
-            T D = T(0), lp = T(0);
-            if (col && q >= 0 && q < nm) {
-                const long long l = base + st * q;
-                lp = __ldg(lamP0 + l);
-                if (line && q >= 1 && q <= nm - 2) {
-                    const T sv[5] = {q >= 2 ? __ldg(in + l - 2 * st) : T(0), __ldg(in + l - st), __ldg(in + l),
-                                     __ldg(in + l + st), q <= nm - 3 ? __ldg(in + l + 2 * st) : T(0)};
-                    D = stage_node_grad(sv, __ldg(f.W[AX] + l), lp, q == 1, q == nm - 2, G);
-                }
+            T D = T(0), lp = T(0), wv = T(0);
+            const bool inr = col && q >= 0 && q < nm, nint = line && q >= 1 && q <= nm - 2;
+            const long long l = base + st * q;
+            if (inr) lp = __ldg(lamP0 + l);
+            if (nint) wv = __ldg(f.W[AX] + l);
+            const bool reuse = !nint || (hp && (wv > T(0) && q != 1) == Pp);
+            const bool skip_m = __all_sync(0xffffffffu, reuse);
+            if (nint) {
+                const T sv[5] = {q >= 2 ? __ldg(in + l - 2 * st) : T(0), __ldg(in + l - st), __ldg(in + l),
+                                 __ldg(in + l + st), q <= nm - 3 ? __ldg(in + l + 2 * st) : T(0)};
+                FaceVG<T> fpn;
+                bool Pn;
+                D = stage_node_grad_c(sv, wv, lp, q == 1, q == nm - 2, reuse, skip_m, fpp, G, fpn, &Pn);
+                fpp = fpn;
+                Pp = Pn;
             }
+            hp = nint;
             lpw[4] = lp;
             dw[4] = D;
 #pragma unroll
@@ -2038,18 +2140,14 @@ LSM_BATCH_RUNNER(RunSignReinit, k_sign_reinit,
                  (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* p0, T* dout,
                   unsigned* err, cudaStream_t s),
                  (inst, bi, nb, f, p0, dout, err))
-LSM_BATCH_RUNNER(RunVolume, k_volume,
+LSM_BATCH_RUNNER(RunVolScan, k_vol_scan,
                  (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi,
-                  unsigned long long* part, cudaStream_t s),
-                 (inst, bi, nb, f, phi, part))
-LSM_BATCH_RUNNER(RunVolumeSlope, k_volume_slope,
-                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi,
-                  unsigned long long* part, cudaStream_t s),
-                 (inst, bi, nb, f, phi, part))
-LSM_BATCH_RUNNER(RunMassWeights, k_mass_weights,
-                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi, const Mass* m,
-                  unsigned long long* wfix, cudaStream_t s),
-                 (inst, bi, nb, f, phi, m, wfix))
+                  unsigned long long* acc, unsigned* list, unsigned* count, cudaStream_t s),
+                 (inst, bi, nb, f, phi, acc, list, count))
+LSM_BATCH_RUNNER(RunIfaceScan, k_iface_scan,
+                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi, unsigned* list,
+                  unsigned* count, cudaStream_t s),
+                 (inst, bi, nb, f, phi, list, count))
 
 template <typename T, int TX, int TY, int TZ>
 struct Occupancy {
@@ -2057,7 +2155,7 @@ struct Occupancy {
         const int nt = TX * TY * TZ;
         switch (kernel) {
         case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_contra<T, TX, TY, TZ>, nt, 0); break;
-        default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_volume<T, TX, TY, TZ>, nt, 0); break;
+        default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_vol_scan<T, TX, TY, TZ>, nt, 0); break;
         }
     }
 };
@@ -2172,11 +2270,19 @@ void bc_reinit(const Inst* inst, int ninst, long long nface, FieldsT<T> f, BC bc
     ProfScope ps_("k_bc_reinit", s);
     k_bc_reinit<T><<<flat_blocks(nface), 256, 0, s>>>(inst, ninst, nface, bc, f, din, dout);
 }
+inline unsigned list_blocks() { return 152 * 8; }
 template <typename T>
-void volume(int shape, int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi,
-            unsigned long long* acc, bool slope, cudaStream_t s) {
-    if (slope) dispatch<RunVolumeSlope, T>(shape, grid, inst, bi, nb, f, phi, acc, s);
-    else dispatch<RunVolume, T>(shape, grid, inst, bi, nb, f, phi, acc, s);
+void volume(int shape, int grid, const Inst* inst, const Brick* bi, int nb, const Flat& fl, FieldsT<T> f,
+            const T* phi, unsigned long long* acc, bool slope, unsigned* list, unsigned* count, cudaStream_t s) {
+    cudaMemsetAsync(count, 0, sizeof(unsigned), s);
+    dispatch<RunVolScan, T>(shape, grid, inst, bi, nb, f, phi, acc, list, count, s);
+    if (slope) {
+        ProfScope ps_("k_vol_iface_slope", s);
+        k_vol_iface<T, true><<<list_blocks(), 128, 0, s>>>(fl, f, phi, list, count, acc);
+    } else {
+        ProfScope ps_("k_vol_iface", s);
+        k_vol_iface<T, false><<<list_blocks(), 128, 0, s>>>(fl, f, phi, list, count, acc);
+    }
 }
 void volume_final(int ninst, unsigned long long* acc, double* vols, const double* target, Mass* mass, Mass* mrec,
                   cudaStream_t s) {
@@ -2191,8 +2297,13 @@ void mass_shift(const Flat& fl, const Mass* mass, const T* src, T* dst, cudaStre
 template <typename T>
 void mass_adjoint(int shape, int grid, const Inst* inst, const Brick* bi, int nb, const Brick* bmap2, int nb2,
                   const Flat& fl, FieldsT<T> f, const T* phi_pre, const Mass* mass, T* lam, unsigned long long* wfix,
-                  double* part, double* ssum, cudaStream_t s) {
-    dispatch<RunMassWeights, T>(shape, grid, inst, bi, nb, f, phi_pre, mass, wfix, s);
+                  double* part, double* ssum, unsigned* list, unsigned* count, cudaStream_t s) {
+    cudaMemsetAsync(count, 0, sizeof(unsigned), s);
+    dispatch<RunIfaceScan, T>(shape, grid, inst, bi, nb, f, phi_pre, list, count, s);
+    {
+        ProfScope ps_("k_mass_weights", s);
+        k_mass_weights<T><<<list_blocks(), 128, 0, s>>>(fl, f, phi_pre, list, count, mass, wfix);
+    }
     {
         ProfScope ps_("k_tile_sum", s);
         k_tile_sum<T><<<std::min(nb2, 152 * 8), 256, 0, s>>>(inst, bmap2, nb2, lam, part);
@@ -2283,11 +2394,12 @@ void adj_contra(const Flat& fl, FieldsT<T> f, const T* w0, const T* w1, const T*
     template void adj_reinit_c<T>(int, const Inst*, const Brick*, int, const T*, long long, const T*, T*,           \
                                   cudaStream_t);                                                                \
     template int adj_reinit_c_blocks_per_sm<T>();                                                               \
-    template void volume<T>(int, int, const Inst*, const Brick*, int, FieldsT<T>, const T*, unsigned long long*,   \
-                             bool, cudaStream_t);                                                                    \
+    template void volume<T>(int, int, const Inst*, const Brick*, int, const Flat&, FieldsT<T>, const T*,           \
+                            unsigned long long*, bool, unsigned*, unsigned*, cudaStream_t);                          \
     template void mass_shift<T>(const Flat&, const Mass*, const T*, T*, cudaStream_t);                                 \
     template void mass_adjoint<T>(int, int, const Inst*, const Brick*, int, const Brick*, int, const Flat&, FieldsT<T>, \
-                                  const T*, const Mass*, T*, unsigned long long*, double*, double*, cudaStream_t);     \
+                                  const T*, const Mass*, T*, unsigned long long*, double*, double*, unsigned*,         \
+                                  unsigned*, cudaStream_t);                                                          \
     template void adj_face<T>(const Flat&, int, long long, BC, int, const T*, const T*, const T*, double, double, T*, \
                               cudaStream_t);                                                                          \
     template void adj_stage<T>(const int*, const Inst*, const Brick* const*, const int*, FieldsT<T>, const T*,      \

@@ -76,6 +76,15 @@ struct __align__(16) Brick {
     int inst, bx, by, bz;
 };
 
+// A flat walk of the packed nodes (one thread per node, the instance found
+// by binary search over the node offsets).
+struct Flat {
+    const Inst* inst;
+    const long long* offs;  // ninst + 1 node offsets
+    int ninst;
+    long long n;            // total nodes
+};
+
 // tile shapes the autotuner chooses from (threads per brick = TX*TY*TZ)
 constexpr int kNumShapes = 5;
 struct Shape { int tx, ty, tz; };
@@ -136,15 +145,17 @@ void reinit_z(int kind, int grid, const Inst* inst, const Brick* bmap2, int nb, 
               T* dout2, T* cf, long long ld, unsigned* err, cudaStream_t s);
 template <typename T>
 int reinit_z_blocks_per_sm();
-// water volume of every instance: k_volume adds 64-bit fixed-point sums
-// (K, S, bulk and, with `slope`, dK/dC) to acc[4 * inst + c] (zero on
-// entry); volume_final writes vols[4 * inst + 0..3] = (K, S, bulk, total)
-// and clears acc; with `mass` (target volumes `target`, NaN = none) it also
-// forms each instance's mass correction into mass[inst] and, when mrec is
-// not null, mrec[inst]
+// water volume of every instance: the cells' 64-bit fixed-point sums (K, S,
+// bulk and, with `slope`, dK/dC) are added to acc[4 * inst + c] (zero on
+// entry) by a streaming pass that also lists the interface cells (list: at
+// least one entry per cell of the batch; count: one word, reset here) and a
+// pass over that list; volume_final writes vols[4 * inst + 0..3] = (K, S,
+// bulk, total) and clears acc; with `mass` (target volumes `target`, NaN =
+// none) it also forms each instance's mass correction into mass[inst] and,
+// when mrec is not null, mrec[inst]
 template <typename T>
-void volume(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, FieldsT<T> f, const T* phi,
-            unsigned long long* acc, bool slope, cudaStream_t s);
+void volume(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, const Flat& fl, FieldsT<T> f,
+            const T* phi, unsigned long long* acc, bool slope, unsigned* list, unsigned* count, cudaStream_t s);
 void volume_final(int ninst, unsigned long long* acc, double* vols, const double* target, Mass* mass, Mass* mrec,
                   cudaStream_t s);
 // fixed-point hexahedron volume of every cell of one instance (static
@@ -153,7 +164,7 @@ void volume_final(int ninst, unsigned long long* acc, double* vols, const double
 void cell_hex(long long off, int ni, int nj, int nk, const double* x, const double* y, const double* z,
               long long* cellfix, cudaStream_t s);
 // resident CTAs per SM of a brick kernel of tile shape `shape` (FP32):
-// kernel 0 k_contra, other k_volume
+// kernel 0 k_contra, other k_vol_scan
 int max_blocks_per_sm(int shape, int kernel);
 
 // ------------------------------------------------------------ adjoint
@@ -172,12 +183,6 @@ __host__ __device__ constexpr AdjShape adj_shape(int map) {
     return map == 0 ? AdjShape{0, 8, 1}
                     : map == 1 ? AdjShape{32, 32, 8} : map == 2 ? AdjShape{32, 8, 32} : AdjShape{30, kReinRY - 2, 32};
 }
-struct Flat {
-    const Inst* inst;
-    const long long* offs;  // ninst + 1 node offsets
-    int ninst;
-    long long n;            // total nodes
-};
 // Reverse of one bcond_lsm face (face = 0..5: i1, im, j1, jm, k1, km) on the
 // adjoint field lam, in place.  The forward values that decide the BigPhi
 // switch are evaluated from the pre-BC field P0, given as
@@ -217,12 +222,13 @@ void mass_shift(const Flat& fl, const Mass* mass, const T* src, T* dst, cudaStre
 // Reverse of the shift phi' = phi + C(phi) in place on lam (the adjoint of
 // phi'): lam -= (sum(lam) / A) (dK/dphi + C d(dK/dC)/dphi), evaluated on
 // the step's pre-correction field phi_pre; wfix (N 64-bit words, zero on
-// entry and on exit) and part (one double per tile of adjoint map 2), ssum
-// (one per instance) are scratch
+// entry and on exit), part (one double per tile of adjoint map 2), ssum
+// (one per instance) and the interface-cell list (list, count) are scratch
 template <typename T>
 void mass_adjoint(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, const Brick* bmap2,
                   int nb2, const Flat& fl, FieldsT<T> f, const T* phi_pre, const Mass* mass, T* lam,
-                  unsigned long long* wfix, double* part, double* ssum, cudaStream_t s);
+                  unsigned long long* wfix, double* part, double* ssum, unsigned* list, unsigned* count,
+                  cudaStream_t s);
 // lam_u_c += sum_m M[m][c] dt lamW_m  (the W = dt M u chain rule)
 template <typename T>
 void adj_contra(const Flat& fl, FieldsT<T> f, const T* lamW0, const T* lamW1, const T* lamW2, T* lu0, T* lu1,

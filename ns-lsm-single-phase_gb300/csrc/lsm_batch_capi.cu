@@ -4,10 +4,12 @@
 // pseudo-steps), the CUDA graph of one physical step, the FP64 mass
 // correction and the checkpointed adjoint (forward_record keeping the last
 // segment's internals / backward).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <initializer_list>
@@ -58,7 +60,9 @@ struct lsm_batch {
     int namap[4] = {0, 0, 0, 0}, agrid[4] = {1, 1, 1, 1};
     int sgrid = 1, acgrid = 1, rzgrid = 1;   // CTAs of the map-2 kernels: stage, k_adj_reinit_c, reinit_z
     bool reinit_march = true;   // plain pseudo-steps march in k (reinit_z) rather than walk the brick table
-    unsigned long long* d_vacc = nullptr;   // volume accumulators, 4 per instance (k_volume)
+    unsigned long long* d_vacc = nullptr;   // volume accumulators, 4 per instance
+    unsigned* d_ilist = nullptr;            // interface cells of a volume pass (N entries) and their count
+    unsigned* d_icount = nullptr;
     double* d_vols = nullptr;
     // mass correction: per-instance target volumes (NaN: none) and the last
     // step's correction; adjoint scratch (N fixed-point weights, one partial
@@ -72,6 +76,12 @@ struct lsm_batch {
     unsigned* d_err = nullptr;
     int shape = 0, grid = 0;
     bool tuned = false;
+    // TMA-staged RK stage (FP32, one instance, ni a multiple of 4): 4-D
+    // tensor maps (ni, nj, nk, arrays) over the field arena and the adjoint
+    // arena, whose arrays are ld elements apart
+    bool tma_eligible = false, tma_stage = false, tma_adj = false;
+    CUtensorMap tm_field{}, tm_adjmap{};
+    int tgrid = 1;
     cudaGraphExec_t exec = nullptr;
     // adjoint state: one allocation, carved by adj_view
     int rec_steps = 0, rec_ck = 0;
@@ -133,6 +143,43 @@ inline unsigned cblocks(long long n) { return (unsigned)std::max<long long>(1, s
 size_t array_stride(long long n, size_t esz) {
     const size_t raw = (size_t)n * esz;
     return (raw + 4095) / 4096 * 4096 + 2304;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library)
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiled encode_tiled() {
+    static EncodeTiled fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiled)p;
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+// 4-D map (x, y, z, array) of `narrays` FP32 arrays of one instance, ld
+// elements apart from `base`, box 40 x 12 x 1 x 1 (the stage's plane tile
+// with its halo); false when the driver refuses it
+bool encode_stage_map(const lsm_batch* b, void* base, long long narrays, CUtensorMap* out) {
+    EncodeTiled fn = encode_tiled();
+    if (!fn || narrays < 1) return false;
+    const auto& I = b->inst[0];
+    const cuuint64_t dim[4] = {(cuuint64_t)I.ni, (cuuint64_t)I.nj, (cuuint64_t)I.nk, (cuuint64_t)narrays};
+    const cuuint64_t stride[3] = {(cuuint64_t)I.ni * 4, (cuuint64_t)I.ni * I.nj * 4, (cuuint64_t)b->ld * 4};
+    const cuuint32_t box[4] = {40, 12, 1, 1}, estr[4] = {1, 1, 1, 1};
+    return fn(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dim, stride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 bool on_device(const void* p) {
@@ -258,6 +305,8 @@ int build_bricks(lsm_batch* b, int shape) {
     const int prz = std::max(1, b->prec ? lsm::batch::reinit_z_blocks_per_sm<double>()
                                         : lsm::batch::reinit_z_blocks_per_sm<float>());
     b->rzgrid = std::max(1, std::min(b->namap[2], sms * prz));
+    if (b->tma_eligible)
+        b->tgrid = std::max(1, std::min(b->namap[2], sms * std::max(1, lsm::batch::stage_tma_blocks_per_sm())));
     b->shape = shape;
     BCU(b, cudaStreamSynchronize(b->stream));
     return LSM_OK;
@@ -304,6 +353,39 @@ T* rec_d(const lsm_batch* b, const Rec<T>& r, int k) {
     return b->cfg.adjoint_mode == 0 ? r.D : r.D + (long long)k * (long long)b->ld;
 }
 
+// One RK stage: the TMA-staged kernel when the batch uses it and the input
+// is an array of a mapped arena, else the shared-memory-staged one.
+template <typename T>
+void enqueue_stage(lsm_batch* b, FieldsT<T> f, const T* phin, const T* in, T* out, int s) {
+    namespace B = lsm::batch;
+    if constexpr (sizeof(T) == 4) {
+        if (b->tma_stage) {
+            const char* p = (const char*)in;
+            const size_t row = b->ld * sizeof(float);
+            const CUtensorMap* map = nullptr;
+            long long a = -1;
+            const char* fb = (const char*)b->field_arena;
+            if (p >= fb && p < fb + row * 21 && (size_t)(p - fb) % row == 0) {
+                map = &b->tm_field;
+                a = (long long)((size_t)(p - fb) / row);
+            } else if (b->tma_adj && b->adj) {
+                const char* ab = (const char*)b->adj;
+                if (p >= ab && p < ab + b->adj_bytes && (size_t)(p - ab) % row == 0) {
+                    map = &b->tm_adjmap;
+                    a = (long long)((size_t)(p - ab) / row);
+                }
+            }
+            if (map && a < (1LL << 31)) {
+                B::stage_tma(b->tgrid, map, (int)a, b->d_inst, b->d_amap[2], b->namap[2], f, phin, in, out, kC[s][0],
+                             kC[s][1], kC[s][2], b->d_err, b->stream);
+                return;
+            }
+        }
+    }
+    B::stage<T>(b->sgrid, b->d_inst, b->d_amap[2], b->namap[2], f, phin, in, out, kC[s][0], kC[s][1], kC[s][2],
+                b->stream);
+}
+
 // One physical step phin -> phi_out (phi_out may alias phin; nullptr skips
 // the final bcond_lsm).  With `rec` the stage outputs, the pseudo-step
 // outputs (before the final bcond_lsm) and the sign field are kept; `vol`
@@ -323,8 +405,10 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
     const bool mc = b->cfg.mass_correction != 0;
     const bool coef = rec && b->cfg.adjoint_mode == 0;   // recorded step storing adjoint coefficients
     if (rec && !coef) f.sgn = rec->sgn;
+    const Flat fl{b->d_inst, b->d_offs, b->ninst, b->N};
     if (vol && !mc) {
-        B::volume<T>(sh, gr, b->d_inst, b->d_brick, nb, f, phin, b->d_vacc, false, b->stream);
+        B::volume<T>(sh, gr, b->d_inst, b->d_brick, nb, fl, f, phin, b->d_vacc, false, b->d_ilist, b->d_icount,
+                     b->stream);
         B::volume_final(b->ninst, b->d_vacc, b->d_vols, nullptr, nullptr, nullptr, b->stream);
     }
     // the field the final bcond_lsm writes
@@ -333,8 +417,7 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
     T* S[3] = {rec ? rec->A[0] : f.stage[0], rec ? rec->A[1] : f.stage[1], rec ? rec->A[2] : f.stage[0]};
     const T* in[3] = {phin, S[0], S[1]};
     for (int s = 0; s < 3; ++s) {
-        B::stage<T>(b->sgrid, b->d_inst, b->d_amap[2], b->namap[2], f, phin, in[s], S[s], kC[s][0], kC[s][1], kC[s][2],
-                    b->stream);
+        enqueue_stage<T>(b, f, phin, in[s], S[s], s);
         B::bc_stage<T>(b->d_inst, b->ninst, b->nface, bc, phin, in[s], S[s], kC[s][0], kC[s][1], b->stream);
     }
     const int R = b->cfg.RNitermax;
@@ -378,9 +461,10 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
     if (mc) {
         // FP64 water volume of the result, the correction C = (target - V) / A
         // and phi_out = result + C
-        B::volume<T>(sh, gr, b->d_inst, b->d_brick, nb, f, res, b->d_vacc, true, b->stream);
+        B::volume<T>(sh, gr, b->d_inst, b->d_brick, nb, fl, f, res, b->d_vacc, true, b->d_ilist, b->d_icount,
+                     b->stream);
         B::volume_final(b->ninst, b->d_vacc, b->d_vols, b->d_target, b->d_mass, mrec, b->stream);
-        if (phi_out) B::mass_shift<T>(Flat{b->d_inst, b->d_offs, b->ninst, b->N}, b->d_mass, res, phi_out, b->stream);
+        if (phi_out) B::mass_shift<T>(fl, b->d_mass, res, phi_out, b->stream);
     }
 }
 
@@ -424,8 +508,9 @@ int autotune(lsm_batch* b) {
             &a[s], &br[s],
             [&]() {
                 B::contra<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, b->stream);
-                B::volume<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, f.phi, b->d_vacc, false,
-                                 b->stream);
+                B::volume<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks,
+                                 Flat{b->d_inst, b->d_offs, b->ninst, b->N}, f, f.phi, b->d_vacc, false, b->d_ilist,
+                                 b->d_icount, b->stream);
                 B::volume_final(b->ninst, b->d_vacc, b->d_vols, nullptr, nullptr, nullptr, b->stream);
             },
             [&]() {
@@ -450,7 +535,37 @@ int autotune(lsm_batch* b) {
     }
     const bool march = a[best_a] + zm < a[best_b] + br[best_b];
     b->reinit_march = march;
-    return done(build_bricks(b, march ? best_a : best_b));
+    const int bs = build_bricks(b, march ? best_a : best_b);
+    if (bs != LSM_OK) return done(bs);
+    // the RK stage: plane tiles staged by TMA copies or by the threads
+    if (b->tma_eligible) {
+        float ms_plain = 0.f, ms_tma = 0.f;
+        const int st2 = timed(
+            &ms_plain, &ms_tma,
+            [&]() {
+                B::stage<float>(b->sgrid, b->d_inst, b->d_amap[2], b->namap[2], f, f.phi, f.phi, f.stage[0], 1.0, 0.0,
+                                1.0, b->stream);
+            },
+            [&]() {
+                B::stage_tma(b->tgrid, &b->tm_field, 0, b->d_inst, b->d_amap[2], b->namap[2], f, f.phi, f.phi,
+                             f.stage[0], 1.0, 0.0, 1.0, b->d_err, b->stream);
+            });
+        if (st2 != LSM_OK) return done(st2);
+        b->tma_stage = ms_tma < ms_plain;
+    }
+    return done(LSM_OK);
+}
+
+// LSM_BATCH_STAGE=tma or =smem forces the RK stage kernel (tests,
+// measurements); otherwise the autotuner times both (when the batch is
+// eligible for the TMA one), and without autotuning the TMA one is used
+// where eligible.
+int stage_override() {
+    const char* e = std::getenv("LSM_BATCH_STAGE");
+    if (!e) return -1;
+    if (!std::strcmp(e, "tma")) return 1;
+    if (!std::strcmp(e, "smem")) return 0;
+    return -1;
 }
 
 int prepare(lsm_batch* b) {
@@ -464,7 +579,10 @@ int prepare(lsm_batch* b) {
             const int sh = std::min(std::max(b->cfg.shape, 0), 5);
             BTRY(build_bricks(b, sh == 5 ? 0 : sh));
             b->reinit_march = sh == 5;
+            b->tma_stage = b->tma_eligible;
         }
+        const int ov = stage_override();
+        if (ov >= 0) b->tma_stage = ov == 1 && b->tma_eligible;
         b->tuned = true;
     }
     if (b->cfg.use_graph && !b->exec) {
@@ -579,6 +697,8 @@ int forward_record_t(lsm_batch* b, int nsteps, int ck) {
         }
         BCU(b, cudaMalloc(&b->adj, bytes));
         b->adj_bytes = bytes;
+        b->tma_adj = b->tma_eligible &&
+                     encode_stage_map(b, b->adj, (long long)(bytes / (b->ld * sizeof(float))), &b->tm_adjmap);
     }
     if (b->cfg.mass_correction && !b->wfix) {
         // adjoint scratch of the mass correction (the weights start at zero
@@ -619,6 +739,7 @@ int forward_record_t(lsm_batch* b, int nsteps, int ck) {
     unsigned flags = 0;
     BCU(b, cudaMemcpyAsync(&flags, b->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream));
     BCU(b, cudaStreamSynchronize(b->stream));
+    if (flags & lsm::kErrTimeout) return fail(b, LSM_ERR_CUDA, "a TMA copy of the RK stage did not complete");
     if (flags & lsm::kErrNonFinite) return fail(b, LSM_ERR_NONFINITE, "non-finite phi in the batch");
     b->rec_live = true;
     return LSM_OK;
@@ -639,7 +760,7 @@ void adj_step(lsm_batch* b, AdjView<T>& v, const Rec<T>& r, const T* phin, const
     // reverse of the mass correction phi^{n+1} = P + C(P), in place on lam
     if (b->cfg.mass_correction)
         B::mass_adjoint<T>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, b->d_amap[2], b->namap[2], fl, f,
-                           r.P, m, v.lam, b->wfix, b->d_tpart, b->d_ssum, b->stream);
+                           r.P, m, v.lam, b->wfix, b->d_tpart, b->d_ssum, b->d_ilist, b->d_icount, b->stream);
     auto faces = [&](int kind, const T* pn, const T* in, const T* out, double c1, double c2) {
         for (int face = 5; face >= 0; --face)
             B::adj_face<T>(fl, face, b->nplane[face >> 1], bc, kind, pn, in, out, c1, c2, v.lam, b->stream);
@@ -762,6 +883,10 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
     }
     b->off.push_back(n);
     b->N = n;
+    if (n >= (1LL << 32)) {   // the interface-cell list holds 32-bit node indices
+        delete b;
+        return LSM_ERR_BAD_SHAPE;
+    }
     auto cleanup = [&](int st) {
         lsm_batch_destroy(b);
         return st;
@@ -779,6 +904,8 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
     if (cudaMalloc(&b->d_vols, sizeof(double) * 4 * ninst) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMallocHost(&b->h_vols, sizeof(double) * 4 * ninst) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->d_err, sizeof(unsigned)) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
+    if (cudaMalloc(&b->d_ilist, sizeof(unsigned) * (size_t)n) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
+    if (cudaMalloc(&b->d_icount, sizeof(unsigned)) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->d_target, sizeof(double) * ninst) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->d_mass, sizeof(Mass) * ninst) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     {
@@ -812,6 +939,9 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
     };
     if (b->prec) wire(b->f64, (double*)nullptr);
     else wire(b->f32, (float*)nullptr);
+    // the TMA-staged stage needs whole 16-byte rows of one instance
+    if (!b->prec && ninst == 1 && inst[0].ni % 4 == 0)
+        b->tma_eligible = encode_stage_map(b, b->field_arena, 21, &b->tm_field);
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     *out = b;
     return LSM_OK;
@@ -825,7 +955,8 @@ int lsm_batch_destroy(lsm_batch_handle b) {
     for (void* p : {b->field_arena, (void*)b->xyz, (void*)b->staging, (void*)b->d_inst, (void*)b->d_offs,
                     (void*)b->d_brick, (void*)b->d_amap[0], (void*)b->d_amap[1], (void*)b->d_amap[2],
                     (void*)b->d_amap[3], (void*)b->d_vacc, (void*)b->d_vols, (void*)b->d_err, b->adj,
-                    (void*)b->d_target, (void*)b->d_mass, (void*)b->wfix, (void*)b->d_tpart, (void*)b->d_ssum})
+                    (void*)b->d_target, (void*)b->d_mass, (void*)b->wfix, (void*)b->d_tpart, (void*)b->d_ssum,
+                    (void*)b->d_ilist, (void*)b->d_icount})
         if (p) cudaFree(p);
     if (b->h_vols) cudaFreeHost(b->h_vols);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
@@ -907,6 +1038,7 @@ int lsm_batch_step(lsm_batch_handle b, int nsteps, double* volumes) {
                                b->stream));
     BCU(b, cudaStreamSynchronize(b->stream));
     if (volumes) std::memcpy(volumes, b->h_vols, sizeof(double) * 4 * b->ninst);
+    if (flags & lsm::kErrTimeout) return fail(b, LSM_ERR_CUDA, "a TMA copy of the RK stage did not complete");
     if (flags & lsm::kErrNonFinite) return fail(b, LSM_ERR_NONFINITE, "non-finite phi in the batch");
     return LSM_OK;
 }
@@ -982,12 +1114,13 @@ int lsm_batch_water_volume(lsm_batch_handle b, double* volumes) {
     Dev guard(b->device);
     BTRY(prepare(b));
     namespace B = lsm::batch;
+    const Flat fl{b->d_inst, b->d_offs, b->ninst, b->N};
     if (b->prec)
-        B::volume<double>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, b->f64, b->f64.phi, b->d_vacc, false,
-                          b->stream);
+        B::volume<double>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, fl, b->f64, b->f64.phi, b->d_vacc,
+                          false, b->d_ilist, b->d_icount, b->stream);
     else
-        B::volume<float>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, b->f32, b->f32.phi, b->d_vacc, false,
-                         b->stream);
+        B::volume<float>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, fl, b->f32, b->f32.phi, b->d_vacc,
+                         false, b->d_ilist, b->d_icount, b->stream);
     B::volume_final(b->ninst, b->d_vacc, b->d_vols, nullptr, nullptr, nullptr, b->stream);
     BCU(b, cudaGetLastError());
     BCU(b, cudaMemcpyAsync(b->h_vols, b->d_vols, sizeof(double) * 4 * b->ninst, cudaMemcpyDeviceToHost, b->stream));
@@ -1023,13 +1156,16 @@ int lsm_batch_shape(lsm_batch_handle b, int* index, int* tx, int* ty, int* tz) {
 
 long long lsm_batch_nodes(lsm_batch_handle b) { return b ? b->N : 0; }
 
+int lsm_batch_stage_kernel(lsm_batch_handle b) { return b ? (b->tma_stage ? 1 : 0) : -1; }
+
 int lsm_batch_launches_per_step(lsm_batch_handle b) {
     if (!b) return 0;
-    // volume 2, contra 1, three stages x (stencil + faces) 6, then
-    // RNitermax pseudo-steps (the first with the sign field) + final faces,
-    // or one full bcond pass; the mass correction's shift 1
+    // volume 3 (scan, interface cells, final), contra 1, three stages x
+    // (stencil + faces) 6, then RNitermax pseudo-steps (the first with the
+    // sign field) + final faces, or one full bcond pass; the mass
+    // correction's shift 1
     const int R = b->cfg.RNitermax;
-    return 2 + 1 + 6 + (R > 0 ? R + 1 : 1) + (b->cfg.mass_correction ? 1 : 0);
+    return 3 + 1 + 6 + (R > 0 ? R + 1 : 1) + (b->cfg.mass_correction ? 1 : 0);
 }
 
 const char* lsm_batch_last_error(lsm_batch_handle b) { return b ? b->err.c_str() : ""; }

@@ -122,6 +122,7 @@ SIGNATURES = {
     "lsm_batch_get_grad_velocity": (_i, [_vp, _i, _vp]),
     "lsm_batch_shape": (_i, [_vp] + [C.POINTER(_i)] * 4),
     "lsm_batch_nodes": (C.c_longlong, [_vp]),
+    "lsm_batch_stage_kernel": (_i, [_vp]),
     "lsm_batch_launches_per_step": (_i, [_vp]),
     "lsm_batch_last_error": (C.c_char_p, [_vp]),
     "lsm_profile_enable": (_i, [_i]),

@@ -199,6 +199,11 @@ class LevelSetBatch:
         return int(self.lib.lsm_batch_nodes(self.h))
 
     @property
+    def stage_kernel(self) -> str:
+        """RK stage kernel in use: "tma" (plane tiles staged by TMA copies) or "smem"."""
+        return "tma" if self.lib.lsm_batch_stage_kernel(self.h) == 1 else "smem"
+
+    @property
     def launches_per_step(self) -> int:
         return int(self.lib.lsm_batch_launches_per_step(self.h))
 

@@ -21,7 +21,8 @@ every 10 steps.
     often); at 1e-8 the quotients agree;
   * the frozen-sign-field assumption in isolation: on a field with every
     |phi| >= 2 eps over the run (no band edge to cross), central differences
-    at 1e-6 agree with the adjoint in every direction, phi0 included;
+    at 1e-6 agree with the adjoint in every direction, phi0 included (1e-5,
+    ten times inside the bar);
   * the FP32 gradient follows the FP64 one.
 """
 import numpy as np
@@ -208,7 +209,7 @@ def test_frozen_sign_field_is_exact_away_from_the_band_edge(lib_built):
             worst = max(worst, abs(an - fd1) / abs(fd1))
     b.close()
     print("no band edge: worst relative error over 12 directions at h = 1e-6: %.2e" % worst)
-    assert worst <= 1e-6
+    assert worst <= 1e-5
 
 
 def test_fp32_gradient_follows_fp64(big):

@@ -19,10 +19,14 @@ phi += C with C = (target - V) / A.  Checked here:
   * the FP64 adjoint with the correction equals central differences of the
     corrected forward along 24 seeded directions (1e-4 relative; the shift's
     derivative includes dA/dphi through second-order dual numbers), each at
-    step 1e-7 where its quotients at h and h/2 agree, else at 1e-9;
+    step 1e-5 where its quotients at h and h/2 agree, else at 1e-6 (the
+    fixed-point volume makes the corrected forward noisy at ~1e-11 in the
+    loss, too much for smaller steps);
   * the checkpoint interval does not change that gradient (bit-identical);
   * the FP32 adjoint follows the FP64 one.
 """
+import math
+
 import numpy as np
 import pytest
 
@@ -172,17 +176,23 @@ def test_fp64_adjoint_with_mass_correction_matches_central_differences(oracle, m
             x0 = [c["it"].q for c in mcases]
             f = lambda t: loss(qs=[x + t * vv for x, vv in zip(x0, v)])  # noqa: E731
             an = sum(float((g * vv).sum()) for g, vv in zip(gq, v))
-        # the configured step where the quotients at h and h/2 agree, else a
-        # smaller one (a branch point of the piecewise-smooth step crossed)
+        # the corrected forward is piecewise smooth, and its fixed-point
+        # volume (2^-48 per cell) moves C by ~1e-13 between nearby inputs, a
+        # noise of ~1e-11 in the loss: steps of 1e-5 (else 1e-6 when a
+        # branch point was crossed), errors relative to the larger of the
+        # directional derivative and its typical size |g| |v| / sqrt(n)
+        gn = math.sqrt(sum(float((g * g).sum()) for g in (gphi if d % 2 == 0 else gq)))
+        vn = math.sqrt(sum(float((vv * vv).sum()) for vv in v))
+        scale = max(abs(an), gn * vn / math.sqrt(sum(vv.size for vv in v)))
         used = None
-        for h in (1e-7, 1e-9):
+        for h in (1e-5, 1e-6):
             fd1 = (f(h) - f(-h)) / (2 * h)
             fd2 = (f(0.5 * h) - f(-0.5 * h)) / h
-            if abs(fd1 - fd2) <= 1e-5 * max(abs(fd1), 1e-12):
+            if abs(fd1 - fd2) <= 1e-4 * scale:
                 used = h
                 break
-        assert used is not None, (d, fd1, fd2)
-        err = abs(an - fd1) / max(abs(fd1), 1e-12)
+        assert used is not None, (d, fd1, fd2, scale)
+        err = abs(an - fd1) / scale
         rows.append("h=%g err=%.1e" % (used, err))
         worst = max(worst, err)
     b.close()
