@@ -667,14 +667,26 @@ def run_fwdadj(args):
         vol64 = float(b64.water_volume()[0, 3])
         b64.close()
         torch.cuda.empty_cache()
-        b32 = make_batch()
-        b32.set_mass_target(0, target)
-        b32.step(NS, volumes=False)
-        phi32 = b32.get_phi(0, like=phi0)
-        vol32 = float(b32.water_volume()[0, 3])
-        b32.close()
+        def fp32_run():
+            b32 = make_batch()
+            b32.set_mass_target(0, target)
+            b32.step(NS, volumes=False)
+            out = b32.get_phi(0, like=phi0), float(b32.water_volume()[0, 3])
+            b32.close()
+            return out
+
+        phi32, vol32 = fp32_run()
         band = phi64.abs() < 4.0 * eps
+        # the same run without the FP64 stage near the interface
+        os.environ["LSM_BATCH_BAND64"] = "0"
+        try:
+            phi32n, _ = fp32_run()
+        finally:
+            del os.environ["LSM_BATCH_BAND64"]
+        err_no64 = float((phi32n - phi64).abs()[band].max())
+        del phi32n
         acc = {"steps": NS, "band_linf_phi_err": float((phi32 - phi64).abs()[band].max()),
+               "band_linf_phi_err_without_fp64_interface_terms": err_no64,
                "band": "|phi64| < 4 epslsm (6 cells)",
                "volume_rel_diff": abs(vol32 - vol64) / abs(vol64),
                "volume_drift_fp32": abs(vol32 - target) / target, "volume_drift_fp64": abs(vol64 - target) / target,

@@ -29,6 +29,14 @@
  * frozen), giving dL/dphi^0 and dL/dq(2:4) (the velocity is held fixed over
  * the recorded steps).
  *
+ * Near the interface the FP32 stencils keep FP64 metric terms: stage nodes
+ * whose input |phi| is below 2 eps take their contravariant velocity from
+ * the FP64 metrics and velocity passed to set_geometry / set_velocity (kept
+ * per node, 15 FP64 arrays) and combine the stage in FP64 over the FP32
+ * WENO differences; the adjoint uses the FP32 contravariant velocity there
+ * too.  The environment variable LSM_BATCH_BAND64=0 at lsm_batch_create
+ * leaves this out (measurements).
+ *
  * Mass correction (config.mass_correction = 1; no counterpart in the
  * reference's Sussman branch, whose GlobalMassCorrection, src/levelsetmethod.
  * F90:245-266, feeds the geometric reinitialisation instead): after each

@@ -167,7 +167,36 @@ __global__ void __launch_bounds__(TX * TY * TZ) k_contra(const Inst* __restrict_
     }
 }
 
+// FP64 contravariant velocity x dt of one instance from the FP64 metrics
+// (m64: 9 arrays) and velocity (u64: 3 arrays), the same formula as
+// k_contra; packed base arrays, `off` the instance's first node
+__global__ void k_w64(long long off, long long n, double dt, const double* const* __restrict__ m64,
+                      const double* const* __restrict__ u64, double* const* __restrict__ w64) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const long long l = off + t;
+        const double u = u64[0][l], v = u64[1][l], w = u64[2][l];
+#pragma unroll
+        for (int m = 0; m < 3; ++m) w64[m][l] = dt * (m64[3 * m][l] * u + m64[3 * m + 1][l] * v + m64[3 * m + 2][l] * w);
+    }
+}
+
 // ------------------------------------------------------------ RK stage
+
+// The stage output c1 phi^n + c2 phi1 - c3 R at node l.  FP32 batches that
+// keep the FP64 contravariant velocity combine the nodes within kBand64 eps
+// of the interface in FP64: R = sum_m W64_m D_m over the FP32 differences D.
+template <typename T>
+__device__ __forceinline__ T stage_out(const FieldsT<T>& f, long long l, bool interior, T c1, T c2, T c3, T pn, T w2,
+                                       T R, T D0, T D1, T D2, T eps) {
+    if constexpr (sizeof(T) == 4) {
+        if (interior && f.W64[0] && fabsf(w2) < kBand64 * eps) {
+            const double r = __ldg(f.W64[0] + l) * (double)D0 + __ldg(f.W64[1] + l) * (double)D1 +
+                             __ldg(f.W64[2] + l) * (double)D2;
+            return (T)((double)c1 * (double)pn + (double)c2 * (double)w2 - (double)c3 * r);
+        }
+    }
+    return c1 * pn + c2 * w2 - c3 * R;
+}
 
 // RK stage on the tiles of adjoint map 2 (32 x 8 columns marching 32 planes
 // in k).  Each plane of phi1 is staged in shared memory with a two-node
@@ -256,12 +285,13 @@ __global__ void __launch_bounds__(256) k_stage_z(const Inst* __restrict__ inst, 
             const bool all_reuse = __all_sync(FM, reuse);
             if (col) {
                 T R = T(0);
+                T D0 = T(0), D1 = T(0), D2 = T(0);
                 if (interior) {
                     const int x = tx + 2, y = ty + 2;
-                    R = W0 * weno_diff(i > 1 ? P[y][x - 2] : T(0), P[y][x - 1], w2, P[y][x + 1],
-                                       i < ni - 2 ? P[y][x + 2] : T(0), W0, i == 1, i == ni - 2);
-                    R = vfma(W1, weno_diff(j > 1 ? P[y - 2][x] : T(0), P[y - 1][x], w2, P[y + 1][x],
-                                           j < nj - 2 ? P[y + 2][x] : T(0), W1, j == 1, j == nj - 2), R);
+                    D0 = weno_diff(i > 1 ? P[y][x - 2] : T(0), P[y][x - 1], w2, P[y][x + 1],
+                                   i < ni - 2 ? P[y][x + 2] : T(0), W0, i == 1, i == ni - 2);
+                    D1 = weno_diff(j > 1 ? P[y - 2][x] : T(0), P[y - 1][x], w2, P[y + 1][x],
+                                   j < nj - 2 ? P[y + 2][x] : T(0), W1, j == 1, j == nj - 2);
                     const T p2 = k < nk - 2 ? w4 : T(0);
                     const T fp = rec3(Pk ? w1 : p2, Pk ? w2 : w3, Pk ? w3 : w2);
                     T fm = fpz;
@@ -270,11 +300,15 @@ __global__ void __launch_bounds__(256) k_stage_z(const Inst* __restrict__ inst, 
                         const T g = rec3(Mk ? m2 : w3, Mk ? w1 : w2, Mk ? w2 : w1);
                         if (!reuse) fm = g;
                     }
-                    R = vfma(W2, fp - fm, R);
+                    D2 = fp - fm;
+                    R = W0 * D0;
+                    R = vfma(W1, D1, R);
+                    R = vfma(W2, D2, R);
                     fpz = fp;
                     Pz = Pk;
                 }
-                out[cb + sk * k] = c1 * pn + c2 * w2 - c3 * R;
+                out[cb + sk * k] = stage_out(f, cb + sk * k, interior, c1, c2, c3, pn, w2, R, D0, D1, D2,
+                                             ipar<T>(I.eps, I.eps64));
             }
             have = interior;
             w0 = w1;
@@ -419,12 +453,13 @@ __global__ void __launch_bounds__(256) k_stage_tma(const __grid_constant__ CUten
             const bool all_reuse = __all_sync(FM, reuse);
             if (col) {
                 float R = 0.f;
+                float D0 = 0.f, D1 = 0.f, D2 = 0.f;
                 if (interior) {
                     const int x = tx + 4, y = ty + 2;
-                    R = W0 * weno_diff(i > 1 ? P[y][x - 2] : 0.f, P[y][x - 1], w2, P[y][x + 1],
-                                       i < ni - 2 ? P[y][x + 2] : 0.f, W0, i == 1, i == ni - 2);
-                    R = vfma(W1, weno_diff(j > 1 ? P[y - 2][x] : 0.f, P[y - 1][x], w2, P[y + 1][x],
-                                           j < nj - 2 ? P[y + 2][x] : 0.f, W1, j == 1, j == nj - 2), R);
+                    D0 = weno_diff(i > 1 ? P[y][x - 2] : 0.f, P[y][x - 1], w2, P[y][x + 1],
+                                   i < ni - 2 ? P[y][x + 2] : 0.f, W0, i == 1, i == ni - 2);
+                    D1 = weno_diff(j > 1 ? P[y - 2][x] : 0.f, P[y - 1][x], w2, P[y + 1][x],
+                                   j < nj - 2 ? P[y + 2][x] : 0.f, W1, j == 1, j == nj - 2);
                     const float p2 = k < nk - 2 ? w4 : 0.f;
                     const float fp = rec3(Pk ? w1 : p2, Pk ? w2 : w3, Pk ? w3 : w2);
                     float fm = fpz;
@@ -433,11 +468,14 @@ __global__ void __launch_bounds__(256) k_stage_tma(const __grid_constant__ CUten
                         const float g = rec3(Mk ? m2 : w3, Mk ? w1 : w2, Mk ? w2 : w1);
                         if (!reuse) fm = g;
                     }
-                    R = vfma(W2, fp - fm, R);
+                    D2 = fp - fm;
+                    R = W0 * D0;
+                    R = vfma(W1, D1, R);
+                    R = vfma(W2, D2, R);
                     fpz = fp;
                     Pz = Pk;
                 }
-                out[cb + sk * k] = c1 * pn + c2 * w2 - c3 * R;
+                out[cb + sk * k] = stage_out(f, cb + sk * k, interior, c1, c2, c3, pn, w2, R, D0, D1, D2, I.eps);
             }
             have = interior;
             // every thread is done with this plane's buffer: it takes plane k + 2
@@ -1649,41 +1687,22 @@ __device__ __forceinline__ T rec3_vg(T fL, T fC, T fR, T* dL, T* dC, T* dR) {
     return vfma(w0, g, T(1.5) * fC - T(0.5) * fL);
 }
 
-// One face's reconstruction and its gradient with respect to its three
-// stencil values (rec3_vg).
-template <typename T>
-struct FaceVG {
-    T v, a, b, c;
-};
-
 // D = Phi+ - Phi- of a node (stencil s, orientation frozen by w) and the
-// gradient G = lp w dD/ds of lp w D, branch-free, with the face - 1/2 of
-// the node shared with the previous node along the axis: that face is the
-// previous node's face + 1/2 with the same stencil whenever the node's M
-// choice equals the previous node's P choice.  `use_prev` takes `prev` for it; `skip_m` (the whole warp
-// takes it) skips its own evaluation.  fp receives the node's face + 1/2,
-// *Pout its P choice.
+// gradient G = lp w dD/ds of lp w D, branch-free
 template <typename T>
-__device__ __forceinline__ T stage_node_grad_c(const T (&s)[5], T w, T lp, bool lo, bool hi, bool use_prev,
-                                               bool skip_m, const FaceVG<T>& prev, T (&G)[5], FaceVG<T>& fp,
-                                               bool* Pout) {
+__device__ __forceinline__ T stage_node_grad(const T (&s)[5], T w, T lp, bool lo, bool hi, T (&G)[5]) {
     const bool up = w > T(0);
     const bool P = up || hi, M = up && !lo;
-    fp.v = rec3_vg(P ? s[1] : s[4], P ? s[2] : s[3], P ? s[3] : s[2], &fp.a, &fp.b, &fp.c);
-    FaceVG<T> fm = prev;
-    if (!skip_m) {
-        FaceVG<T> g;
-        g.v = rec3_vg(M ? s[0] : s[3], M ? s[1] : s[2], M ? s[2] : s[1], &g.a, &g.b, &g.c);
-        if (!use_prev) fm = g;
-    }
+    T a, b, c, a2, b2, c2;
+    const T vp = rec3_vg(P ? s[1] : s[4], P ? s[2] : s[3], P ? s[3] : s[2], &a, &b, &c);
+    const T vm = rec3_vg(M ? s[0] : s[3], M ? s[1] : s[2], M ? s[2] : s[1], &a2, &b2, &c2);
     const T k = lp * w;
-    G[0] = -k * (M ? fm.a : T(0));
-    G[1] = k * ((P ? fp.a : T(0)) - (M ? fm.b : fm.c));
-    G[2] = k * ((P ? fp.b : fp.c) - (M ? fm.c : fm.b));
-    G[3] = k * ((P ? fp.c : fp.b) - (M ? T(0) : fm.a));
-    G[4] = k * (P ? T(0) : fp.a);
-    *Pout = P;
-    return fp.v - fm.v;
+    G[0] = -k * (M ? a2 : T(0));
+    G[1] = k * ((P ? a : T(0)) - (M ? b2 : c2));
+    G[2] = k * ((P ? b : c) - (M ? c2 : b2));
+    G[3] = k * ((P ? c : b) - (M ? T(0) : a2));
+    G[4] = k * (P ? T(0) : a);
+    return vp - vm;
 }
 
 // Stage adjoint, x part (adjoint map 0: bricks of 8 whole rows of one
@@ -1709,73 +1728,21 @@ __global__ void __launch_bounds__(256) k_adj_stage_x(const Inst* __restrict__ in
         const bool jk_int = j >= 1 && j <= nj - 2 && k >= 1 && k <= nk - 2;
         const long long rowbase = I.off + (long long)ni * (j + (long long)nj * k);
         const int nc = (ni + 31) >> 5;
-        // face + 1/2 of lane 31 of the last evaluated chunk (last_c), its P
-        // choice and whether it was evaluated
-        FaceVG<T> fpl{T(0), T(0), T(0), T(0)};
-        bool Pl = false, hl = false;
-        int last_c = -2;
-        // G_x of chunk c (zero outside the row and at non-interior nodes).
-        // Each node evaluates its face + 1/2; its face - 1/2 is the previous
-        // node's face + 1/2 (lane - 1, or lane 31 of the previous chunk) when
-        // their stencil choices agree, and is evaluated only when a lane of
-        // the warp needs it.
+        // G_x of chunk c (zero outside the row and at non-interior nodes)
         auto eval = [&](int c, T (&G)[5], T& D, T& lp) {
-            const unsigned FM = 0xffffffffu;
 #pragma unroll
             for (int p = 0; p < 5; ++p) G[p] = T(0);
             D = lp = T(0);
             const int ii = (c << 5) + lane;
-            const bool inr = c >= 0 && c < nc && ii < ni;
-            const bool nint = inr && jk_int && ii >= 1 && ii <= ni - 2;
-            const long long l = rowbase + ii;
-            T wv = T(0), sv[5] = {T(0), T(0), T(0), T(0), T(0)};
-            if (inr) lp = __ldg(lamP0 + l);
-            if (nint) {
-                wv = __ldg(f.W[0] + l);
-                sv[0] = ii >= 2 ? __ldg(in + l - 2) : T(0);
-                sv[1] = __ldg(in + l - 1);
-                sv[2] = __ldg(in + l);
-                sv[3] = __ldg(in + l + 1);
-                sv[4] = ii <= ni - 3 ? __ldg(in + l + 2) : T(0);
+            if (c >= 0 && c < nc && ii < ni) {
+                const long long l = rowbase + ii;
+                lp = __ldg(lamP0 + l);
+                if (jk_int && ii >= 1 && ii <= ni - 2) {
+                    const T sv[5] = {ii >= 2 ? __ldg(in + l - 2) : T(0), __ldg(in + l - 1), __ldg(in + l),
+                                     __ldg(in + l + 1), ii <= ni - 3 ? __ldg(in + l + 2) : T(0)};
+                    D = stage_node_grad(sv, __ldg(f.W[0] + l), lp, ii == 1, ii == ni - 2, G);
+                }
             }
-            const bool up = wv > T(0);
-            const bool P = up || ii == ni - 2, M = up && ii != 1;
-            FaceVG<T> fp{T(0), T(0), T(0), T(0)};
-            if (nint) fp.v = rec3_vg(P ? sv[1] : sv[4], P ? sv[2] : sv[3], P ? sv[3] : sv[2], &fp.a, &fp.b, &fp.c);
-            FaceVG<T> pv;
-            pv.v = __shfl_up_sync(FM, fp.v, 1);
-            pv.a = __shfl_up_sync(FM, fp.a, 1);
-            pv.b = __shfl_up_sync(FM, fp.b, 1);
-            pv.c = __shfl_up_sync(FM, fp.c, 1);
-            bool Pv = __shfl_up_sync(FM, (int)P, 1) != 0, hv = __shfl_up_sync(FM, (int)nint, 1) != 0;
-            if (lane == 0) {
-                pv = fpl;
-                Pv = Pl;
-                hv = hl && last_c == c - 1;
-            }
-            const bool reuse = !nint || (hv && M == Pv);
-            FaceVG<T> fm = pv;
-            if (!__all_sync(FM, reuse)) {
-                FaceVG<T> g;
-                g.v = rec3_vg(M ? sv[0] : sv[3], M ? sv[1] : sv[2], M ? sv[2] : sv[1], &g.a, &g.b, &g.c);
-                if (!reuse) fm = g;
-            }
-            if (nint) {
-                const T k = lp * wv;
-                G[0] = -k * (M ? fm.a : T(0));
-                G[1] = k * ((P ? fp.a : T(0)) - (M ? fm.b : fm.c));
-                G[2] = k * ((P ? fp.b : fp.c) - (M ? fm.c : fm.b));
-                G[3] = k * ((P ? fp.c : fp.b) - (M ? T(0) : fm.a));
-                G[4] = k * (P ? T(0) : fp.a);
-                D = fp.v - fm.v;
-            }
-            fpl.v = __shfl_sync(FM, fp.v, 31);
-            fpl.a = __shfl_sync(FM, fp.a, 31);
-            fpl.b = __shfl_sync(FM, fp.b, 31);
-            fpl.c = __shfl_sync(FM, fp.c, 31);
-            Pl = __shfl_sync(FM, (int)P, 31) != 0;
-            hl = __shfl_sync(FM, (int)nint, 31) != 0;
-            last_c = c;
         };
         // march chunks a .. b-1 (outputs), with chunk a-1 primed
         auto segment = [&](int a, int b) {
@@ -1835,10 +1802,7 @@ __global__ void __launch_bounds__(256) k_adj_stage_x(const Inst* __restrict__ in
 // Stage adjoint, y (AX = 1, adjoint map 1) or z (AX = 2, map 2) part: each
 // thread marches one line along AX over adj_shape(map) outputs, keeping
 // windows of five G, lamP0 and D values in registers; lam_in -= c3 acc,
-// lamW_AX -= c3 lamP0 D.  The face - 1/2 of a node is carried from the
-// previous node of the line when their stencil choices agree
-// (stage_node_grad_c); a warp evaluates it only when one of its lanes needs
-// it.
+// lamW_AX -= c3 lamP0 D.
 template <typename T, int AX>
 __global__ void __launch_bounds__(256) k_adj_stage_m(const Inst* __restrict__ inst, const Brick* __restrict__ bmap,
         int nb, FieldsT<T> f, const T* __restrict__ in, const T* __restrict__ lamP0, T* __restrict__ lam_in,
@@ -1868,8 +1832,6 @@ __global__ void __launch_bounds__(256) k_adj_stage_m(const Inst* __restrict__ in
 #pragma unroll
             for (int p = 0; p < 5; ++p) g[a][p] = T(0);
         }
-        FaceVG<T> fpp{T(0), T(0), T(0), T(0)};   // face + 1/2 of the previous node and its P choice
-        bool Pp = false, hp = false;
         for (int q = m0 - 2; q < m1 + 2; ++q) {
             const int jo = q - 2;   // output position: window index 2 after the shift
             const bool wo = col && jo >= m0 && jo < m1;
@@ -1887,23 +1849,16 @@ __global__ void __launch_bounds__(256) k_adj_stage_m(const Inst* __restrict__ in
                 for (int p = 0; p < 5; ++p) g[a][p] = g[a + 1][p];
             }
             T G[5] = {T(0), T(0), T(0), T(0), T(0)};
-            T D = T(0), lp = T(0), wv = T(0);
-            const bool inr = col && q >= 0 && q < nm, nint = line && q >= 1 && q <= nm - 2;
-            const long long l = base + st * q;
-            if (inr) lp = __ldg(lamP0 + l);
-            if (nint) wv = __ldg(f.W[AX] + l);
-            const bool reuse = !nint || (hp && (wv > T(0) && q != 1) == Pp);
-            const bool skip_m = __all_sync(0xffffffffu, reuse);
-            if (nint) {
-                const T sv[5] = {q >= 2 ? __ldg(in + l - 2 * st) : T(0), __ldg(in + l - st), __ldg(in + l),
-                                 __ldg(in + l + st), q <= nm - 3 ? __ldg(in + l + 2 * st) : T(0)};
-                FaceVG<T> fpn;
-                bool Pn;
-                D = stage_node_grad_c(sv, wv, lp, q == 1, q == nm - 2, reuse, skip_m, fpp, G, fpn, &Pn);
-                fpp = fpn;
-                Pp = Pn;
+            T D = T(0), lp = T(0);
+            if (col && q >= 0 && q < nm) {
+                const long long l = base + st * q;
+                lp = __ldg(lamP0 + l);
+                if (line && q >= 1 && q <= nm - 2) {
+                    const T sv[5] = {q >= 2 ? __ldg(in + l - 2 * st) : T(0), __ldg(in + l - st), __ldg(in + l),
+                                     __ldg(in + l + st), q <= nm - 3 ? __ldg(in + l + 2 * st) : T(0)};
+                    D = stage_node_grad(sv, __ldg(f.W[AX] + l), lp, q == 1, q == nm - 2, G);
+                }
             }
-            hp = nint;
             lpw[4] = lp;
             dw[4] = D;
 #pragma unroll
@@ -2315,6 +2270,11 @@ void mass_adjoint(int shape, int grid, const Inst* inst, const Brick* bi, int nb
     ProfScope ps_("k_mass_apply", s);
     k_mass_apply<T><<<(unsigned)std::min<long long>((fl.n + 255) / 256, 152 * 16), 256, 0, s>>>(fl, mass, ssum, lam,
                                                                                                  wfix);
+}
+void w64(long long off, long long n, double dt, const double* const* m64, const double* const* u64,
+         double* const* w, cudaStream_t s) {
+    ProfScope ps_("k_w64", s);
+    k_w64<<<(unsigned)std::min<long long>((n + 255) / 256, 152 * 16), 256, 0, s>>>(off, n, dt, m64, u64, w);
 }
 void cell_hex(long long off, int ni, int nj, int nk, const double* x, const double* y, const double* z,
               long long* cellfix, cudaStream_t s) {

@@ -42,9 +42,15 @@ struct FieldsT {
     T* u[3];           // Cartesian velocity
     T* sgn;            // sign field of the reinitialisation (0 where the lambda correction freezes d)
     const double* xyz[3];  // FP64 coordinates (volume)
+    const double* W64[3];  // FP32 batches: W in FP64 (from the FP64 metrics and velocity) for the
+                           // stage nodes within kBand64 eps of the interface; nullptr: not kept
     long long* cellfix;    // hexahedron volume of cell (i..i+1, j..j+1, k..k+1) in fixed point, by base node
 };
 using Fields = FieldsT<float>;
+
+// Stage nodes whose input |phi| is below kBand64 * eps combine the RK stage
+// with the FP64 contravariant velocity and in FP64 (FP32 batches).
+constexpr float kBand64 = 2.0f;
 
 // Batched water volumes are accumulated as 64-bit fixed point: each cell's
 // FP64 volume is rounded to a multiple of 2^-48 (coordinate units^3) and the
@@ -158,6 +164,11 @@ void volume(int shape, int grid, const Inst* inst, const Brick* bricks, int nbri
             const T* phi, unsigned long long* acc, bool slope, unsigned* list, unsigned* count, cudaStream_t s);
 void volume_final(int ninst, unsigned long long* acc, double* vols, const double* target, Mass* mass, Mass* mrec,
                   cudaStream_t s);
+// FP64 W = dt (grad xi_m . u) of one instance (n nodes from `off`) from the
+// FP64 metrics m64[9] and velocity u64[3] (arrays of device pointers, in
+// device memory)
+void w64(long long off, long long n, double dt, const double* const* m64, const double* const* u64,
+         double* const* w, cudaStream_t s);
 // fixed-point hexahedron volume of every cell of one instance (static
 // geometry); x, y, z and cellfix are the packed base arrays, `off` the
 // instance's first node

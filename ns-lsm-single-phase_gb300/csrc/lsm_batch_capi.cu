@@ -50,6 +50,12 @@ struct lsm_batch {
     void* bufs[6] = {};          // phi, stage0, stage1, d0, d1, sgn
     void* comps[15] = {};        // W[3], m[9], u[3]
     double* xyz = nullptr;       // FP64 coordinates x, y, z (stride ld8); cellfix follows
+    // FP32 batches: FP64 metrics (9), velocity (3) and contravariant velocity
+    // x dt (3) for the stage nodes near the interface (stride ld8), their
+    // device pointer table, and which instances have geometry / velocity set
+    double* f64x = nullptr;
+    double** d_p64 = nullptr;
+    std::vector<char> geom_set, vel_set;
     long long* cellfix = nullptr;  // N fixed-point cell hexahedron volumes
     double* staging = nullptr;   // FP64 scratch for conversions (4 * max instance nodes)
     Inst* d_inst = nullptr;
@@ -131,6 +137,14 @@ __global__ void k_cvt_out(const T* __restrict__ src, int stride, int comp, long 
     for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < n; l += (long long)gridDim.x * blockDim.x)
         dst[l * stride + comp] = (double)src[l];
 }
+// FP64 W of instance q once its FP64 geometry and velocity are both in place
+void update_w64(lsm_batch* b, int q) {
+    if (!b->f64x || !b->geom_set[q] || !b->vel_set[q]) return;
+    const auto& I = b->inst[q];
+    const long long n = (long long)I.ni * I.nj * I.nk;
+    lsm::batch::w64(b->off[q], n, I.dt, b->d_p64, b->d_p64 + 9, b->d_p64 + 12, b->stream);
+}
+
 template <typename T>
 __global__ void k_zero(long long n, T* __restrict__ a) {
     for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < n; l += (long long)gridDim.x * blockDim.x)
@@ -905,6 +919,21 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
     if (cudaMallocHost(&b->h_vols, sizeof(double) * 4 * ninst) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->d_err, sizeof(unsigned)) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->d_ilist, sizeof(unsigned) * (size_t)n) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
+    b->geom_set.assign((size_t)ninst, 0);
+    b->vel_set.assign((size_t)ninst, 0);
+    {
+        // the FP64 stage near the interface (FP32 batches; LSM_BATCH_BAND64=0 leaves it out)
+        const char* e = std::getenv("LSM_BATCH_BAND64");
+        if (!b->prec && !(e && !std::strcmp(e, "0"))) {
+            if (cudaMalloc(&b->f64x, 8 * b->ld8 * 15) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
+            if (cudaMalloc(&b->d_p64, sizeof(double*) * 15) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
+            double* hp[15];
+            for (int a = 0; a < 15; ++a) hp[a] = b->f64x + (size_t)a * b->ld8;
+            if (cudaMemcpy(b->d_p64, hp, sizeof(hp), cudaMemcpyHostToDevice) != cudaSuccess)
+                return cleanup(LSM_ERR_CUDA);
+            cudaMemsetAsync(b->f64x, 0, 8 * b->ld8 * 15, b->stream);
+        }
+    }
     if (cudaMalloc(&b->d_icount, sizeof(unsigned)) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->d_target, sizeof(double) * ninst) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->d_mass, sizeof(Mass) * ninst) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
@@ -936,6 +965,7 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
         }
         for (int c = 0; c < 9; ++c) f.m[c] = (T*)b->comps[3 + c];
         f.cellfix = b->cellfix;
+        for (int c = 0; c < 3; ++c) f.W64[c] = b->f64x ? b->f64x + (size_t)(12 + c) * b->ld8 : nullptr;
     };
     if (b->prec) wire(b->f64, (double*)nullptr);
     else wire(b->f32, (float*)nullptr);
@@ -956,7 +986,7 @@ int lsm_batch_destroy(lsm_batch_handle b) {
                     (void*)b->d_brick, (void*)b->d_amap[0], (void*)b->d_amap[1], (void*)b->d_amap[2],
                     (void*)b->d_amap[3], (void*)b->d_vacc, (void*)b->d_vols, (void*)b->d_err, b->adj,
                     (void*)b->d_target, (void*)b->d_mass, (void*)b->wfix, (void*)b->d_tpart, (void*)b->d_ssum,
-                    (void*)b->d_ilist, (void*)b->d_icount})
+                    (void*)b->d_ilist, (void*)b->d_icount, (void*)b->f64x, (void*)b->d_p64})
         if (p) cudaFree(p);
     if (b->h_vols) cudaFreeHost(b->h_vols);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
@@ -978,8 +1008,15 @@ int lsm_batch_set_geometry(lsm_batch_handle b, int q, const double* x, const dou
     const double* m3[3] = {csi, eta, zet};
     for (int d = 0; d < 3; ++d) {
         BTRY(stage_in(b, m3[d], 3 * n));
-        for (int c = 0; c < 3; ++c) cvt_in(b, 3, c, n, (char*)b->comps[3 + 3 * d + c] + b->esz * o);
+        for (int c = 0; c < 3; ++c) {
+            cvt_in(b, 3, c, n, (char*)b->comps[3 + 3 * d + c] + b->esz * o);
+            if (b->f64x)
+                k_cvt_in<double><<<cblocks(n), 256, 0, b->stream>>>(b->staging, 3, c, n,
+                                                                    b->f64x + (size_t)(3 * d + c) * b->ld8 + o);
+        }
     }
+    b->geom_set[q] = 1;
+    update_w64(b, q);
     // cell_hex indexes from the packed base arrays with the instance offset o
     lsm::batch::cell_hex(o, I.ni, I.nj, I.nk, b->xyz, b->xyz + b->ld8, b->xyz + 2 * b->ld8, b->cellfix, b->stream);
     BCU(b, cudaGetLastError());
@@ -994,7 +1031,14 @@ int lsm_batch_set_velocity(lsm_batch_handle b, int q, const double* qv) {
     const auto& I = b->inst[q];
     const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
     BTRY(stage_in(b, qv, 4 * n));
-    for (int c = 0; c < 3; ++c) cvt_in(b, 4, c + 1, n, (char*)b->comps[12 + c] + b->esz * o);
+    for (int c = 0; c < 3; ++c) {
+        cvt_in(b, 4, c + 1, n, (char*)b->comps[12 + c] + b->esz * o);
+        if (b->f64x)
+            k_cvt_in<double><<<cblocks(n), 256, 0, b->stream>>>(b->staging, 4, c + 1, n,
+                                                                b->f64x + (size_t)(9 + c) * b->ld8 + o);
+    }
+    b->vel_set[q] = 1;
+    update_w64(b, q);
     BCU(b, cudaGetLastError());
     BCU(b, cudaStreamSynchronize(b->stream));
     return LSM_OK;
