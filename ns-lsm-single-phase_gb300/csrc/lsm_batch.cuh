@@ -50,7 +50,7 @@ using Fields = FieldsT<float>;
 
 // Stage nodes whose input |phi| is below kBand64 * eps combine the RK stage
 // with the FP64 contravariant velocity and in FP64 (FP32 batches).
-constexpr float kBand64 = 2.0f;
+constexpr float kBand64 = 1.0f;
 
 // Batched water volumes are accumulated as 64-bit fixed point: each cell's
 // FP64 volume is rounded to a multiple of 2^-48 (coordinate units^3) and the

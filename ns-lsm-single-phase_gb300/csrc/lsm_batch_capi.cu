@@ -82,6 +82,9 @@ struct lsm_batch {
     unsigned* d_err = nullptr;
     int shape = 0, grid = 0;
     bool tuned = false;
+    // the contravariant velocity W = dt (metrics . u) depends only on the
+    // geometry and the velocity: formed once after either changes
+    bool w_stale = true;
     // TMA-staged RK stage (FP32, one instance, ni a multiple of 4): 4-D
     // tensor maps (ni, nj, nk, arrays) over the field arena and the adjoint
     // arena, whose arrays are ld elements apart
@@ -427,7 +430,6 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
     }
     // the field the final bcond_lsm writes
     T* res = mc && rec ? rec->P : phi_out;
-    B::contra<T>(sh, gr, b->d_inst, b->d_brick, nb, f, b->stream);
     T* S[3] = {rec ? rec->A[0] : f.stage[0], rec ? rec->A[1] : f.stage[1], rec ? rec->A[2] : f.stage[0]};
     const T* in[3] = {phin, S[0], S[1]};
     for (int s = 0; s < 3; ++s) {
@@ -582,6 +584,17 @@ int stage_override() {
     return -1;
 }
 
+// W of every instance from the current metrics and velocity (the steps
+// read it; set_geometry / set_velocity mark it stale)
+int refresh_w(lsm_batch* b) {
+    if (!b->w_stale) return LSM_OK;
+    if (b->prec) lsm::batch::contra<double>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, b->f64, b->stream);
+    else lsm::batch::contra<float>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, b->f32, b->stream);
+    BCU(b, cudaGetLastError());
+    b->w_stale = false;
+    return LSM_OK;
+}
+
 int prepare(lsm_batch* b) {
     if (!b->tuned) {
         const bool tune = b->cfg.autotune && !b->prec;
@@ -599,6 +612,7 @@ int prepare(lsm_batch* b) {
         if (ov >= 0) b->tma_stage = ov == 1 && b->tma_eligible;
         b->tuned = true;
     }
+    BTRY(refresh_w(b));
     if (b->cfg.use_graph && !b->exec) {
         cudaGraph_t g = nullptr;
         BCU(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
@@ -1016,6 +1030,7 @@ int lsm_batch_set_geometry(lsm_batch_handle b, int q, const double* x, const dou
         }
     }
     b->geom_set[q] = 1;
+    b->w_stale = true;
     update_w64(b, q);
     // cell_hex indexes from the packed base arrays with the instance offset o
     lsm::batch::cell_hex(o, I.ni, I.nj, I.nk, b->xyz, b->xyz + b->ld8, b->xyz + 2 * b->ld8, b->cellfix, b->stream);
@@ -1038,6 +1053,7 @@ int lsm_batch_set_velocity(lsm_batch_handle b, int q, const double* qv) {
                                                                 b->f64x + (size_t)(9 + c) * b->ld8 + o);
     }
     b->vel_set[q] = 1;
+    b->w_stale = true;
     update_w64(b, q);
     BCU(b, cudaGetLastError());
     BCU(b, cudaStreamSynchronize(b->stream));
@@ -1114,6 +1130,7 @@ int lsm_batch_set_grad_phi(lsm_batch_handle b, int q, const double* g) {
 int lsm_batch_backward(lsm_batch_handle b) {
     if (!b) return LSM_ERR_NULL;
     Dev guard(b->device);
+    BTRY(refresh_w(b));
     return b->prec ? backward_t<double>(b) : backward_t<float>(b);
 }
 
@@ -1204,12 +1221,12 @@ int lsm_batch_stage_kernel(lsm_batch_handle b) { return b ? (b->tma_stage ? 1 : 
 
 int lsm_batch_launches_per_step(lsm_batch_handle b) {
     if (!b) return 0;
-    // volume 3 (scan, interface cells, final), contra 1, three stages x
-    // (stencil + faces) 6, then RNitermax pseudo-steps (the first with the
-    // sign field) + final faces, or one full bcond pass; the mass
-    // correction's shift 1
+    // volume 3 (scan, interface cells, final), three stages x (stencil +
+    // faces) 6, then RNitermax pseudo-steps (the first with the sign field)
+    // + final faces, or one full bcond pass; the mass correction's shift 1
+    // (W is formed outside the step, once per change of its inputs)
     const int R = b->cfg.RNitermax;
-    return 3 + 1 + 6 + (R > 0 ? R + 1 : 1) + (b->cfg.mass_correction ? 1 : 0);
+    return 3 + 6 + (R > 0 ? R + 1 : 1) + (b->cfg.mass_correction ? 1 : 0);
 }
 
 const char* lsm_batch_last_error(lsm_batch_handle b) { return b ? b->err.c_str() : ""; }
