@@ -319,6 +319,8 @@ BATCH_ALGO_BYTES = {
     "k_stage_z": 17.0 / 3.0 * 4,   # phi_prev, phi^n (stages 2-3), W(3); phi
     "k_reinit_z": 12.0 * 4,      # d, s, metrics(9); d
     "k_sign_reinit_z": 12.0 * 4, # phi0, metrics(9); s, d
+    "k_reinit": 12.0 * 4,        # brick-table pseudo-step: d, s, metrics(9); d
+    "k_sign_reinit": 12.0 * 4,   # brick-table first pseudo-step: phi0, metrics(9); s, d
     "k_contra": 15.0 * 4,        # u(3), metrics(9); W(3)
     "k_vol_scan": 4.0 + 8.0,     # phi (FP32) + FP64 cell volume (interface cells listed for k_vol_iface)
     "k_bc_full": 8.0,
