@@ -322,7 +322,7 @@ BATCH_ALGO_BYTES = {
     "k_reinit": 12.0 * 4,        # brick-table pseudo-step: d, s, metrics(9); d
     "k_sign_reinit": 12.0 * 4,   # brick-table first pseudo-step: phi0, metrics(9); s, d
     "k_contra": 15.0 * 4,        # u(3), metrics(9); W(3)
-    "k_vol_scan": 4.0 + 8.0,     # phi (FP32) + FP64 cell volume (interface cells listed for k_vol_iface)
+    "k_vol_scan_z": 4.0 + 8.0,   # phi (FP32) + fixed-point cell volume (interface cells listed for k_vol_iface)
     "k_bc_full": 8.0,
 }
 
@@ -558,7 +558,7 @@ FWDADJ_BYTES = {
     "k_reinit_rec_z": 18 * 4,      # d, s, metrics(9); d, adjoint coefficients(6)
     "k_sign_reinit_rec_z": 18 * 4, # phi0, metrics(9); s, d, adjoint coefficients(6)
     "k_adj_reinit_c": 8 * 4,       # lam, coefficients(6); lam_out
-    "k_vol_scan": 4 + 8,           # phi (FP32) + fixed-point cell volume; interface cells listed
+    "k_vol_scan_z": 4 + 8,         # phi (FP32) + fixed-point cell volume; interface cells listed
     "k_bc_full": 2 * 4,            # phi in, phi out
     "k_adj_stage_x": 8 * 4,        # in, W_x, lamP0, lamPhin (rmw), lamW_x (rmw); lam_in
     "k_adj_stage_y": 7 * 4,        # in, W_y, lamP0, lam_in (rmw), lamW_y (rmw)
@@ -567,7 +567,7 @@ FWDADJ_BYTES = {
     "k_adj_contra": 18 * 4,        # lamW(3), metrics(9), lam_u(3, rmw)
     "k_cvt_in": 8 + 4,
     "k_cvt_out": 4 + 8,
-    "k_iface_scan": 4,             # phi; interface cells listed (the mass correction's adjoint)
+    "k_iface_scan_z": 4,           # phi; interface cells listed (the mass correction's adjoint)
     "k_mass_shift": 2 * 4,         # phi in, phi out
     "k_mass_weights": 4,           # phi (interface cells' coordinates and weight atomics not counted)
     "k_tile_sum": 4,               # lam

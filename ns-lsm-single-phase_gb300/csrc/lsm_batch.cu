@@ -1319,69 +1319,101 @@ __device__ __forceinline__ long long warp_sum_nn(long long v) {
     return (long long)(s0 + (s1 << 22) + (s2 << 44));
 }
 
-// bulk water volumes of the cells and the interface-cell list (SUMS: also
-// add the bulk cells' fixed-point volumes to acc[4 inst + 2])
-template <typename T, int TX, int TY, int TZ, bool SUMS>
-__device__ __forceinline__ void vol_scan_body(const Inst* __restrict__ inst, const Brick* __restrict__ bricks,
-                                              int nbricks, const FieldsT<T>& f, const T* __restrict__ phi,
-                                              unsigned long long* __restrict__ acc, unsigned* __restrict__ list,
-                                              unsigned* __restrict__ count) {
+// Bulk water volumes of the cells and the interface-cell list (SUMS: also
+// add the bulk cells' fixed-point volumes to acc[4 inst + 2]), on the tiles
+// of adjoint map 2: thread (lane, row) owns the cell column (i0 + lane, j0 +
+// row) and marches the tile's planes in k.  A cell's eight vertices are the
+// 2 x 2 quads of planes k and k + 1; a quad is the thread's own node and
+// the one at j + 1 (loaded), with the i + 1 pair from the next lane by a
+// shuffle (the tile's last lane loads it).  Each plane is loaded once, a
+// plane ahead of its use; a quad is reduced to two flags (all water, all
+// air) and a cell is water / air when both of its quads are.
+template <typename T, bool SUMS>
+__global__ void __launch_bounds__(256) k_vol_scan_z(const Inst* __restrict__ inst, const Brick* __restrict__ bmap,
+        int nb, FieldsT<T> f, const T* __restrict__ phi, unsigned long long* __restrict__ acc,
+        unsigned* __restrict__ list, unsigned* __restrict__ count) {
     const T eps = T(kEpsSims);
-    const int lane = threadIdx.x & 31;
+    const unsigned FM = 0xffffffffu;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     long long Bq = 0;
     int cur = -1;
     auto flush = [&]() {
         const long long v = warp_sum_nn(Bq);
-        if (lane == 0 && v != 0) atomicAdd(acc + 4 * (long long)cur + 2, (unsigned long long)v);
+        if (tx == 0 && v != 0) atomicAdd(acc + 4 * (long long)cur + 2, (unsigned long long)v);
         Bq = 0;
     };
-    for (int blk = blockIdx.x; blk < nbricks; blk += gridDim.x) {
-        const Node b = brick_node<TX, TY, TZ>(inst, bricks, blk);
-        if (SUMS && b.inst != cur) {
+    for (int blk = blockIdx.x; blk < nb; blk += gridDim.x) {
+        const ABrick ab = adj_brick(bmap, 2, blk);
+        if (SUMS && ab.inst != cur) {
             if (cur >= 0) flush();
-            cur = b.inst;
+            cur = ab.inst;
         }
-        const Inst& I = inst[b.inst];
-        const long long sj = I.ni, sk = (long long)I.ni * I.nj;
-        bool mix = false;
-        long long l = 0;
-        if (b.i < I.ni - 1 && b.j < I.nj - 1 && b.k < I.nk - 1) {
-            l = I.off + b.i + sj * b.j + sk * b.k;
-            const long long o[8] = {l, l + 1, l + 1 + sj, l + sj, l + sk, l + 1 + sk, l + 1 + sj + sk, l + sj + sk};
-            long long cv = 0;
-            if (SUMS) cv = __ldg(f.cellfix + l);
-            bool allw = true, alla = true;
-#pragma unroll
-            for (int v = 0; v < 8; ++v) {
-                const T p = __ldg(phi + o[v]);
-                allw &= p > eps; alla &= p < -eps;
+        const Inst& I = inst[ab.inst];
+        const int ni = I.ni, nj = I.nj, nk = I.nk;
+        const long long sj = ni, sk = (long long)ni * nj;
+        const int i = ab.i0 + tx, j = ab.j0 + ty;
+        // cells k0 .. kc1 - 1 (a cell's top plane k + 1 stays inside the grid)
+        const int k0 = ab.k0, kc1 = min(k0 + adj_shape(2).oz, nk - 1);
+        const bool cell = i < ni - 1 && j < nj - 1;
+        const bool own = i < ni && j < nj - 1, edge = tx == 31 && i + 1 < ni && j < nj - 1;
+        const long long cb = I.off + i + sj * j;
+        struct Quad {
+            T a, c, ae, ce;   // (i, j), (i, j + 1); the last lane's (i + 1, j), (i + 1, j + 1)
+        };
+        auto ld = [&](int k, Quad& q) {
+            q.a = q.c = q.ae = q.ce = T(0);
+            const long long l = cb + sk * k;
+            if (own) {
+                q.a = __ldg(phi + l);
+                q.c = __ldg(phi + l + sj);
             }
-            if (SUMS && allw) Bq += cv;
-            mix = !allw && !alla;
+            if (edge) {
+                q.ae = __ldg(phi + l + 1);
+                q.ce = __ldg(phi + l + 1 + sj);
+            }
+        };
+        auto flags = [&](const Quad& q, bool& qw, bool& qa) {
+            const T b = __shfl_down_sync(FM, q.a, 1), d = __shfl_down_sync(FM, q.c, 1);
+            const T bb = tx == 31 ? q.ae : b, dd = tx == 31 ? q.ce : d;
+            qw = q.a > eps && bb > eps && q.c > eps && dd > eps;
+            qa = q.a < -eps && bb < -eps && q.c < -eps && dd < -eps;
+        };
+        bool qw0 = false, qa0 = false;
+        Quad qn;
+        long long cv = 0;
+        if (k0 < kc1) {
+            Quad q0;
+            ld(k0, q0);
+            ld(k0 + 1, qn);
+            if (SUMS && cell) cv = __ldg(f.cellfix + cb + sk * k0);
+            flags(q0, qw0, qa0);
         }
-        const unsigned m = __ballot_sync(0xffffffffu, mix);
-        if (m) {
-            unsigned base = 0;
-            if (lane == 0) base = atomicAdd(count, (unsigned)__popc(m));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (mix) list[base + __popc(m & ((1u << lane) - 1u))] = (unsigned)l;
+        for (int k = k0; k < kc1; ++k) {
+            Quad qq;
+            long long cvn = 0;
+            if (k + 1 < kc1) {
+                ld(k + 2, qq);
+                if (SUMS && cell) cvn = __ldg(f.cellfix + cb + sk * (k + 1));
+            }
+            bool qw1, qa1;
+            flags(qn, qw1, qa1);
+            const bool allw = qw0 && qw1, alla = qa0 && qa1;
+            if (SUMS && cell && allw) Bq += cv;
+            const bool mix = cell && !allw && !alla;
+            const unsigned m = __ballot_sync(FM, mix);
+            if (m) {
+                unsigned base = 0;
+                if (tx == 0) base = atomicAdd(count, (unsigned)__popc(m));
+                base = __shfl_sync(FM, base, 0);
+                if (mix) list[base + __popc(m & ((1u << tx) - 1u))] = (unsigned)(cb + sk * k);
+            }
+            qw0 = qw1;
+            qa0 = qa1;
+            qn = qq;
+            cv = cvn;
         }
     }
     if (SUMS && cur >= 0) flush();
-}
-
-template <typename T, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(TX * TY * TZ) k_vol_scan(const Inst* __restrict__ inst,
-        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phi,
-        unsigned long long* __restrict__ acc, unsigned* __restrict__ list, unsigned* __restrict__ count) {
-    vol_scan_body<T, TX, TY, TZ, true>(inst, bricks, nbricks, f, phi, acc, list, count);
-}
-// the interface-cell list alone (the mass correction's adjoint)
-template <typename T, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(TX * TY * TZ) k_iface_scan(const Inst* __restrict__ inst,
-        const Brick* __restrict__ bricks, int nbricks, FieldsT<T> f, const T* __restrict__ phi,
-        unsigned* __restrict__ list, unsigned* __restrict__ count) {
-    vol_scan_body<T, TX, TY, TZ, false>(inst, bricks, nbricks, f, phi, nullptr, list, count);
 }
 
 // the eight vertex values and the coordinates relative to vertex 0 of the
@@ -1528,8 +1560,10 @@ __global__ void __launch_bounds__(128) k_mass_weights(Flat fl, FieldsT<T> f, con
 }
 
 // Adjoint of the shift, part 2: per tile of adjoint map 2 (32 x 8 columns
-// x 32 planes, inside one instance) the FP64 sum of lam over the tile, in a
-// fixed order (each thread its column, then a fixed tree)
+// x 32 planes, inside one instance) the sum of lam over the tile, in a
+// fixed order (each thread its column, then a fixed tree), accumulated in
+// FP64.  FP32 lam is first summed in FP32 over runs of 8 planes (the FP64
+// pipe would otherwise take a conversion and an add per node).
 template <typename T>
 __global__ void __launch_bounds__(256) k_tile_sum(const Inst* __restrict__ inst, const Brick* __restrict__ bmap,
                                                    int nb, const T* __restrict__ lam, double* __restrict__ part) {
@@ -1543,7 +1577,17 @@ __global__ void __launch_bounds__(256) k_tile_sum(const Inst* __restrict__ inst,
         if (i < I.ni && j < I.nj) {
             const long long sk = (long long)I.ni * I.nj;
             const T* p = lam + I.off + i + (long long)I.ni * j;
-            for (int k = ab.k0; k < k1; ++k) sacc += (double)__ldg(p + sk * k);
+            if constexpr (sizeof(T) == 4) {
+                for (int k = ab.k0; k < k1; k += 8) {
+                    float r = 0.f;
+#pragma unroll
+                    for (int u = 0; u < 8; ++u)
+                        if (k + u < k1) r += __ldg(p + sk * (k + u));
+                    sacc += (double)r;
+                }
+            } else {
+                for (int k = ab.k0; k < k1; ++k) sacc += (double)__ldg(p + sk * k);
+            }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
@@ -2095,23 +2139,13 @@ LSM_BATCH_RUNNER(RunSignReinit, k_sign_reinit,
                  (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* p0, T* dout,
                   unsigned* err, cudaStream_t s),
                  (inst, bi, nb, f, p0, dout, err))
-LSM_BATCH_RUNNER(RunVolScan, k_vol_scan,
-                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi,
-                  unsigned long long* acc, unsigned* list, unsigned* count, cudaStream_t s),
-                 (inst, bi, nb, f, phi, acc, list, count))
-LSM_BATCH_RUNNER(RunIfaceScan, k_iface_scan,
-                 (int grid, const Inst* inst, const Brick* bi, int nb, FieldsT<T> f, const T* phi, unsigned* list,
-                  unsigned* count, cudaStream_t s),
-                 (inst, bi, nb, f, phi, list, count))
 
 template <typename T, int TX, int TY, int TZ>
 struct Occupancy {
     static void run(int kernel, int* out) {
         const int nt = TX * TY * TZ;
-        switch (kernel) {
-        case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_contra<T, TX, TY, TZ>, nt, 0); break;
-        default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_vol_scan<T, TX, TY, TZ>, nt, 0); break;
-        }
+        (void)kernel;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_contra<T, TX, TY, TZ>, nt, 0);
     }
 };
 
@@ -2227,10 +2261,13 @@ void bc_reinit(const Inst* inst, int ninst, long long nface, FieldsT<T> f, BC bc
 }
 inline unsigned list_blocks() { return 152 * 8; }
 template <typename T>
-void volume(int shape, int grid, const Inst* inst, const Brick* bi, int nb, const Flat& fl, FieldsT<T> f,
-            const T* phi, unsigned long long* acc, bool slope, unsigned* list, unsigned* count, cudaStream_t s) {
+void volume(int grid2, const Inst* inst, const Brick* bmap2, int nb2, const Flat& fl, FieldsT<T> f, const T* phi,
+            unsigned long long* acc, bool slope, unsigned* list, unsigned* count, cudaStream_t s) {
     cudaMemsetAsync(count, 0, sizeof(unsigned), s);
-    dispatch<RunVolScan, T>(shape, grid, inst, bi, nb, f, phi, acc, list, count, s);
+    {
+        ProfScope ps_("k_vol_scan_z", s);
+        k_vol_scan_z<T, true><<<grid2, 256, 0, s>>>(inst, bmap2, nb2, f, phi, acc, list, count);
+    }
     if (slope) {
         ProfScope ps_("k_vol_iface_slope", s);
         k_vol_iface<T, true><<<list_blocks(), 128, 0, s>>>(fl, f, phi, list, count, acc);
@@ -2250,11 +2287,14 @@ void mass_shift(const Flat& fl, const Mass* mass, const T* src, T* dst, cudaStre
     k_mass_shift<T><<<(unsigned)std::min<long long>((fl.n + 255) / 256, 152 * 16), 256, 0, s>>>(fl, mass, src, dst);
 }
 template <typename T>
-void mass_adjoint(int shape, int grid, const Inst* inst, const Brick* bi, int nb, const Brick* bmap2, int nb2,
-                  const Flat& fl, FieldsT<T> f, const T* phi_pre, const Mass* mass, T* lam, unsigned long long* wfix,
-                  double* part, double* ssum, unsigned* list, unsigned* count, cudaStream_t s) {
+void mass_adjoint(int grid2, const Inst* inst, const Brick* bmap2, int nb2, const Flat& fl, FieldsT<T> f,
+                  const T* phi_pre, const Mass* mass, T* lam, unsigned long long* wfix, double* part, double* ssum,
+                  unsigned* list, unsigned* count, cudaStream_t s) {
     cudaMemsetAsync(count, 0, sizeof(unsigned), s);
-    dispatch<RunIfaceScan, T>(shape, grid, inst, bi, nb, f, phi_pre, list, count, s);
+    {
+        ProfScope ps_("k_iface_scan_z", s);
+        k_vol_scan_z<T, false><<<grid2, 256, 0, s>>>(inst, bmap2, nb2, f, phi_pre, nullptr, list, count);
+    }
     {
         ProfScope ps_("k_mass_weights", s);
         k_mass_weights<T><<<list_blocks(), 128, 0, s>>>(fl, f, phi_pre, list, count, mass, wfix);
@@ -2286,6 +2326,12 @@ void cell_hex(long long off, int ni, int nj, int nk, const double* x, const doub
 int max_blocks_per_sm(int shape, int kernel) {
     int n = 0;
     dispatch<Occupancy, float>(shape, kernel, &n);
+    return n;
+}
+template <typename T>
+int vol_scan_blocks_per_sm() {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_vol_scan_z<T, true>, 256, 0);
     return n;
 }
 
@@ -2354,12 +2400,13 @@ void adj_contra(const Flat& fl, FieldsT<T> f, const T* w0, const T* w1, const T*
     template void adj_reinit_c<T>(int, const Inst*, const Brick*, int, const T*, long long, const T*, T*,           \
                                   cudaStream_t);                                                                \
     template int adj_reinit_c_blocks_per_sm<T>();                                                               \
-    template void volume<T>(int, int, const Inst*, const Brick*, int, const Flat&, FieldsT<T>, const T*,           \
+    template void volume<T>(int, const Inst*, const Brick*, int, const Flat&, FieldsT<T>, const T*,                \
                             unsigned long long*, bool, unsigned*, unsigned*, cudaStream_t);                          \
+    template int vol_scan_blocks_per_sm<T>();                                                                   \
     template void mass_shift<T>(const Flat&, const Mass*, const T*, T*, cudaStream_t);                                 \
-    template void mass_adjoint<T>(int, int, const Inst*, const Brick*, int, const Brick*, int, const Flat&, FieldsT<T>, \
-                                  const T*, const Mass*, T*, unsigned long long*, double*, double*, unsigned*,         \
-                                  unsigned*, cudaStream_t);                                                          \
+    template void mass_adjoint<T>(int, const Inst*, const Brick*, int, const Flat&, FieldsT<T>, const T*,          \
+                                  const Mass*, T*, unsigned long long*, double*, double*, unsigned*, unsigned*,        \
+                                  cudaStream_t);                                                                     \
     template void adj_face<T>(const Flat&, int, long long, BC, int, const T*, const T*, const T*, double, double, T*, \
                               cudaStream_t);                                                                          \
     template void adj_stage<T>(const int*, const Inst*, const Brick* const*, const int*, FieldsT<T>, const T*,      \

@@ -153,15 +153,17 @@ template <typename T>
 int reinit_z_blocks_per_sm();
 // water volume of every instance: the cells' 64-bit fixed-point sums (K, S,
 // bulk and, with `slope`, dK/dC) are added to acc[4 * inst + c] (zero on
-// entry) by a streaming pass that also lists the interface cells (list: at
-// least one entry per cell of the batch; count: one word, reset here) and a
-// pass over that list; volume_final writes vols[4 * inst + 0..3] = (K, S,
+// entry) by a streaming pass over the tiles of map 2 (grid2 CTAs) that also
+// lists the interface cells (list: at least one entry per cell of the batch;
+// count: one word, reset here) and a pass over that list; volume_final writes vols[4 * inst + 0..3] = (K, S,
 // bulk, total) and clears acc; with `mass` (target volumes `target`, NaN =
 // none) it also forms each instance's mass correction into mass[inst] and,
 // when mrec is not null, mrec[inst]
 template <typename T>
-void volume(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, const Flat& fl, FieldsT<T> f,
-            const T* phi, unsigned long long* acc, bool slope, unsigned* list, unsigned* count, cudaStream_t s);
+void volume(int grid2, const Inst* inst, const Brick* bmap2, int nb2, const Flat& fl, FieldsT<T> f, const T* phi,
+            unsigned long long* acc, bool slope, unsigned* list, unsigned* count, cudaStream_t s);
+template <typename T>
+int vol_scan_blocks_per_sm();
 void volume_final(int ninst, unsigned long long* acc, double* vols, const double* target, Mass* mass, Mass* mrec,
                   cudaStream_t s);
 // FP64 W = dt (grad xi_m . u) of one instance (n nodes from `off`) from the
@@ -174,8 +176,8 @@ void w64(long long off, long long n, double dt, const double* const* m64, const 
 // instance's first node
 void cell_hex(long long off, int ni, int nj, int nk, const double* x, const double* y, const double* z,
               long long* cellfix, cudaStream_t s);
-// resident CTAs per SM of a brick kernel of tile shape `shape` (FP32):
-// kernel 0 k_contra, other k_vol_scan
+// resident CTAs per SM of the brick kernel k_contra of tile shape `shape`
+// (FP32; `kernel` is 0)
 int max_blocks_per_sm(int shape, int kernel);
 
 // ------------------------------------------------------------ adjoint
@@ -236,10 +238,9 @@ void mass_shift(const Flat& fl, const Mass* mass, const T* src, T* dst, cudaStre
 // entry and on exit), part (one double per tile of adjoint map 2), ssum
 // (one per instance) and the interface-cell list (list, count) are scratch
 template <typename T>
-void mass_adjoint(int shape, int grid, const Inst* inst, const Brick* bricks, int nbricks, const Brick* bmap2,
-                  int nb2, const Flat& fl, FieldsT<T> f, const T* phi_pre, const Mass* mass, T* lam,
-                  unsigned long long* wfix, double* part, double* ssum, unsigned* list, unsigned* count,
-                  cudaStream_t s);
+void mass_adjoint(int grid2, const Inst* inst, const Brick* bmap2, int nb2, const Flat& fl, FieldsT<T> f,
+                  const T* phi_pre, const Mass* mass, T* lam, unsigned long long* wfix, double* part, double* ssum,
+                  unsigned* list, unsigned* count, cudaStream_t s);
 // lam_u_c += sum_m M[m][c] dt lamW_m  (the W = dt M u chain rule)
 template <typename T>
 void adj_contra(const Flat& fl, FieldsT<T> f, const T* lamW0, const T* lamW1, const T* lamW2, T* lu0, T* lu1,

@@ -65,6 +65,7 @@ struct lsm_batch {
     lsm::batch::Brick* d_amap[4] = {};  // brick tables of the adjoint stencil kernels (lsm::batch::adj_shape)
     int namap[4] = {0, 0, 0, 0}, agrid[4] = {1, 1, 1, 1};
     int sgrid = 1, acgrid = 1, rzgrid = 1;   // CTAs of the map-2 kernels: stage, k_adj_reinit_c, reinit_z
+    int vgrid = 1;                           // CTAs of the map-2 volume scan
     bool reinit_march = true;   // plain pseudo-steps march in k (reinit_z) rather than walk the brick table
     unsigned long long* d_vacc = nullptr;   // volume accumulators, 4 per instance
     unsigned* d_ilist = nullptr;            // interface cells of a volume pass (N entries) and their count
@@ -322,6 +323,9 @@ int build_bricks(lsm_batch* b, int shape) {
     const int prz = std::max(1, b->prec ? lsm::batch::reinit_z_blocks_per_sm<double>()
                                         : lsm::batch::reinit_z_blocks_per_sm<float>());
     b->rzgrid = std::max(1, std::min(b->namap[2], sms * prz));
+    const int pv = std::max(1, b->prec ? lsm::batch::vol_scan_blocks_per_sm<double>()
+                                       : lsm::batch::vol_scan_blocks_per_sm<float>());
+    b->vgrid = std::max(1, std::min(b->namap[2], sms * pv));
     if (b->tma_eligible)
         b->tgrid = std::max(1, std::min(b->namap[2], sms * std::max(1, lsm::batch::stage_tma_blocks_per_sm())));
     b->shape = shape;
@@ -424,8 +428,8 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
     if (rec && !coef) f.sgn = rec->sgn;
     const Flat fl{b->d_inst, b->d_offs, b->ninst, b->N};
     if (vol && !mc) {
-        B::volume<T>(sh, gr, b->d_inst, b->d_brick, nb, fl, f, phin, b->d_vacc, false, b->d_ilist, b->d_icount,
-                     b->stream);
+        B::volume<T>(b->vgrid, b->d_inst, b->d_amap[2], b->namap[2], fl, f, phin, b->d_vacc, false, b->d_ilist,
+                     b->d_icount, b->stream);
         B::volume_final(b->ninst, b->d_vacc, b->d_vols, nullptr, nullptr, nullptr, b->stream);
     }
     // the field the final bcond_lsm writes
@@ -477,8 +481,8 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
     if (mc) {
         // FP64 water volume of the result, the correction C = (target - V) / A
         // and phi_out = result + C
-        B::volume<T>(sh, gr, b->d_inst, b->d_brick, nb, fl, f, res, b->d_vacc, true, b->d_ilist, b->d_icount,
-                     b->stream);
+        B::volume<T>(b->vgrid, b->d_inst, b->d_amap[2], b->namap[2], fl, f, res, b->d_vacc, true, b->d_ilist,
+                     b->d_icount, b->stream);
         B::volume_final(b->ninst, b->d_vacc, b->d_vols, b->d_target, b->d_mass, mrec, b->stream);
         if (phi_out) B::mass_shift<T>(fl, b->d_mass, res, phi_out, b->stream);
     }
@@ -491,8 +495,8 @@ void enqueue_step(lsm_batch* b) {
 
 // Chooses the tile shape of the brick-table kernels and whether the plain
 // pseudo-steps march in k (reinit_z) or walk the brick table: times, on
-// the batch itself, contra + volume and the brick pseudo-step for every
-// shape, and the marching pseudo-step once.
+// the batch itself, the brick pseudo-steps for every shape and the marching
+// pseudo-steps once (the per-step kernels that depend on the choice).
 int autotune(lsm_batch* b) {
     namespace B = lsm::batch;
     cudaEvent_t ev[3];
@@ -516,19 +520,12 @@ int autotune(lsm_batch* b) {
         cudaEventElapsedTime(ms_b, ev[1], ev[2]);
         return LSM_OK;
     };
-    float a[B::kNumShapes], br[B::kNumShapes], zm = 0.f, dummy = 0.f;
+    float br[B::kNumShapes], zm = 0.f, dummy = 0.f;
     for (int s = 0; s < B::kNumShapes; ++s) {
         const int bs = build_bricks(b, s);
         if (bs != LSM_OK) return done(bs);
         const int st = timed(
-            &a[s], &br[s],
-            [&]() {
-                B::contra<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, b->stream);
-                B::volume<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks,
-                                 Flat{b->d_inst, b->d_offs, b->ninst, b->N}, f, f.phi, b->d_vacc, false, b->d_ilist,
-                                 b->d_icount, b->stream);
-                B::volume_final(b->ninst, b->d_vacc, b->d_vols, nullptr, nullptr, nullptr, b->stream);
-            },
+            &dummy, &br[s], [&]() {},
             [&]() {
                 B::sign_reinit<float>(s, b->grid, b->d_inst, b->d_brick, b->nbricks, f, f.phi, f.d[0], nullptr,
                                       b->stream);
@@ -544,14 +541,11 @@ int autotune(lsm_batch* b) {
                            nullptr, b->stream);
     });
     if (st != LSM_OK) return done(st);
-    int best_b = 0, best_a = 0;
-    for (int s = 1; s < B::kNumShapes; ++s) {
-        if (a[s] + br[s] < a[best_b] + br[best_b]) best_b = s;
-        if (a[s] < a[best_a]) best_a = s;
-    }
-    const bool march = a[best_a] + zm < a[best_b] + br[best_b];
-    b->reinit_march = march;
-    const int bs = build_bricks(b, march ? best_a : best_b);
+    int best_b = 0;
+    for (int s = 1; s < B::kNumShapes; ++s)
+        if (br[s] < br[best_b]) best_b = s;
+    b->reinit_march = zm < br[best_b];
+    const int bs = build_bricks(b, best_b);
     if (bs != LSM_OK) return done(bs);
     // the RK stage: plane tiles staged by TMA copies or by the threads
     if (b->tma_eligible) {
@@ -787,8 +781,8 @@ void adj_step(lsm_batch* b, AdjView<T>& v, const Rec<T>& r, const T* phin, const
     const int R = b->cfg.RNitermax;
     // reverse of the mass correction phi^{n+1} = P + C(P), in place on lam
     if (b->cfg.mass_correction)
-        B::mass_adjoint<T>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, b->d_amap[2], b->namap[2], fl, f,
-                           r.P, m, v.lam, b->wfix, b->d_tpart, b->d_ssum, b->d_ilist, b->d_icount, b->stream);
+        B::mass_adjoint<T>(b->vgrid, b->d_inst, b->d_amap[2], b->namap[2], fl, f, r.P, m, v.lam, b->wfix, b->d_tpart,
+                           b->d_ssum, b->d_ilist, b->d_icount, b->stream);
     auto faces = [&](int kind, const T* pn, const T* in, const T* out, double c1, double c2) {
         for (int face = 5; face >= 0; --face)
             B::adj_face<T>(fl, face, b->nplane[face >> 1], bc, kind, pn, in, out, c1, c2, v.lam, b->stream);
@@ -1177,11 +1171,11 @@ int lsm_batch_water_volume(lsm_batch_handle b, double* volumes) {
     namespace B = lsm::batch;
     const Flat fl{b->d_inst, b->d_offs, b->ninst, b->N};
     if (b->prec)
-        B::volume<double>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, fl, b->f64, b->f64.phi, b->d_vacc,
-                          false, b->d_ilist, b->d_icount, b->stream);
+        B::volume<double>(b->vgrid, b->d_inst, b->d_amap[2], b->namap[2], fl, b->f64, b->f64.phi, b->d_vacc, false,
+                          b->d_ilist, b->d_icount, b->stream);
     else
-        B::volume<float>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, fl, b->f32, b->f32.phi, b->d_vacc,
-                         false, b->d_ilist, b->d_icount, b->stream);
+        B::volume<float>(b->vgrid, b->d_inst, b->d_amap[2], b->namap[2], fl, b->f32, b->f32.phi, b->d_vacc, false,
+                         b->d_ilist, b->d_icount, b->stream);
     B::volume_final(b->ninst, b->d_vacc, b->d_vols, nullptr, nullptr, nullptr, b->stream);
     BCU(b, cudaGetLastError());
     BCU(b, cudaMemcpyAsync(b->h_vols, b->d_vols, sizeof(double) * 4 * b->ninst, cudaMemcpyDeviceToHost, b->stream));
