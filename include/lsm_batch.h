@@ -91,7 +91,13 @@ int lsm_batch_destroy(lsm_batch_handle h);
 
 /* Per-instance inputs in the reference's layout (FP64, host or device):
    coordinates x, y, z and metrics csi, eta, zet (1:3, ...); velocity q (1:4, ...)
-   of which q(2:4) is read; phi. */
+   of which q(2:4) is read; phi.
+   Every array argument of the batch (inputs and outputs) may be pageable
+   host memory (copied through a device staging buffer), page-locked host
+   memory registered on the batch's device (cudaHostAlloc / cudaHostRegister:
+   read and written in place by the conversion kernels, the fastest host
+   path), or device memory (used in place on the batch's device, copied from
+   another device).  Each call returns once the transfer is complete. */
 int lsm_batch_set_geometry(lsm_batch_handle h, int inst, const double* x, const double* y,
                            const double* z, const double* csi, const double* eta, const double* zet);
 int lsm_batch_set_velocity(lsm_batch_handle h, int inst, const double* q);

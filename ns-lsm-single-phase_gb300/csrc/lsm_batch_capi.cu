@@ -131,15 +131,44 @@ struct Dev {
     }
 };
 
+// Caller arrays are records of `stride` doubles per node in the reference's
+// layout (a scalar field: stride 1; q(1:4, .): 4; csi(1:3, .): 3).  Each
+// conversion is one pass over the records, all components at once.
+// Components c0 .. c0 + nc - 1 of every record -> d[0 .. nc - 1] (type T),
+// and to the FP64 arrays e[c] too where those are not null.
+struct CvtDst {
+    void* d[3];
+    double* e[3];
+};
 template <typename T>
-__global__ void k_cvt_in(const double* __restrict__ src, int stride, int comp, long long n, T* __restrict__ dst) {
-    for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < n; l += (long long)gridDim.x * blockDim.x)
-        dst[l] = (T)src[l * stride + comp];
+__global__ void k_cvt_in(const double* __restrict__ src, int stride, int c0, int nc, long long n, CvtDst o) {
+    for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < n;
+         l += (long long)gridDim.x * blockDim.x) {
+        const double* r = src + l * stride + c0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            if (c >= nc) break;
+            const double v = r[c];
+            static_cast<T*>(o.d[c])[l] = (T)v;
+            if (o.e[c]) o.e[c][l] = v;
+        }
+    }
 }
+// src[0 .. nc - 1] (type T) -> components c0 .. c0 + nc - 1 of every record,
+// the record's other components zero
+struct CvtSrc {
+    const void* s[3];
+};
 template <typename T>
-__global__ void k_cvt_out(const T* __restrict__ src, int stride, int comp, long long n, double* __restrict__ dst) {
-    for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < n; l += (long long)gridDim.x * blockDim.x)
-        dst[l * stride + comp] = (double)src[l];
+__global__ void k_cvt_out(CvtSrc in, int stride, int c0, int nc, long long n, double* __restrict__ dst) {
+    for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < n;
+         l += (long long)gridDim.x * blockDim.x) {
+        double* r = dst + l * stride;
+        for (int c = 0; c < stride; ++c) {
+            const int k = c - c0;
+            r[c] = k >= 0 && k < nc ? (double)static_cast<const T*>(in.s[k])[l] : 0.0;
+        }
+    }
 }
 // FP64 W of instance q once its FP64 geometry and velocity are both in place
 void update_w64(lsm_batch* b, int q) {
@@ -200,34 +229,52 @@ bool encode_stage_map(const lsm_batch* b, void* base, long long narrays, CUtenso
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-bool on_device(const void* p) {
+// The address at which this batch's kernels can use a caller's array in
+// place: memory of the batch's device, or page-locked host memory registered
+// on that device (its mapped alias; the conversion kernels then read and
+// write it across the host link).  nullptr for anything else (pageable host
+// memory, another device's memory), which goes through the staging buffer
+// by a copy.  After long kernels over most of HBM the first transfer of a
+// host array pays for its page translations again; many SMs take those
+// misses in parallel, a copy engine does not (measured on GB300: 5-10 ms
+// against 17-31 ms for 268 MB; 1.3 ms either way once warm).
+double* kernel_view(const lsm_batch* b, const void* p) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
-        return false;
+        return nullptr;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.device != b->device) return nullptr;
+    if (a.type == cudaMemoryTypeDevice) return static_cast<double*>(const_cast<void*>(p));
+    if (a.type == cudaMemoryTypeHost && a.devicePointer) return static_cast<double*>(a.devicePointer);
+    return nullptr;
 }
 
-// copy `n` doubles (host or device) into the staging buffer
-int stage_in(lsm_batch* b, const double* src, long long n) {
-    BCU(b, cudaMemcpyAsync(b->staging, src, sizeof(double) * n,
-                           on_device(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, b->stream));
+// n records of the caller's `src` -> components c0 .. c0 + nc - 1 into
+// o.d (the batch's type, or FP64 with `f64`) and o.e
+int load_in(lsm_batch* b, const double* src, long long n, int stride, int c0, int nc, CvtDst o, bool f64 = false) {
+    const double* v = kernel_view(b, src);
+    if (!v) {
+        BCU(b, cudaMemcpyAsync(b->staging, src, sizeof(double) * n * stride, cudaMemcpyDefault, b->stream));
+        v = b->staging;
+    }
+    lsm::ProfScope ps("k_cvt_in", b->stream);
+    if (f64 || b->prec) k_cvt_in<double><<<cblocks(n), 256, 0, b->stream>>>(v, stride, c0, nc, n, o);
+    else k_cvt_in<float><<<cblocks(n), 256, 0, b->stream>>>(v, stride, c0, nc, n, o);
+    BCU(b, cudaGetLastError());
     return LSM_OK;
 }
-void cvt_in(lsm_batch* b, int stride, int comp, long long n, void* dst) {
-    lsm::ProfScope ps("k_cvt_in", b->stream);
-    if (b->prec) k_cvt_in<double><<<cblocks(n), 256, 0, b->stream>>>(b->staging, stride, comp, n, (double*)dst);
-    else k_cvt_in<float><<<cblocks(n), 256, 0, b->stream>>>(b->staging, stride, comp, n, (float*)dst);
-}
-void cvt_out(lsm_batch* b, const void* src, int stride, int comp, long long n) {
-    lsm::ProfScope ps("k_cvt_out", b->stream);
-    if (b->prec) k_cvt_out<double><<<cblocks(n), 256, 0, b->stream>>>((const double*)src, stride, comp, n, b->staging);
-    else k_cvt_out<float><<<cblocks(n), 256, 0, b->stream>>>((const float*)src, stride, comp, n, b->staging);
-}
-int copy_out(lsm_batch* b, double* dst, long long n) {
-    BCU(b, cudaMemcpyAsync(dst, b->staging, sizeof(double) * n,
-                           on_device(dst) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, b->stream));
+// the batch's arrays `in` -> n records of the caller's `dst` (components c0
+// .. c0 + nc - 1; the others zero); returns once dst holds them
+int store_out(lsm_batch* b, double* dst, long long n, int stride, int c0, int nc, CvtSrc in) {
+    double* v = kernel_view(b, dst);
+    {
+        lsm::ProfScope ps("k_cvt_out", b->stream);
+        if (b->prec) k_cvt_out<double><<<cblocks(n), 256, 0, b->stream>>>(in, stride, c0, nc, n, v ? v : b->staging);
+        else k_cvt_out<float><<<cblocks(n), 256, 0, b->stream>>>(in, stride, c0, nc, n, v ? v : b->staging);
+    }
+    BCU(b, cudaGetLastError());
+    if (!v) BCU(b, cudaMemcpyAsync(dst, b->staging, sizeof(double) * n * stride, cudaMemcpyDefault, b->stream));
     BCU(b, cudaStreamSynchronize(b->stream));
     return LSM_OK;
 }
@@ -1011,17 +1058,15 @@ int lsm_batch_set_geometry(lsm_batch_handle b, int q, const double* x, const dou
     const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
     const double* c3[3] = {x, y, z};
     for (int c = 0; c < 3; ++c)
-        BCU(b, cudaMemcpyAsync(b->xyz + c * b->ld8 + o, c3[c], sizeof(double) * n,
-                               on_device(c3[c]) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, b->stream));
+        BTRY(load_in(b, c3[c], n, 1, 0, 1, CvtDst{{b->xyz + c * b->ld8 + o}, {}}, true));
     const double* m3[3] = {csi, eta, zet};
     for (int d = 0; d < 3; ++d) {
-        BTRY(stage_in(b, m3[d], 3 * n));
+        CvtDst to{};
         for (int c = 0; c < 3; ++c) {
-            cvt_in(b, 3, c, n, (char*)b->comps[3 + 3 * d + c] + b->esz * o);
-            if (b->f64x)
-                k_cvt_in<double><<<cblocks(n), 256, 0, b->stream>>>(b->staging, 3, c, n,
-                                                                    b->f64x + (size_t)(3 * d + c) * b->ld8 + o);
+            to.d[c] = (char*)b->comps[3 + 3 * d + c] + b->esz * o;
+            to.e[c] = b->f64x ? b->f64x + (size_t)(3 * d + c) * b->ld8 + o : nullptr;
         }
+        BTRY(load_in(b, m3[d], n, 3, 0, 3, to));
     }
     b->geom_set[q] = 1;
     b->w_stale = true;
@@ -1039,13 +1084,12 @@ int lsm_batch_set_velocity(lsm_batch_handle b, int q, const double* qv) {
     Dev guard(b->device);
     const auto& I = b->inst[q];
     const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
-    BTRY(stage_in(b, qv, 4 * n));
+    CvtDst to{};
     for (int c = 0; c < 3; ++c) {
-        cvt_in(b, 4, c + 1, n, (char*)b->comps[12 + c] + b->esz * o);
-        if (b->f64x)
-            k_cvt_in<double><<<cblocks(n), 256, 0, b->stream>>>(b->staging, 4, c + 1, n,
-                                                                b->f64x + (size_t)(9 + c) * b->ld8 + o);
+        to.d[c] = (char*)b->comps[12 + c] + b->esz * o;
+        to.e[c] = b->f64x ? b->f64x + (size_t)(9 + c) * b->ld8 + o : nullptr;
     }
+    BTRY(load_in(b, qv, n, 4, 1, 3, to));
     b->vel_set[q] = 1;
     b->w_stale = true;
     update_w64(b, q);
@@ -1060,9 +1104,7 @@ int lsm_batch_set_phi(lsm_batch_handle b, int q, const double* phi) {
     Dev guard(b->device);
     const auto& I = b->inst[q];
     const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
-    BTRY(stage_in(b, phi, n));
-    cvt_in(b, 1, 0, n, (char*)b->bufs[0] + b->esz * o);
-    BCU(b, cudaGetLastError());
+    BTRY(load_in(b, phi, n, 1, 0, 1, CvtDst{{(char*)b->bufs[0] + b->esz * o}, {}}));
     BCU(b, cudaStreamSynchronize(b->stream));
     return LSM_OK;
 }
@@ -1073,9 +1115,7 @@ int lsm_batch_get_phi(lsm_batch_handle b, int q, double* phi) {
     Dev guard(b->device);
     const auto& I = b->inst[q];
     const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
-    cvt_out(b, (const char*)b->bufs[0] + b->esz * o, 1, 0, n);
-    BCU(b, cudaGetLastError());
-    return copy_out(b, phi, n);
+    return store_out(b, phi, n, 1, 0, 1, CvtSrc{{(const char*)b->bufs[0] + b->esz * o}});
 }
 
 int lsm_batch_step(lsm_batch_handle b, int nsteps, double* volumes) {
@@ -1114,9 +1154,7 @@ int lsm_batch_set_grad_phi(lsm_batch_handle b, int q, const double* g) {
     Dev guard(b->device);
     const auto& I = b->inst[q];
     const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
-    BTRY(stage_in(b, g, n));
-    cvt_in(b, 1, 0, n, (char*)adj_field(b, 0) + b->esz * o);
-    BCU(b, cudaGetLastError());
+    BTRY(load_in(b, g, n, 1, 0, 1, CvtDst{{(char*)adj_field(b, 0) + b->esz * o}, {}}));
     BCU(b, cudaStreamSynchronize(b->stream));
     return LSM_OK;
 }
@@ -1135,9 +1173,7 @@ int lsm_batch_get_grad_phi0(lsm_batch_handle b, int q, double* g) {
     Dev guard(b->device);
     const auto& I = b->inst[q];
     const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
-    cvt_out(b, (const char*)adj_field(b, 0) + b->esz * o, 1, 0, n);
-    BCU(b, cudaGetLastError());
-    return copy_out(b, g, n);
+    return store_out(b, g, n, 1, 0, 1, CvtSrc{{(const char*)adj_field(b, 0) + b->esz * o}});
 }
 
 int lsm_batch_get_grad_velocity(lsm_batch_handle b, int q, double* gq) {
@@ -1147,10 +1183,9 @@ int lsm_batch_get_grad_velocity(lsm_batch_handle b, int q, double* gq) {
     Dev guard(b->device);
     const auto& I = b->inst[q];
     const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
-    BCU(b, cudaMemsetAsync(b->staging, 0, sizeof(double) * 4 * n, b->stream));
-    for (int c = 0; c < 3; ++c) cvt_out(b, (const char*)adj_field(b, 1 + c) + b->esz * o, 4, c + 1, n);
-    BCU(b, cudaGetLastError());
-    return copy_out(b, gq, 4 * n);
+    CvtSrc from{};
+    for (int c = 0; c < 3; ++c) from.s[c] = (const char*)adj_field(b, 1 + c) + b->esz * o;
+    return store_out(b, gq, n, 4, 1, 3, from);
 }
 
 int lsm_batch_set_mass_target(lsm_batch_handle b, int q, double volume) {
