@@ -464,14 +464,13 @@ def run_batched(args):
         o = torch.empty(m["inst"].grid.n, dtype=torch.float64, pin_memory=True)
         pinned.append((v, t, o.numpy().reshape(m["inst"].grid.shape, order="F"), o))
     e2e_steps = max(2, min(args.steps, 5))
+    qv, po = [p[0] for p in pinned], [p[2] for p in pinned]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for s in range(e2e_steps):
-        for k, (v, _t, _o, _ot) in enumerate(pinned):
-            b.set_velocity(k, v)
+        b.set_velocities(qv)          # every instance's q in one call (lsm_batch_set_velocities)
         b.step(1, volumes=True)
-        for k, (_v, _t, o, _ot) in enumerate(pinned):
-            b._chk(b.lib.lsm_batch_get_phi(b.h, k, o.ctypes.data), "get_phi")
+        b.get_phis(po)                # every instance's phi out in one call (lsm_batch_get_phis)
     torch.cuda.synchronize()
     e2e_s = dist_max(time.perf_counter() - t0, world)
     e2e_value = world * n * e2e_steps / e2e_s / 1e9

@@ -104,6 +104,13 @@ int lsm_batch_set_velocity(lsm_batch_handle h, int inst, const double* q);
 int lsm_batch_set_phi(lsm_batch_handle h, int inst, const double* phi);
 /* Read phi of one instance back as FP64 (host or device array). */
 int lsm_batch_get_phi(lsm_batch_handle h, int inst, double* phi);
+/* The same for every instance in one call: q[k] / phi[k] is instance k's
+   array (ninst pointers, none null).  The transfers of all instances are
+   queued and waited for once, where a loop over the single-instance calls
+   waits for each (a coupled solver that exchanges every instance's
+   velocity and phi each step).  No reference counterpart. */
+int lsm_batch_set_velocities(lsm_batch_handle h, const double* const* q);
+int lsm_batch_get_phis(lsm_batch_handle h, double* const* phi);
 
 /* Advance every instance by `nsteps` physical steps.  `volumes` (nullable,
    host, 4*ninst doubles) receives each instance's pre-advection volumes of

@@ -265,8 +265,8 @@ int load_in(lsm_batch* b, const double* src, long long n, int stride, int c0, in
     return LSM_OK;
 }
 // the batch's arrays `in` -> n records of the caller's `dst` (components c0
-// .. c0 + nc - 1; the others zero); returns once dst holds them
-int store_out(lsm_batch* b, double* dst, long long n, int stride, int c0, int nc, CvtSrc in) {
+// .. c0 + nc - 1; the others zero); with `wait`, returns once dst holds them
+int store_out(lsm_batch* b, double* dst, long long n, int stride, int c0, int nc, CvtSrc in, bool wait = true) {
     double* v = kernel_view(b, dst);
     {
         lsm::ProfScope ps("k_cvt_out", b->stream);
@@ -275,7 +275,7 @@ int store_out(lsm_batch* b, double* dst, long long n, int stride, int c0, int nc
     }
     BCU(b, cudaGetLastError());
     if (!v) BCU(b, cudaMemcpyAsync(dst, b->staging, sizeof(double) * n * stride, cudaMemcpyDefault, b->stream));
-    BCU(b, cudaStreamSynchronize(b->stream));
+    if (wait) BCU(b, cudaStreamSynchronize(b->stream));
     return LSM_OK;
 }
 
@@ -1078,10 +1078,11 @@ int lsm_batch_set_geometry(lsm_batch_handle b, int q, const double* x, const dou
     return LSM_OK;
 }
 
-int lsm_batch_set_velocity(lsm_batch_handle b, int q, const double* qv) {
-    if (!b || !qv) return LSM_ERR_NULL;
-    BTRY(check_inst(b, q));
-    Dev guard(b->device);
+}  // extern "C"
+
+namespace {
+// q(2:4, .) of instance q into the batch (and its FP64 copy); enqueued only
+int velocity_in(lsm_batch* b, int q, const double* qv) {
     const auto& I = b->inst[q];
     const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
     CvtDst to{};
@@ -1094,6 +1095,33 @@ int lsm_batch_set_velocity(lsm_batch_handle b, int q, const double* qv) {
     b->w_stale = true;
     update_w64(b, q);
     BCU(b, cudaGetLastError());
+    return LSM_OK;
+}
+// phi of instance q out to the caller's array; enqueued only
+int phi_out(lsm_batch* b, int q, double* phi) {
+    const auto& I = b->inst[q];
+    const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
+    return store_out(b, phi, n, 1, 0, 1, CvtSrc{{(const char*)b->bufs[0] + b->esz * o}}, false);
+}
+}  // namespace
+
+extern "C" {
+
+int lsm_batch_set_velocity(lsm_batch_handle b, int q, const double* qv) {
+    if (!b || !qv) return LSM_ERR_NULL;
+    BTRY(check_inst(b, q));
+    Dev guard(b->device);
+    BTRY(velocity_in(b, q, qv));
+    BCU(b, cudaStreamSynchronize(b->stream));
+    return LSM_OK;
+}
+
+int lsm_batch_set_velocities(lsm_batch_handle b, const double* const* qv) {
+    if (!b || !qv) return LSM_ERR_NULL;
+    for (int q = 0; q < b->ninst; ++q)
+        if (!qv[q]) return LSM_ERR_NULL;
+    Dev guard(b->device);
+    for (int q = 0; q < b->ninst; ++q) BTRY(velocity_in(b, q, qv[q]));
     BCU(b, cudaStreamSynchronize(b->stream));
     return LSM_OK;
 }
@@ -1113,9 +1141,19 @@ int lsm_batch_get_phi(lsm_batch_handle b, int q, double* phi) {
     if (!b || !phi) return LSM_ERR_NULL;
     BTRY(check_inst(b, q));
     Dev guard(b->device);
-    const auto& I = b->inst[q];
-    const long long n = (long long)I.ni * I.nj * I.nk, o = b->off[q];
-    return store_out(b, phi, n, 1, 0, 1, CvtSrc{{(const char*)b->bufs[0] + b->esz * o}});
+    BTRY(phi_out(b, q, phi));
+    BCU(b, cudaStreamSynchronize(b->stream));
+    return LSM_OK;
+}
+
+int lsm_batch_get_phis(lsm_batch_handle b, double* const* phi) {
+    if (!b || !phi) return LSM_ERR_NULL;
+    for (int q = 0; q < b->ninst; ++q)
+        if (!phi[q]) return LSM_ERR_NULL;
+    Dev guard(b->device);
+    for (int q = 0; q < b->ninst; ++q) BTRY(phi_out(b, q, phi[q]));
+    BCU(b, cudaStreamSynchronize(b->stream));
+    return LSM_OK;
 }
 
 int lsm_batch_step(lsm_batch_handle b, int nsteps, double* volumes) {

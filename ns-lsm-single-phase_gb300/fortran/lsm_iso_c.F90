@@ -278,6 +278,19 @@ module lsm_iso_c
          real(c_double), intent(out) :: phi(*)
       end function
 
+      ! q(k) / phi(k): c_loc of instance k's array, one per instance
+      integer(c_int) function lsm_batch_set_velocities(h, q) bind(C, name="lsm_batch_set_velocities")
+         import :: c_int, c_ptr
+         type(c_ptr), value :: h
+         type(c_ptr), intent(in) :: q(*)
+      end function
+
+      integer(c_int) function lsm_batch_get_phis(h, phi) bind(C, name="lsm_batch_get_phis")
+         import :: c_int, c_ptr
+         type(c_ptr), value :: h
+         type(c_ptr), intent(in) :: phi(*)
+      end function
+
       integer(c_int) function lsm_batch_step(h, nsteps, vols) bind(C, name="lsm_batch_step")
          import :: c_int, c_ptr, c_double
          type(c_ptr), value :: h

@@ -111,6 +111,8 @@ SIGNATURES = {
     "lsm_batch_set_velocity": (_i, [_vp, _i, _vp]),
     "lsm_batch_set_phi": (_i, [_vp, _i, _vp]),
     "lsm_batch_get_phi": (_i, [_vp, _i, _vp]),
+    "lsm_batch_set_velocities": (_i, [_vp, C.POINTER(_vp)]),
+    "lsm_batch_get_phis": (_i, [_vp, C.POINTER(_vp)]),
     "lsm_batch_step": (_i, [_vp, _i, _vp]),
     "lsm_batch_water_volume": (_i, [_vp, _vp]),
     "lsm_batch_set_mass_target": (_i, [_vp, _i, _d]),

@@ -109,6 +109,24 @@ class LevelSetBatch:
         _torch_sync(q)
         self._chk(self.lib.lsm_batch_set_velocity(self.h, k, _addr(q, g, 4, np.float64)), "lsm_batch_set_velocity")
 
+    def set_velocities(self, qs):
+        """Every instance's velocity in one call (qs[k]: instance k's q)."""
+        if len(qs) != self.ninst:
+            raise ValueError("one velocity array per instance")
+        _torch_sync(*qs)
+        ptrs = (C.c_void_p * self.ninst)(*[_addr(q, g, 4, np.float64) for q, g in zip(qs, self.grids)])
+        self._chk(self.lib.lsm_batch_set_velocities(self.h, ptrs), "lsm_batch_set_velocities")
+
+    def get_phis(self, outs):
+        """Every instance's phi into outs[k] (Fortran-ordered numpy arrays or
+        CUDA tensors of the reversed shape) in one call."""
+        if len(outs) != self.ninst:
+            raise ValueError("one output array per instance")
+        _torch_sync(*outs)
+        ptrs = (C.c_void_p * self.ninst)(*[_addr(o, g, 1, np.float64) for o, g in zip(outs, self.grids)])
+        self._chk(self.lib.lsm_batch_get_phis(self.h, ptrs), "lsm_batch_get_phis")
+        return outs
+
     def set_phi(self, k, phi):
         g = self.grids[k]
         _torch_sync(phi)

@@ -130,3 +130,52 @@ def test_tiny_ragged_instances(oracle):
             assert float(np.abs(got - ref)[band].max()) <= BAND_TOL
         assert float(np.abs(got - ref).max()) <= 1e-4
         assert abs(vols[k, 3] - rv[3]) / rv[3] <= VOL_TOL
+
+
+@pytest.mark.parametrize("kind", ["pageable", "pinned", "device"])
+def test_batch_wide_transfers_equal_per_instance_calls(small_batch, kind):
+    """lsm_batch_set_velocities / lsm_batch_get_phis (every instance in one
+    call, one wait) load and return the same bits as the per-instance calls,
+    for each kind of caller array."""
+    def arr(a):
+        a = np.asfortranarray(a)
+        if kind == "pageable":
+            return a, None
+        if kind == "pinned":
+            t = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
+            v = t.numpy().reshape(a.shape, order="F")
+            v[...] = a
+            return v, t
+        return torch.from_numpy(np.ascontiguousarray(a.T)).cuda(), None
+
+    def host(a):
+        return a.cpu().numpy().T.copy(order="F") if torch.is_tensor(a) else np.array(a, order="F")
+
+    keep = []
+    qs = []
+    for p in small_batch:
+        q = p["inst"].q.copy(order="F")
+        q[1:] *= 0.9                      # a velocity other than the one the batch was built with
+        v, t = arr(q)
+        qs.append(v)
+        keep.append(t)
+    outs = []
+    for p in small_batch:
+        v, t = arr(np.zeros(p["inst"].grid.shape, order="F"))
+        outs.append(v)
+        keep.append(t)
+    a = _make_batch(small_batch, 3)
+    for k, q in enumerate(qs):
+        a.set_velocity(k, q)
+    a.step(2)
+    ref = [a.get_phi(k) for k in range(len(small_batch))]
+    a.close()
+    b = _make_batch(small_batch, 3)
+    b.set_velocities(qs)
+    b.step(2)
+    b.get_phis(outs)
+    torch.cuda.synchronize()
+    b.close()
+    for r, o in zip(ref, outs):
+        assert np.array_equal(host(o), r)
+    del keep
