@@ -96,3 +96,32 @@ def test_batch_create_validates_before_touching_a_device(lib_built):
         setattr(cfg, field, 0 if field != "RNitermax" else 5)
     cfg.btype_lsm[3] = 7
     assert lib.lsm_batch_create(C.byref(h), 0, None, 2, inst, C.byref(cfg)) == _lib.LSM_ERR_BAD_PARAM
+
+
+def test_batch_entry_points_reject_null_handles(lib_built):
+    """Every batch entry point answers a null handle or array with its status
+    code instead of touching a device (no GPU needed)."""
+    from nslsm import _lib
+    lib = _lib.load()
+    h = C.c_void_p()
+    cfg = _lib.LsmBatchConfig()
+    cfg.RNitermax, cfg.BigPhi = 5, 5.0
+    for f in range(6):
+        cfg.btype_lsm[f] = 1
+    cfg.mass_correction = 2
+    inst = (_lib.LsmBatchInstance * 1)()
+    inst[0].ni, inst[0].nj, inst[0].nk = 8, 8, 8
+    inst[0].dt, inst[0].dtau, inst[0].eps = 1e-3, 1e-3, 1e-2
+    assert lib.lsm_batch_create(C.byref(h), 0, None, 1, inst, C.byref(cfg)) == _lib.LSM_ERR_BAD_PARAM
+    ptrs = (C.c_void_p * 1)()
+    assert lib.lsm_batch_set_velocities(None, ptrs) == _lib.LSM_ERR_NULL
+    assert lib.lsm_batch_get_phis(None, ptrs) == _lib.LSM_ERR_NULL
+    assert lib.lsm_batch_set_velocity(None, 0, None) == _lib.LSM_ERR_NULL
+    assert lib.lsm_batch_get_phi(None, 0, None) == _lib.LSM_ERR_NULL
+    assert lib.lsm_batch_water_volume(None, None) == _lib.LSM_ERR_NULL
+    assert lib.lsm_batch_set_mass_target(None, 0, 1.0) == _lib.LSM_ERR_NULL
+    assert lib.lsm_batch_mass_state(None, None) == _lib.LSM_ERR_NULL
+    assert lib.lsm_batch_step(None, 1, None) == _lib.LSM_ERR_NULL
+    assert lib.lsm_batch_backward(None) == _lib.LSM_ERR_NULL
+    assert lib.lsm_batch_stage_kernel(None) == -1
+    assert lib.lsm_batch_launches_per_step(None) == 0
