@@ -568,9 +568,9 @@ FWDADJ_BYTES = {
     "k_cvt_out": 4 + 8,
     "k_iface_scan_z": 4,           # phi; interface cells listed (the mass correction's adjoint)
     "k_mass_shift": 2 * 4,         # phi in, phi out
-    "k_mass_weights": 4,           # phi (interface cells' coordinates and weight atomics not counted)
     "k_tile_sum": 4,               # lam
-    "k_mass_apply": 8,             # fixed-point weights (lam read and written on interface nodes only)
+    # k_vol_iface, k_mass_weights and k_mass_apply walk the interface-cell
+    # list: their bytes scale with the interface, not with the node count
 }
 
 

@@ -1622,20 +1622,32 @@ __global__ void __launch_bounds__(256) k_inst_sum(const Inst* __restrict__ inst,
     }
 }
 
-// part 4: lam_pre = lam - (S / A) w with S = sum(lam) of the instance, w =
-// wfix in fixed point; clears wfix for the next step
+// part 4: lam_pre = lam - (S / A) w with S = sum(lam) of the instance and
+// w = wfix in fixed point, on the vertices of the listed interface cells
+// (the only nodes with a weight).  Each vertex's weight is taken and cleared
+// for the next step by one atomic exchange, so exactly one thread applies
+// it, whatever the list order.
 template <typename T>
-__global__ void k_mass_apply(Flat fl, const Mass* __restrict__ mass, const double* __restrict__ ssum,
-                             T* __restrict__ lam, unsigned long long* __restrict__ wfix) {
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < fl.n;
-         t += (long long)gridDim.x * blockDim.x) {
-        const long long q = (long long)wfix[t];
-        if (q == 0) continue;
-        wfix[t] = 0ull;
-        Node nd;
-        flat_node(fl, t, &nd);
-        const Mass M = mass[nd.inst];
-        lam[t] = (T)((double)lam[t] - ssum[nd.inst] / M.A * ((double)q * kVolUnit));
+__global__ void __launch_bounds__(128) k_mass_apply(Flat fl, const Mass* __restrict__ mass,
+                                                    const double* __restrict__ ssum, const unsigned* __restrict__ list,
+                                                    const unsigned* __restrict__ count, T* __restrict__ lam,
+                                                    unsigned long long* __restrict__ wfix) {
+    const unsigned n = *count;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long l = list[e];
+        const int q = node_instance(fl, l);
+        const Mass M = mass[q];
+        if (!mass_on(M)) continue;
+        const Inst& I = fl.inst[q];
+        const long long sj = I.ni, sk = (long long)I.ni * I.nj;
+        const long long o[8] = {l, l + 1, l + 1 + sj, l + sj, l + sk, l + 1 + sk, l + 1 + sj + sk, l + sj + sk};
+        const double r = ssum[q] / M.A;
+#pragma unroll
+        for (int v = 0; v < 8; ++v) {
+            const long long w = (long long)atomicExch(wfix + o[v], 0ull);
+            if (w != 0) lam[o[v]] = (T)((double)lam[o[v]] - r * ((double)w * kVolUnit));
+        }
     }
 }
 
@@ -2308,8 +2320,7 @@ void mass_adjoint(int grid2, const Inst* inst, const Brick* bmap2, int nb2, cons
         k_inst_sum<<<fl.ninst, 256, 0, s>>>(inst, part, ssum);
     }
     ProfScope ps_("k_mass_apply", s);
-    k_mass_apply<T><<<(unsigned)std::min<long long>((fl.n + 255) / 256, 152 * 16), 256, 0, s>>>(fl, mass, ssum, lam,
-                                                                                                 wfix);
+    k_mass_apply<T><<<list_blocks(), 128, 0, s>>>(fl, mass, ssum, list, count, lam, wfix);
 }
 void w64(long long off, long long n, double dt, const double* const* m64, const double* const* u64,
          double* const* w, cudaStream_t s) {
