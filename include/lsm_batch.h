@@ -84,7 +84,12 @@ typedef struct lsm_batch_config {
 
 typedef struct lsm_batch* lsm_batch_handle;
 
-/* Allocate the packed device arrays of `ninst` instances on `device`. */
+/* Allocate the packed device arrays of `ninst` instances on `device`
+   (N = total nodes, below 2^32): 21
+   stencil-precision arrays of N, the FP64 coordinates and cell volumes (4 N
+   doubles), and for FP32 batches the FP64 metrics, velocity and
+   contravariant velocity (15 N doubles) and the relative vertex coordinates
+   of every cell (24 N floats). */
 int lsm_batch_create(lsm_batch_handle* h, int device, void* cuda_stream, int ninst,
                      const lsm_batch_instance* inst, const lsm_batch_config* cfg);
 int lsm_batch_destroy(lsm_batch_handle h);

@@ -1424,15 +1424,34 @@ __device__ __forceinline__ void cell_gather(const Inst& I, const FieldsT<T>& f, 
     const long long sj = I.ni, sk = (long long)I.ni * I.nj;
     o[0] = l; o[1] = l + 1; o[2] = l + 1 + sj; o[3] = l + sj;
     o[4] = l + sk; o[5] = l + 1 + sk; o[6] = l + 1 + sj + sk; o[7] = l + sj + sk;
+#pragma unroll
+    for (int v = 0; v < 8; ++v) P8[v] = __ldg(phi + o[v]);
+    if constexpr (sizeof(T) == 4) {
+        if (f.cellrel) {
+            // the same values, formed once per geometry (k_cell_rel)
+            const float4* r = reinterpret_cast<const float4*>(f.cellrel + 24 * l);
+            float q[24];
+#pragma unroll
+            for (int u = 0; u < 6; ++u) {
+                const float4 w = __ldg(r + u);
+                q[4 * u] = w.x; q[4 * u + 1] = w.y; q[4 * u + 2] = w.z; q[4 * u + 3] = w.w;
+            }
+#pragma unroll
+            for (int a = 0; a < 3; ++a) C[0][a] = T(0);
+#pragma unroll
+            for (int v = 1; v < 8; ++v)
+#pragma unroll
+                for (int a = 0; a < 3; ++a) C[v][a] = q[3 * (v - 1) + a];
+            return;
+        }
+    }
     double X0[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) X0[a] = __ldg(f.xyz[a] + l);
 #pragma unroll
-    for (int v = 0; v < 8; ++v) {
-        P8[v] = __ldg(phi + o[v]);
+    for (int v = 0; v < 8; ++v)
 #pragma unroll
         for (int a = 0; a < 3; ++a) C[v][a] = (T)(__ldg(f.xyz[a] + o[v]) - X0[a]);
-    }
 }
 
 // instance of packed node t (binary search over the node offsets)
@@ -1666,6 +1685,34 @@ __global__ void k_cell_hex(long long off, int ni, int nj, int nk, const double* 
 #pragma unroll
         for (int v = 0; v < 8; ++v) { C[v][0] = x[o[v]]; C[v][1] = y[o[v]]; C[v][2] = z[o[v]]; }
         cellfix[l] = __double2ll_rn(hex_volume(C) * kVolScale);
+    }
+}
+
+// FP32 coordinates of the vertices 1..7 of every cell relative to its vertex
+// 0, the differences formed in FP64 (cell_gather's values), 24 floats per
+// cell by base node
+__global__ void k_cell_rel(long long off, int ni, int nj, int nk, const double* __restrict__ x,
+                           const double* __restrict__ y, const double* __restrict__ z, float* __restrict__ rel) {
+    const long long ncell = (long long)(ni - 1) * (nj - 1) * (nk - 1);
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncell;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(c % (ni - 1)), j = (int)((c / (ni - 1)) % (nj - 1));
+        const int k = (int)(c / ((long long)(ni - 1) * (nj - 1)));
+        const long long sj = ni, sk = (long long)ni * nj;
+        const long long l = off + i + sj * j + sk * k;
+        const long long o[8] = {l, l + 1, l + 1 + sj, l + sj, l + sk, l + 1 + sk, l + 1 + sj + sk, l + sj + sk};
+        const double X0[3] = {x[l], y[l], z[l]};
+        float q[24];
+#pragma unroll
+        for (int v = 1; v < 8; ++v) {
+            q[3 * (v - 1)] = (float)(x[o[v]] - X0[0]);
+            q[3 * (v - 1) + 1] = (float)(y[o[v]] - X0[1]);
+            q[3 * (v - 1) + 2] = (float)(z[o[v]] - X0[2]);
+        }
+        q[21] = q[22] = q[23] = 0.f;
+        float4* r = reinterpret_cast<float4*>(rel + 24 * l);
+#pragma unroll
+        for (int u = 0; u < 6; ++u) r[u] = make_float4(q[4 * u], q[4 * u + 1], q[4 * u + 2], q[4 * u + 3]);
     }
 }
 
@@ -2333,6 +2380,13 @@ void cell_hex(long long off, int ni, int nj, int nk, const double* x, const doub
     ProfScope ps_("k_cell_hex", s);
     k_cell_hex<<<(unsigned)std::min<long long>((ncell + 255) / 256, 152 * 16), 256, 0, s>>>(off, ni, nj, nk, x, y, z,
                                                                                              cellfix);
+}
+void cell_rel(long long off, int ni, int nj, int nk, const double* x, const double* y, const double* z, float* rel,
+              cudaStream_t s) {
+    const long long ncell = (long long)(ni - 1) * (nj - 1) * (nk - 1);
+    ProfScope ps_("k_cell_rel", s);
+    k_cell_rel<<<(unsigned)std::min<long long>((ncell + 255) / 256, 152 * 16), 256, 0, s>>>(off, ni, nj, nk, x, y, z,
+                                                                                             rel);
 }
 int max_blocks_per_sm(int shape, int kernel) {
     int n = 0;

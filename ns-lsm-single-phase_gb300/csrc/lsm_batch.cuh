@@ -45,6 +45,10 @@ struct FieldsT {
     const double* W64[3];  // FP32 batches: W in FP64 (from the FP64 metrics and velocity) for the
                            // stage nodes within kBand64 eps of the interface; nullptr: not kept
     long long* cellfix;    // hexahedron volume of cell (i..i+1, j..j+1, k..k+1) in fixed point, by base node
+    // FP32 batches: per cell (by base node, 24 floats apart) the FP32
+    // coordinates of its vertices 1..7 relative to vertex 0 (differences
+    // formed in FP64), 21 values and 3 of padding; nullptr: formed per use
+    const float* cellrel;
 };
 using Fields = FieldsT<float>;
 
@@ -176,6 +180,10 @@ void w64(long long off, long long n, double dt, const double* const* m64, const 
 // instance's first node
 void cell_hex(long long off, int ni, int nj, int nk, const double* x, const double* y, const double* z,
               long long* cellfix, cudaStream_t s);
+// the relative vertex coordinates of every cell of one instance (FieldsT
+// cellrel; the same packed base arrays)
+void cell_rel(long long off, int ni, int nj, int nk, const double* x, const double* y, const double* z, float* rel,
+              cudaStream_t s);
 // resident CTAs per SM of the brick kernel k_contra of tile shape `shape`
 // (FP32; `kernel` is 0)
 int max_blocks_per_sm(int shape, int kernel);

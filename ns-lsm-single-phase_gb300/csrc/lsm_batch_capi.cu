@@ -57,6 +57,7 @@ struct lsm_batch {
     double** d_p64 = nullptr;
     std::vector<char> geom_set, vel_set;
     long long* cellfix = nullptr;  // N fixed-point cell hexahedron volumes
+    float* cellrel = nullptr;      // FP32 batches: 24 N floats, relative vertex coordinates per cell
     double* staging = nullptr;   // FP64 scratch for conversions (4 * max instance nodes)
     Inst* d_inst = nullptr;
     long long* d_offs = nullptr;
@@ -967,6 +968,8 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
     for (int a = 0; a < 15; ++a) b->comps[a] = (char*)b->field_arena + b->esz * b->ld * (6 + a);
     if (cudaMalloc(&b->xyz, 8 * b->ld8 * 4) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     b->cellfix = (long long*)(b->xyz + 3 * b->ld8);
+    if (!b->prec && cudaMalloc(&b->cellrel, sizeof(float) * 24 * (size_t)n) != cudaSuccess)
+        return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->staging, sizeof(double) * 4 * b->max_inst_nodes) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->d_inst, sizeof(Inst) * ninst) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->d_offs, sizeof(long long) * (ninst + 1)) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
@@ -1020,6 +1023,7 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
         }
         for (int c = 0; c < 9; ++c) f.m[c] = (T*)b->comps[3 + c];
         f.cellfix = b->cellfix;
+        f.cellrel = b->cellrel;
         for (int c = 0; c < 3; ++c) f.W64[c] = b->f64x ? b->f64x + (size_t)(12 + c) * b->ld8 : nullptr;
     };
     if (b->prec) wire(b->f64, (double*)nullptr);
@@ -1041,7 +1045,7 @@ int lsm_batch_destroy(lsm_batch_handle b) {
                     (void*)b->d_brick, (void*)b->d_amap[0], (void*)b->d_amap[1], (void*)b->d_amap[2],
                     (void*)b->d_amap[3], (void*)b->d_vacc, (void*)b->d_vols, (void*)b->d_err, b->adj,
                     (void*)b->d_target, (void*)b->d_mass, (void*)b->wfix, (void*)b->d_tpart, (void*)b->d_ssum,
-                    (void*)b->d_ilist, (void*)b->d_icount, (void*)b->f64x, (void*)b->d_p64})
+                    (void*)b->d_ilist, (void*)b->d_icount, (void*)b->f64x, (void*)b->d_p64, (void*)b->cellrel})
         if (p) cudaFree(p);
     if (b->h_vols) cudaFreeHost(b->h_vols);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
@@ -1073,6 +1077,8 @@ int lsm_batch_set_geometry(lsm_batch_handle b, int q, const double* x, const dou
     update_w64(b, q);
     // cell_hex indexes from the packed base arrays with the instance offset o
     lsm::batch::cell_hex(o, I.ni, I.nj, I.nk, b->xyz, b->xyz + b->ld8, b->xyz + 2 * b->ld8, b->cellfix, b->stream);
+    if (b->cellrel)
+        lsm::batch::cell_rel(o, I.ni, I.nj, I.nk, b->xyz, b->xyz + b->ld8, b->xyz + 2 * b->ld8, b->cellrel, b->stream);
     BCU(b, cudaGetLastError());
     BCU(b, cudaStreamSynchronize(b->stream));
     return LSM_OK;

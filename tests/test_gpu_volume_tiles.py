@@ -4,7 +4,9 @@ tile's last lane itself, and a z tile may hold only the grid's last plane
 (no cells).  The FP64 batch's volumes (K tetrahedra, second tetrahedra,
 bulk, total) must equal the oracle's TotalWaterVolume of the same field:
 every cell counted once (fixed-point rounding of each cell's share to
-2^-48 bounds the difference far below the 1e-10 bar)."""
+2^-48 bounds the difference far below the 1e-10 bar).  The FP32 batch
+(phi rounded to FP32, the cells' relative vertex coordinates formed once
+per geometry) must agree to 1e-6."""
 import numpy as np
 import pytest
 
@@ -30,7 +32,7 @@ def _case(ni, nj, nk):
     return F(X), F(Y), F(Z), F(phi)
 
 
-def _batch_volumes(oracle, shapes):
+def _batch_volumes(oracle, shapes, precision="fp64"):
     from nslsm.batch import LevelSetBatch
     cases = []
     for s in shapes:
@@ -38,7 +40,7 @@ def _batch_volumes(oracle, shapes):
         csi, eta, zet, _ = oracle.mg_metrics(O.make_grid(*s), x, y, z)
         cases.append((s, x, y, z, phi, csi, eta, zet))
     b = LevelSetBatch([(*s, 1e-3, 1e-3, 1e-2) for s, *_ in cases], RNitermax=2, btype=(1,) * 6, BigPhi=5.0,
-                      precision="fp64", autotune=False)
+                      precision=precision, autotune=False)
     q = [np.zeros((4,) + s, order="F") for s, *_ in cases]
     for k, (s, x, y, z, phi, csi, eta, zet) in enumerate(cases):
         b.set_geometry(k, x, y, z, csi, eta, zet)
@@ -62,3 +64,9 @@ def test_scan_volume_equals_oracle_uneven_batch(oracle, lib_built):
     v, ref = _batch_volumes(oracle, SHAPES)
     for k in range(len(SHAPES)):
         assert np.all(np.abs(v[k] - ref[k]) <= 1e-10 * ref[k][3]), (k, v[k], ref[k])
+
+
+def test_scan_volume_fp32_batch_within_fp32_rounding(oracle, lib_built):
+    v, ref = _batch_volumes(oracle, SHAPES, "fp32")
+    for k in range(len(SHAPES)):
+        assert abs(v[k][3] - ref[k][3]) <= 1e-6 * ref[k][3], (k, v[k], ref[k])
