@@ -541,6 +541,17 @@ void enqueue_step(lsm_batch* b) {
     else enqueue_step_io<float>(b, b->f32.phi, b->f32.phi, nullptr, true);
 }
 
+// W of every instance from the current metrics and velocity (the steps
+// read it; set_geometry / set_velocity mark it stale)
+int refresh_w(lsm_batch* b) {
+    if (!b->w_stale) return LSM_OK;
+    if (b->prec) lsm::batch::contra<double>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, b->f64, b->stream);
+    else lsm::batch::contra<float>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, b->f32, b->stream);
+    BCU(b, cudaGetLastError());
+    b->w_stale = false;
+    return LSM_OK;
+}
+
 // Chooses the tile shape of the brick-table kernels and whether the plain
 // pseudo-steps march in k (reinit_z) or walk the brick table: times, on
 // the batch itself, the brick pseudo-steps for every shape and the marching
@@ -595,8 +606,11 @@ int autotune(lsm_batch* b) {
     b->reinit_march = zm < br[best_b];
     const int bs = build_bricks(b, best_b);
     if (bs != LSM_OK) return done(bs);
-    // the RK stage: plane tiles staged by TMA copies or by the threads
+    // the RK stage: plane tiles staged by TMA copies or by the threads,
+    // timed on this batch's contravariant velocity (its upwind choices)
     if (b->tma_eligible) {
+        const int sw = refresh_w(b);
+        if (sw != LSM_OK) return done(sw);
         float ms_plain = 0.f, ms_tma = 0.f;
         const int st2 = timed(
             &ms_plain, &ms_tma,
@@ -626,16 +640,6 @@ int stage_override() {
     return -1;
 }
 
-// W of every instance from the current metrics and velocity (the steps
-// read it; set_geometry / set_velocity mark it stale)
-int refresh_w(lsm_batch* b) {
-    if (!b->w_stale) return LSM_OK;
-    if (b->prec) lsm::batch::contra<double>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, b->f64, b->stream);
-    else lsm::batch::contra<float>(b->shape, b->grid, b->d_inst, b->d_brick, b->nbricks, b->f32, b->stream);
-    BCU(b, cudaGetLastError());
-    b->w_stale = false;
-    return LSM_OK;
-}
 
 int prepare(lsm_batch* b) {
     if (!b->tuned) {
