@@ -1730,10 +1730,18 @@ __device__ __forceinline__ T prev_value(const BC& bc, const P0& p0, int face, in
 }
 
 template <typename T>
-__global__ void k_adj_face(Flat fl, int face, long long nplane, BC bc, int kind, const T* __restrict__ phin,
-                           const T* __restrict__ in, const T* __restrict__ out, T c1, T c2, T* lam) {
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (t >= nplane || !face_on(bc, face)) return;
+__global__ void k_adj_face(Flat fl, int face0, long long nplane, int nface, BC bc, int kind,
+                           const T* __restrict__ phin, const T* __restrict__ in, const T* __restrict__ out, T c1, T c2,
+                           T* lam) {
+    // nface 2: face0 (odd) and the opposite face face0 - 1 of the same axis in
+    // one launch (no shared nodes, no shared targets when the axis has at
+    // least 6 nodes in every instance)
+    const long long tt = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (tt >= nplane * nface) return;
+    const bool second = tt >= nplane;
+    const int face = second ? face0 - 1 : face0;
+    const long long t = second ? tt - nplane : tt;
+    if (!face_on(bc, face)) return;
     const int ax = face >> 1;
     int lo = 0, hi = fl.ninst - 1;
     while (lo < hi) {
@@ -2401,10 +2409,11 @@ int vol_scan_blocks_per_sm() {
 }
 
 template <typename T>
-void adj_face(const Flat& fl, int face, long long nplane, BC bc, int kind, const T* phin, const T* in, const T* out,
-              double c1, double c2, T* lam, cudaStream_t s) {
+void adj_face(const Flat& fl, int face, long long nplane, int nface, BC bc, int kind, const T* phin, const T* in,
+              const T* out, double c1, double c2, T* lam, cudaStream_t s) {
     ProfScope ps_("k_adj_face", s);
-    k_adj_face<T><<<flat_blocks(nplane), 256, 0, s>>>(fl, face, nplane, bc, kind, phin, in, out, T(c1), T(c2), lam);
+    k_adj_face<T><<<flat_blocks(nplane * nface), 256, 0, s>>>(fl, face, nplane, nface, bc, kind, phin, in, out, T(c1),
+                                                              T(c2), lam);
 }
 template <typename T>
 void adj_stage(const int* grid, const Inst* inst, const Brick* const* bmap, const int* nb, FieldsT<T> f, const T* in,
@@ -2472,8 +2481,8 @@ void adj_contra(const Flat& fl, FieldsT<T> f, const T* w0, const T* w1, const T*
     template void mass_adjoint<T>(int, const Inst*, const Brick*, int, const Flat&, FieldsT<T>, const T*,          \
                                   const Mass*, T*, unsigned long long*, double*, double*, unsigned*, unsigned*,        \
                                   cudaStream_t);                                                                     \
-    template void adj_face<T>(const Flat&, int, long long, BC, int, const T*, const T*, const T*, double, double, T*, \
-                              cudaStream_t);                                                                          \
+    template void adj_face<T>(const Flat&, int, long long, int, BC, int, const T*, const T*, const T*, double, double, \
+                              T*, cudaStream_t);                                                                     \
     template void adj_stage<T>(const int*, const Inst*, const Brick* const*, const int*, FieldsT<T>, const T*,      \
                                const T*, T*, T*, T*, T*, T*, double, double, double, bool, cudaStream_t);      \
     template void adj_reinit<T>(int, const Inst*, const Brick*, int, FieldsT<T>, const T*, const T*, T*,            \

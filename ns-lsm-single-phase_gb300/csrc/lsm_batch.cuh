@@ -209,9 +209,12 @@ __host__ __device__ constexpr AdjShape adj_shape(int map) {
 // switch are evaluated from the pre-BC field P0, given as
 //   kind 0 (stage):  interior = out, boundary = c1*phin + c2*in
 //   kind 1 (field):  P0 = src (passed as `out`) everywhere
+// nface 2 reverses the odd `face` and the opposite face face - 1 of the same
+// axis in one launch (valid when every instance has at least 6 nodes along
+// that axis: the two faces' nodes and targets are then disjoint)
 template <typename T>
-void adj_face(const Flat& fl, int face, long long nface_nodes, BC bc, int kind, const T* phin, const T* in,
-              const T* out, double c1, double c2, T* lam, cudaStream_t s);
+void adj_face(const Flat& fl, int face, long long nface_nodes, int nface, BC bc, int kind, const T* phin,
+              const T* in, const T* out, double c1, double c2, T* lam, cudaStream_t s);
 // Reverse of one RK stage in three passes (x on adjoint map 0 by warp
 // shuffles, y and z marches on maps 1 and 2).  lamP0: adjoint of the
 // stage's pre-BC field; writes lam_in = c2 lamP0 - c3 (dR/din)^T lamP0

@@ -38,6 +38,9 @@ struct lsm_batch {
     lsm_batch_config cfg{};
     std::vector<long long> off;  // ninst + 1 node offsets
     long long N = 0, nface = 0, max_inst_nodes = 0, nplane[3] = {0, 0, 0};
+    // the adjoint reverses the two faces of axis a in one launch when every
+    // instance has at least 6 nodes along a (their targets are then disjoint)
+    bool face_pair[3] = {false, false, false};
     FieldsT<float> f32{};
     FieldsT<double> f64{};
     // Per-node arrays live in arenas with a stride between arrays that is a
@@ -836,8 +839,14 @@ void adj_step(lsm_batch* b, AdjView<T>& v, const Rec<T>& r, const T* phin, const
         B::mass_adjoint<T>(b->vgrid, b->d_inst, b->d_amap[2], b->namap[2], fl, f, r.P, m, v.lam, b->wfix, b->d_tpart,
                            b->d_ssum, b->d_ilist, b->d_icount, b->stream);
     auto faces = [&](int kind, const T* pn, const T* in, const T* out, double c1, double c2) {
-        for (int face = 5; face >= 0; --face)
-            B::adj_face<T>(fl, face, b->nplane[face >> 1], bc, kind, pn, in, out, c1, c2, v.lam, b->stream);
+        for (int ax = 2; ax >= 0; --ax) {
+            if (b->face_pair[ax]) {
+                B::adj_face<T>(fl, 2 * ax + 1, b->nplane[ax], 2, bc, kind, pn, in, out, c1, c2, v.lam, b->stream);
+            } else {
+                B::adj_face<T>(fl, 2 * ax + 1, b->nplane[ax], 1, bc, kind, pn, in, out, c1, c2, v.lam, b->stream);
+                B::adj_face<T>(fl, 2 * ax, b->nplane[ax], 1, bc, kind, pn, in, out, c1, c2, v.lam, b->stream);
+            }
+        }
     };
     if (R > 0) {
         faces(1, nullptr, nullptr, rec_d(b, r, R - 1), 0.0, 0.0);
@@ -957,6 +966,13 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
     }
     b->off.push_back(n);
     b->N = n;
+    for (int a = 0; a < 3; ++a) {
+        b->face_pair[a] = true;
+        for (int q = 0; q < ninst; ++q) {
+            const int na = a == 0 ? inst[q].ni : a == 1 ? inst[q].nj : inst[q].nk;
+            if (na < 6) b->face_pair[a] = false;
+        }
+    }
     if (n >= (1LL << 32)) {   // the interface-cell list holds 32-bit node indices
         delete b;
         return LSM_ERR_BAD_SHAPE;

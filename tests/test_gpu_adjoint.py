@@ -303,3 +303,46 @@ def test_tiny_ragged_instances_adjoint(oracle, lib_built, mode):
         (out * T.to_torch(wts[k], "cuda")).sum().backward()
         assert _rel(gphi[k], np.asfortranarray(p.grad.cpu().numpy().T)) <= 1e-10
         assert _rel(gq[k], np.asfortranarray(q.grad.cpu().numpy().T)) <= 1e-10
+
+
+def test_fp64_adjoint_thin_instances_match_torch_tape(oracle, lib_built):
+    """Instances with fewer than 6 nodes along an axis: the adjoint then
+    reverses that axis's two boundary faces one after the other instead of
+    in one launch (their targets would overlap).  Gradients equal the torch
+    tape to 1e-10 on a batch whose x and z axes take the sequential path and
+    whose y axis takes the paired one."""
+    from types import SimpleNamespace
+    from nslsm.configs import _mesh
+    cases = []
+    for shape in ((16, 12, 5), (5, 14, 9)):
+        XI, ET, ZE = _mesh(*shape)
+        X, Y, Z = XI + 0.05 * ET, ET - 0.03 * ZE, ZE + 0.04 * XI
+        F = lambda a: np.asfortranarray(a, dtype=np.float64)  # noqa: E731
+        q = np.zeros((4,) + shape, order="F")
+        q[1] = 0.6 + 0.3 * np.sin(2 * np.pi * Y)
+        q[2] = -0.4 * np.cos(2 * np.pi * X)
+        q[3] = 0.2 * np.sin(2 * np.pi * X)
+        h = 1.0 / (max(shape) - 1)
+        it = SimpleNamespace(grid=SimpleNamespace(shape=shape), x=F(X), y=F(Y), z=F(Z),
+                             phi0=F(Z - 0.5 - 0.04 * np.cos(2 * np.pi * (2 * X + Y))), q=F(q), dtau=0.5 * h,
+                             eps=1.5 * h)
+        g = O.make_grid(*shape)
+        csi, eta, zet, aj = oracle.mg_metrics(g, it.x, it.y, it.z)
+        smax = max(float(np.abs(m[0] * q[1] + m[1] * q[2] + m[2] * q[3]).max()) for m in (csi, eta, zet))
+        cases.append(dict(it=it, g=g, csi=csi, eta=eta, zet=zet, aj=aj, dt=0.4 / smax))
+    R = 3
+    b = _batch(cases, R)
+    wts = _weights(cases)
+    gphi, gq = _adjoint(b, cases, wts)
+    b.close()
+    for k, c in enumerate(cases):
+        it = c["it"]
+        M = T.metrics_torch(c["csi"], c["eta"], c["zet"], "cuda")
+        p = T.to_torch(it.phi0, "cuda").requires_grad_(True)
+        q = T.to_torch(it.q, "cuda").requires_grad_(True)
+        out = T.run(p, q, M, c["dt"], it.dtau, it.eps, R, NSTEPS)
+        (out * T.to_torch(wts[k], "cuda")).sum().backward()
+        ref_phi = np.asfortranarray(p.grad.cpu().numpy().T)
+        ref_q = np.asfortranarray(q.grad.cpu().numpy().T)
+        assert _rel(gphi[k], ref_phi) <= 1e-10, (k, _rel(gphi[k], ref_phi))
+        assert _rel(gq[k], ref_q) <= 1e-10, (k, _rel(gq[k], ref_q))
