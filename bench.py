@@ -566,7 +566,6 @@ FWDADJ_BYTES = {
     "k_adj_contra": 18 * 4,        # lamW(3), metrics(9), lam_u(3, rmw)
     "k_cvt_in": 8 + 4,
     "k_cvt_out": 4 + 8,
-    "k_iface_scan_z": 4,           # phi; interface cells listed (the mass correction's adjoint)
     "k_mass_shift": 2 * 4,         # phi in, phi out
     "k_tile_sum": 4,               # lam
     # k_vol_iface, k_mass_weights and k_mass_apply walk the interface-cell

@@ -142,8 +142,10 @@ int lsm_batch_mass_state(lsm_batch_handle h, double* out);
    from its checkpoint (keeping its internals); with nsteps <=
    checkpoint_every nothing is recomputed.  Device memory: N (ceil(nsteps /
    k) + k (5 + m + c RNitermax) + 9) elements of the batch precision, k =
-   checkpoint_every, c = 6 (adjoint_mode 0) or 1 (adjoint_mode 1), m = 1
-   with the mass correction (which adds N 8-byte words of scratch) else 0. */
+   checkpoint_every, c = 6 (adjoint_mode 0) or 1 (adjoint_mode 1), m = 2
+   with the mass correction (each recorded step keeps its pre-correction
+   field and that field's interface cells; N 8-byte words of scratch more)
+   else 0. */
 int lsm_batch_forward_record(lsm_batch_handle h, int nsteps, int checkpoint_every);
 /* Seed dL/dphi at the end of the recorded steps for one instance (FP64, host
    or device; instances not seeded get zero). */

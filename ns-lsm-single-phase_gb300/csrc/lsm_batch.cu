@@ -2354,14 +2354,9 @@ void mass_shift(const Flat& fl, const Mass* mass, const T* src, T* dst, cudaStre
     k_mass_shift<T><<<(unsigned)std::min<long long>((fl.n + 255) / 256, 152 * 16), 256, 0, s>>>(fl, mass, src, dst);
 }
 template <typename T>
-void mass_adjoint(int grid2, const Inst* inst, const Brick* bmap2, int nb2, const Flat& fl, FieldsT<T> f,
-                  const T* phi_pre, const Mass* mass, T* lam, unsigned long long* wfix, double* part, double* ssum,
-                  unsigned* list, unsigned* count, cudaStream_t s) {
-    cudaMemsetAsync(count, 0, sizeof(unsigned), s);
-    {
-        ProfScope ps_("k_iface_scan_z", s);
-        k_vol_scan_z<T, false><<<grid2, 256, 0, s>>>(inst, bmap2, nb2, f, phi_pre, nullptr, list, count);
-    }
+void mass_adjoint(const Inst* inst, const Brick* bmap2, int nb2, const Flat& fl, FieldsT<T> f, const T* phi_pre,
+                  const Mass* mass, T* lam, unsigned long long* wfix, double* part, double* ssum, const unsigned* list,
+                  const unsigned* count, cudaStream_t s) {
     {
         ProfScope ps_("k_mass_weights", s);
         k_mass_weights<T><<<list_blocks(), 128, 0, s>>>(fl, f, phi_pre, list, count, mass, wfix);
@@ -2478,8 +2473,8 @@ void adj_contra(const Flat& fl, FieldsT<T> f, const T* w0, const T* w1, const T*
                             unsigned long long*, bool, unsigned*, unsigned*, cudaStream_t);                          \
     template int vol_scan_blocks_per_sm<T>();                                                                   \
     template void mass_shift<T>(const Flat&, const Mass*, const T*, T*, cudaStream_t);                                 \
-    template void mass_adjoint<T>(int, const Inst*, const Brick*, int, const Flat&, FieldsT<T>, const T*,          \
-                                  const Mass*, T*, unsigned long long*, double*, double*, unsigned*, unsigned*,        \
+    template void mass_adjoint<T>(const Inst*, const Brick*, int, const Flat&, FieldsT<T>, const T*, const Mass*,  \
+                                  T*, unsigned long long*, double*, double*, const unsigned*, const unsigned*,          \
                                   cudaStream_t);                                                                     \
     template void adj_face<T>(const Flat&, int, long long, int, BC, int, const T*, const T*, const T*, double, double, \
                               T*, cudaStream_t);                                                                     \

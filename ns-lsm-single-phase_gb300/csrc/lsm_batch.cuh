@@ -246,12 +246,13 @@ void mass_shift(const Flat& fl, const Mass* mass, const T* src, T* dst, cudaStre
 // Reverse of the shift phi' = phi + C(phi) in place on lam (the adjoint of
 // phi'): lam -= (sum(lam) / A) (dK/dphi + C d(dK/dC)/dphi), evaluated on
 // the step's pre-correction field phi_pre; wfix (N 64-bit words, zero on
-// entry and on exit), part (one double per tile of adjoint map 2), ssum
-// (one per instance) and the interface-cell list (list, count) are scratch
+// entry and on exit), part (one double per tile of adjoint map 2) and ssum
+// (one per instance) are scratch; (list, count) are the interface cells of
+// phi_pre as the forward step's volume pass listed them
 template <typename T>
-void mass_adjoint(int grid2, const Inst* inst, const Brick* bmap2, int nb2, const Flat& fl, FieldsT<T> f,
-                  const T* phi_pre, const Mass* mass, T* lam, unsigned long long* wfix, double* part, double* ssum,
-                  unsigned* list, unsigned* count, cudaStream_t s);
+void mass_adjoint(const Inst* inst, const Brick* bmap2, int nb2, const Flat& fl, FieldsT<T> f, const T* phi_pre,
+                  const Mass* mass, T* lam, unsigned long long* wfix, double* part, double* ssum, const unsigned* list,
+                  const unsigned* count, cudaStream_t s);
 // lam_u_c += sum_m M[m][c] dt lamW_m  (the W = dt M u chain rule)
 template <typename T>
 void adj_contra(const Flat& fl, FieldsT<T> f, const T* lamW0, const T* lamW1, const T* lamW2, T* lu0, T* lu1,

@@ -416,6 +416,8 @@ struct Rec {
     T* sgn;   // mode 1 only
     T* C;     // mode 0 only
     T* P;     // mass correction only
+    unsigned* list;    // mass correction only: the interface cells of P (the step's volume pass)
+    unsigned* count;   // and their number
 };
 
 // raw output of pseudo-step k of a recorded step (mode 1: every k; mode 0:
@@ -532,8 +534,10 @@ void enqueue_step_io(lsm_batch* b, const T* phin, T* phi_out, const Rec<T>* rec,
     if (mc) {
         // FP64 water volume of the result, the correction C = (target - V) / A
         // and phi_out = result + C
-        B::volume<T>(b->vgrid, b->d_inst, b->d_amap[2], b->namap[2], fl, f, res, b->d_vacc, true, b->d_ilist,
-                     b->d_icount, b->stream);
+        // a recorded step keeps the interface cells of its result for the
+        // reverse of the correction
+        B::volume<T>(b->vgrid, b->d_inst, b->d_amap[2], b->namap[2], fl, f, res, b->d_vacc, true,
+                     rec ? rec->list : b->d_ilist, rec ? rec->count : b->d_icount, b->stream);
         B::volume_final(b->ninst, b->d_vacc, b->d_vols, b->d_target, b->d_mass, mrec, b->stream);
         if (phi_out) B::mass_shift<T>(fl, b->d_mass, res, phi_out, b->stream);
     }
@@ -700,17 +704,22 @@ template <typename T>
 struct AdjView {
     T *ckpt, *seg, *slots, *lam, *lam2, *lamPhin, *lamW[3], *lamU[3];
     Mass* mrec;   // mass correction of every step of the segment, ninst per step
+    unsigned* lcount;   // interface-cell count of every step of the segment (Rec::count)
 };
 
 int n_ckpt(int nsteps, int ck) { return (nsteps + ck - 1) / ck; }
 // arrays of one recorded step, each b->ld elements apart
 long long slot_elems(const lsm_batch* b) {
     const long long R = b->cfg.RNitermax;
-    return ((b->cfg.adjoint_mode == 0 ? 4 + 6 * R : 4 + R) + (b->cfg.mass_correction ? 1 : 0)) * (long long)b->ld;
+    // with the mass correction: the pre-correction field P and the interface
+    // cells of P (32-bit node indices, one array)
+    return ((b->cfg.adjoint_mode == 0 ? 4 + 6 * R : 4 + R) + (b->cfg.mass_correction ? 2 : 0)) * (long long)b->ld;
 }
 
 size_t adj_elems(const lsm_batch* b, int nsteps, int ck) {
-    const size_t mrec = ((size_t)ck * (size_t)b->ninst * sizeof(Mass) + b->esz - 1) / b->esz;
+    // the recorded steps' mass states, then their interface-cell counts
+    const size_t mrec =
+        ((size_t)ck * (size_t)b->ninst * sizeof(Mass) + (size_t)ck * sizeof(unsigned) + b->esz - 1) / b->esz;
     return b->ld * (size_t)(n_ckpt(nsteps, ck) + ck + 3 + 3 + 3) + (size_t)ck * (size_t)slot_elems(b) + mrec;
 }
 
@@ -728,7 +737,9 @@ Rec<T> slot(lsm_batch* b, const AdjView<T>& v, int q) {
         r.C = nullptr;
         r.sgn = p + (3 + b->cfg.RNitermax) * L;
     }
-    r.P = b->cfg.mass_correction ? p + slot_elems(b) - L : nullptr;
+    r.P = b->cfg.mass_correction ? p + slot_elems(b) - 2 * L : nullptr;
+    r.list = b->cfg.mass_correction ? reinterpret_cast<unsigned*>(p + slot_elems(b) - L) : nullptr;
+    r.count = b->cfg.mass_correction ? v.lcount + q : nullptr;
     return r;
 }
 
@@ -758,6 +769,7 @@ AdjView<T> adj_view(lsm_batch* b) {
         p += N;
     }
     v.mrec = (Mass*)p;   // arrays are multiples of 256 bytes apart
+    v.lcount = reinterpret_cast<unsigned*>(v.mrec + (long long)b->rec_ck * b->ninst);
     return v;
 }
 
@@ -836,8 +848,8 @@ void adj_step(lsm_batch* b, AdjView<T>& v, const Rec<T>& r, const T* phin, const
     const int R = b->cfg.RNitermax;
     // reverse of the mass correction phi^{n+1} = P + C(P), in place on lam
     if (b->cfg.mass_correction)
-        B::mass_adjoint<T>(b->vgrid, b->d_inst, b->d_amap[2], b->namap[2], fl, f, r.P, m, v.lam, b->wfix, b->d_tpart,
-                           b->d_ssum, b->d_ilist, b->d_icount, b->stream);
+        B::mass_adjoint<T>(b->d_inst, b->d_amap[2], b->namap[2], fl, f, r.P, m, v.lam, b->wfix, b->d_tpart,
+                           b->d_ssum, r.list, r.count, b->stream);
     auto faces = [&](int kind, const T* pn, const T* in, const T* out, double c1, double c2) {
         for (int ax = 2; ax >= 0; --ax) {
             if (b->face_pair[ax]) {

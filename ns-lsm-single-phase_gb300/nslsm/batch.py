@@ -170,10 +170,11 @@ class LevelSetBatch:
     def adjoint_bytes(nodes: int, RNitermax: int, nsteps: int, checkpoint_every: int, precision: str = "fp32",
                       adjoint_mode: str = "store", mass_correction: bool = False) -> int:
         """Device bytes forward_record allocates for the adjoint state (padding ignored):
-        N (ceil(nsteps / k) + k (5 + m + c R) + 9) elements, c = 6 (store) or 1 (recompute), m = 1
-        with the mass correction (plus N 8-byte words of scratch)."""
+        N (ceil(nsteps / k) + k (5 + m + c R) + 9) elements, c = 6 (store) or 1 (recompute), m = 2
+        with the mass correction (the pre-correction field and its interface-cell list per step,
+        plus N 8-byte words of scratch)."""
         c = 6 if adjoint_mode == "store" else 1
-        m = 1 if mass_correction else 0
+        m = 2 if mass_correction else 0
         k = min(int(checkpoint_every), int(nsteps))
         arrays = -(-int(nsteps) // k) + k * (5 + m + c * int(RNitermax)) + 9
         return int(nodes) * arrays * (8 if precision == "fp64" else 4) + (8 * int(nodes) if m else 0)
