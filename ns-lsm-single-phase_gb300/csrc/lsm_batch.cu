@@ -1294,8 +1294,8 @@ __device__ void cell_mass_weights(const P (&ph8)[8], const P (&C)[8][3], P Cs, P
     }
 }
 
-// The volume pass runs in two kernels.  k_vol_scan streams every cell of
-// every instance (one thread per cell on the brick table): cells whose
+// The volume pass runs in two kernels.  k_vol_scan_z streams every cell of
+// every instance (a k march over the tiles of adjoint map 2): cells whose
 // eight vertices are water (phi > eps_sims, in the phi type) add their
 // precomputed FP64 hexahedron volume in 64-bit fixed point; interface cells
 // (any other mix) are appended to a list, each warp reserving its slots with
@@ -1303,7 +1303,8 @@ __device__ void cell_mass_weights(const P (&ph8)[8], const P (&C)[8][3], P Cs, P
 // the result does not depend on it).  k_vol_iface then runs the reference's
 // six-tetrahedra split on the listed cells with every lane busy, in the
 // stencil precision on coordinates relative to each cell's first vertex
-// (differences formed in FP64), optionally with the mass correction's slope
+// (differences formed in FP64; an FP32 batch keeps them per cell, formed
+// once per geometry), optionally with the mass correction's slope
 // dK/dC.  Each cell's shares are rounded to multiples of 2^-48 and added to
 // the instance's accumulators with integer atomics after a warp sum: exact
 // and order-independent.
