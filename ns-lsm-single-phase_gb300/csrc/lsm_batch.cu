@@ -456,16 +456,17 @@ __global__ void __launch_bounds__(256) k_stage_tma(const __grid_constant__ CUten
                 float D0 = 0.f, D1 = 0.f, D2 = 0.f;
                 if (interior) {
                     const int x = tx + 4, y = ty + 2;
-                    D0 = weno_diff(i > 1 ? P[y][x - 2] : 0.f, P[y][x - 1], w2, P[y][x + 1],
-                                   i < ni - 2 ? P[y][x + 2] : 0.f, W0, i == 1, i == ni - 2);
-                    D1 = weno_diff(j > 1 ? P[y - 2][x] : 0.f, P[y - 1][x], w2, P[y + 1][x],
-                                   j < nj - 2 ? P[y + 2][x] : 0.f, W1, j == 1, j == nj - 2);
-                    const float p2 = k < nk - 2 ? w4 : 0.f;
+                    // the outer stencil values are read unconditionally: the
+                    // tile always holds them (zero-filled outside the grid),
+                    // and weno_diff leaves m2 unused at the first interior node
+                    // and p2 at the last
+                    D0 = weno_diff(P[y][x - 2], P[y][x - 1], w2, P[y][x + 1], P[y][x + 2], W0, i == 1, i == ni - 2);
+                    D1 = weno_diff(P[y - 2][x], P[y - 1][x], w2, P[y + 1][x], P[y + 2][x], W1, j == 1, j == nj - 2);
+                    const float p2 = w4;
                     const float fp = rec3(Pk ? w1 : p2, Pk ? w2 : w3, Pk ? w3 : w2);
                     float fm = fpz;
                     if (!all_reuse) {
-                        const float m2 = k > 1 ? w0 : 0.f;
-                        const float g = rec3(Mk ? m2 : w3, Mk ? w1 : w2, Mk ? w2 : w1);
+                        const float g = rec3(Mk ? w0 : w3, Mk ? w1 : w2, Mk ? w2 : w1);
                         if (!reuse) fm = g;
                     }
                     D2 = fp - fm;
