@@ -288,16 +288,17 @@ __global__ void __launch_bounds__(256) k_stage_z(const Inst* __restrict__ inst, 
                 T D0 = T(0), D1 = T(0), D2 = T(0);
                 if (interior) {
                     const int x = tx + 2, y = ty + 2;
-                    D0 = weno_diff(i > 1 ? P[y][x - 2] : T(0), P[y][x - 1], w2, P[y][x + 1],
-                                   i < ni - 2 ? P[y][x + 2] : T(0), W0, i == 1, i == ni - 2);
-                    D1 = weno_diff(j > 1 ? P[y - 2][x] : T(0), P[y - 1][x], w2, P[y + 1][x],
-                                   j < nj - 2 ? P[y + 2][x] : T(0), W1, j == 1, j == nj - 2);
-                    const T p2 = k < nk - 2 ? w4 : T(0);
+                    // the outer stencil values are read unconditionally: every
+                    // slot of the cross is written each plane (zero outside the
+                    // grid), and weno_diff leaves m2 unused at the first
+                    // interior node and p2 at the last
+                    D0 = weno_diff(P[y][x - 2], P[y][x - 1], w2, P[y][x + 1], P[y][x + 2], W0, i == 1, i == ni - 2);
+                    D1 = weno_diff(P[y - 2][x], P[y - 1][x], w2, P[y + 1][x], P[y + 2][x], W1, j == 1, j == nj - 2);
+                    const T p2 = w4;
                     const T fp = rec3(Pk ? w1 : p2, Pk ? w2 : w3, Pk ? w3 : w2);
                     T fm = fpz;
                     if (!all_reuse) {
-                        const T m2 = k > 1 ? w0 : T(0);
-                        const T g = rec3(Mk ? m2 : w3, Mk ? w1 : w2, Mk ? w2 : w1);
+                        const T g = rec3(Mk ? w0 : w3, Mk ? w1 : w2, Mk ? w2 : w1);
                         if (!reuse) fm = g;
                     }
                     D2 = fp - fm;
