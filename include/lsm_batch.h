@@ -88,8 +88,9 @@ typedef struct lsm_batch* lsm_batch_handle;
    (N = total nodes, below 2^32): 21
    stencil-precision arrays of N, the FP64 coordinates and cell volumes (4 N
    doubles), and for FP32 batches the FP64 metrics, velocity and
-   contravariant velocity (15 N doubles) and the relative vertex coordinates
-   of every cell (24 N floats). */
+   contravariant velocity (15 N doubles) and, when they fit, the relative
+   vertex coordinates of every cell (24 N floats; a cache: without it the
+   volume kernels form the same values per use). */
 int lsm_batch_create(lsm_batch_handle* h, int device, void* cuda_stream, int ninst,
                      const lsm_batch_instance* inst, const lsm_batch_config* cfg);
 int lsm_batch_destroy(lsm_batch_handle h);

@@ -1000,8 +1000,12 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
     for (int a = 0; a < 15; ++a) b->comps[a] = (char*)b->field_arena + b->esz * b->ld * (6 + a);
     if (cudaMalloc(&b->xyz, 8 * b->ld8 * 4) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     b->cellfix = (long long*)(b->xyz + 3 * b->ld8);
-    if (!b->prec && cudaMalloc(&b->cellrel, sizeof(float) * 24 * (size_t)n) != cudaSuccess)
-        return cleanup(LSM_ERR_CUDA);
+    // a cache (the volume kernels form the same values per use without it):
+    // left out when it does not fit
+    if (!b->prec && cudaMalloc(&b->cellrel, sizeof(float) * 24 * (size_t)n) != cudaSuccess) {
+        cudaGetLastError();
+        b->cellrel = nullptr;
+    }
     if (cudaMalloc(&b->staging, sizeof(double) * 4 * b->max_inst_nodes) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->d_inst, sizeof(Inst) * ninst) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->d_offs, sizeof(long long) * (ninst + 1)) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
