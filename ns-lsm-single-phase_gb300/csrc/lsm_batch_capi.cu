@@ -1001,10 +1001,14 @@ int lsm_batch_create(lsm_batch_handle* out, int device, void* stream, int ninst,
     if (cudaMalloc(&b->xyz, 8 * b->ld8 * 4) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     b->cellfix = (long long*)(b->xyz + 3 * b->ld8);
     // a cache (the volume kernels form the same values per use without it):
-    // left out when it does not fit
-    if (!b->prec && cudaMalloc(&b->cellrel, sizeof(float) * 24 * (size_t)n) != cudaSuccess) {
-        cudaGetLastError();
-        b->cellrel = nullptr;
+    // left out when it does not fit, or with LSM_BATCH_CELLREL=0 (A/B runs)
+    {
+        const char* e = std::getenv("LSM_BATCH_CELLREL");
+        if (!b->prec && !(e && !std::strcmp(e, "0")) &&
+            cudaMalloc(&b->cellrel, sizeof(float) * 24 * (size_t)n) != cudaSuccess) {
+            cudaGetLastError();
+            b->cellrel = nullptr;
+        }
     }
     if (cudaMalloc(&b->staging, sizeof(double) * 4 * b->max_inst_nodes) != cudaSuccess) return cleanup(LSM_ERR_CUDA);
     if (cudaMalloc(&b->d_inst, sizeof(Inst) * ninst) != cudaSuccess) return cleanup(LSM_ERR_CUDA);

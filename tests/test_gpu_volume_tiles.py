@@ -70,3 +70,48 @@ def test_scan_volume_fp32_batch_within_fp32_rounding(oracle, lib_built):
     v, ref = _batch_volumes(oracle, SHAPES, "fp32")
     for k in range(len(SHAPES)):
         assert abs(v[k][3] - ref[k][3]) <= 1e-6 * ref[k][3], (k, v[k], ref[k])
+
+
+def test_cell_coordinate_cache_changes_no_bit(oracle, lib_built):
+    """FP32 batches keep each cell's relative vertex coordinates (a cache of
+    the values the volume kernels would form per use).  With the cache
+    switched off (LSM_BATCH_CELLREL=0, also what a batch that cannot fit it
+    does) the mass-corrected steps, their volumes and the gradients through
+    the correction's reverse are bit-identical."""
+    import os
+    from nslsm.batch import LevelSetBatch
+
+    def run():
+        cases = []
+        for s in SHAPES[:2]:
+            x, y, z, phi = _case(*s)
+            csi, eta, zet, _ = oracle.mg_metrics(O.make_grid(*s), x, y, z)
+            cases.append((s, x, y, z, phi, csi, eta, zet))
+        b = LevelSetBatch([(*s, 2e-3, 5e-3, 2e-2) for s, *_ in cases], RNitermax=2, btype=(1,) * 6, BigPhi=5.0,
+                          mass_correction=True, autotune=False)
+        for k, (s, x, y, z, phi, csi, eta, zet) in enumerate(cases):
+            q = np.zeros((4,) + s, order="F")
+            q[1], q[3] = 0.3, 0.1 * np.sin(2 * np.pi * x)
+            b.set_geometry(k, x, y, z, csi, eta, zet)
+            b.set_velocity(k, q)
+            b.set_phi(k, phi)
+        v0 = b.water_volume()
+        for k in range(len(cases)):
+            b.set_mass_target(k, 1.001 * v0[k, 3])
+        b.forward_record(3, 2)
+        out = [b.water_volume()] + [b.get_phi(k) for k in range(len(cases))]
+        for k, (s, *_rest) in enumerate(cases):
+            b.set_grad_phi(k, np.asfortranarray(np.random.default_rng(k).standard_normal(s)))
+        b.backward()
+        out += [b.get_grad_phi0(k) for k in range(len(cases))]
+        b.close()
+        return out
+
+    with_cache = run()
+    os.environ["LSM_BATCH_CELLREL"] = "0"
+    try:
+        without = run()
+    finally:
+        del os.environ["LSM_BATCH_CELLREL"]
+    for a, c in zip(with_cache, without):
+        assert np.array_equal(a, c)
